@@ -1,0 +1,432 @@
+#!/usr/bin/env python3
+"""Benchmark of the relational-operator hot path on GB300.
+
+Headline workload (the configuration the metric is quoted on): group-by
+aggregation and fused filter_aggregation over 64M rows -- int32 key Zipf(1.0)
+over 1M groups, int32 value uniform [0, 1000), SUM as int64 plus COUNT; the
+fused variant keeps rows with value2 < 500.  One step = both operators over
+the batch, output in key order (the reference's group-by order).  `value` is
+input rows per second summed over the two operators, inputs resident in HBM;
+`e2e` is the same metric through the public API with host inputs copied in
+and results copied out every step.  Per-operator lines for the filter
+(16M rows) and the join + filter + sort (R 16M, S 256M) are in `operators`.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the CPU restatement of the reference operators runs on
+the host cores (all threads) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_ROWS = 1 << 26
+GROUPS = 1 << 20
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(s[1]) for s in self.samples if num(s[1]) is not None]
+        smax = [num(s[2]) for s in self.samples if num(s[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[5 + i].lower() == "active"})
+        power = [num(s[3]) for s in self.samples if num(s[3]) is not None]
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(self.samples),
+                "power_w_max": max(power) if power else None}
+
+
+def dist_init(n_gpus):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU restatement of the reference operators on host cores
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import numpy as np
+
+    from oracle import oracle as orc
+    from query_on_opencl_fpga_gb300 import datagen
+
+    orc.lib()
+    threads = orc.threads()
+    sample = 1 << 23  # 8M rows per operator per step keeps a 13-step run to about a minute
+    d = datagen.config1_groupby(sample, GROUPS, seed=0)
+    key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
+
+    def step():
+        orc.groupby_cols(key, val, None, d["lo2"], d["hi2"], cap=GROUPS * 2, mt=True)
+        orc.groupby_cols(key, val, val2, d["lo2"], d["hi2"], cap=GROUPS * 2, mt=True)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = (time.perf_counter() - t0) / args.steps
+    value = 2 * sample / dt
+    line = {
+        "impl": "reference", "metric": "rows_per_s", "value": value, "unit": "rows/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
+        "data": "synthetic (seeded; Zipf(1.0) keys over 1M groups, uniform values)",
+        "config": {"workload": "config1 groupby SUM+COUNT + fused filter_aggregation (value2<500), "
+                               "Zipf(1.0) 1M groups; bounded sample of 8M rows per operator per step",
+                   "rows_per_step": 2 * sample},
+        "cpu_baseline": {"value": value, "unit": "rows/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} rows x 2 operators per step (the 64M-row batch, sampled)"},
+        "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference OpenCL CPU runtime unavailable on this box; oracle port of the reference "
+                "operators (oracle/qg_oracle.c, OpenMP) on all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def timed(ctx, fn, steps, warmup, world, stream):
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ctx.timing_report()  # drop warm-up launches
+    ctx.enable_timing(True)
+    launches0 = ctx.launches
+    barrier(world)
+    torch.cuda.synchronize()
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(steps):
+        fn()
+    end.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms = start.elapsed_time(end) / steps
+    kern = ctx.timing_report()
+    ctx.enable_timing(False)
+    return ms, kern, ctx.launches - launches0
+
+
+def roofline(kern, name, bytes_per_launch, peak_gbs, traffic=None):
+    cnt, tot = kern.get(name, (0, 0.0))
+    if cnt == 0:
+        return None
+    avg_ms = tot / cnt
+    achieved = bytes_per_launch / (avg_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+            "frac": achieved / peak_gbs, "traffic": traffic, "avg_launch_ms": avg_ms,
+            "algorithmic_bytes_per_launch": bytes_per_launch}
+
+
+def cpu_baseline_groupby(d_host, sample):
+    import numpy as np
+
+    from oracle import oracle as orc
+
+    orc.lib()
+    key, val, val2 = (d_host["key"][:sample], d_host["val"][:sample], d_host["val2"][:sample])
+    key, val, val2 = [np.ascontiguousarray(x) for x in (key, val, val2)]
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        orc.groupby_cols(key, val, None, -(2 ** 31), 499, cap=GROUPS * 2, mt=True)
+        orc.groupby_cols(key, val, val2, -(2 ** 31), 499, cap=GROUPS * 2, mt=True)
+        reps += 1
+        if time.perf_counter() - t0 > 8.0 or reps >= 5:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": 2 * sample / dt, "unit": "rows/s", "cores": orc.threads(), "kind": "port",
+            "sample": f"first {sample} rows of the batch, both operators, {reps} reps"}
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    from query_on_opencl_fpga_gb300 import datagen
+    from query_on_opencl_fpga_gb300.api import QG_ORDER_KEY, QG_ORDER_NONE, Context
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    peaks, peak_kind = load_peaks()
+    peak = float(peaks["hbm_gbs"])
+    ctx = Context(stream)
+
+    d = datagen.config1_groupby(N_ROWS, GROUPS, seed=rank, device="cuda")
+    key, val, val2, lo2, hi2 = d["key"], d["val"], d["val2"], d["lo2"], d["hi2"]
+    cap = GROUPS * 2
+
+    def step():
+        ctx.groupby_cols(key, val, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+        ctx.groupby_cols(key, val, val2, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms, kern, launches = timed(ctx, step, args.steps, args.warmup, world, stream)
+    clocks.stop()
+    ms = max_over_ranks(ms, world)
+    rows_per_step = 2 * N_ROWS
+    value = rows_per_step * world / (ms * 1e-3)
+
+    # dominant kernel: the hash aggregation (plain or fused, whichever takes longer in total)
+    names = {"k_groupby_hash": N_ROWS * 8, "k_groupby_hash_fused": N_ROWS * 12}
+    dom = max(names, key=lambda n: kern.get(n, (0, 0.0))[1])
+    roof = roofline(kern, dom, names[dom], peak)
+    traffic_path = ROOT / "profiles" / "traffic.json"
+    if roof and traffic_path.exists():
+        roof["traffic"] = json.loads(traffic_path.read_text()).get(dom)
+    roof_other = {n: roofline(kern, n, b, peak) for n, b in names.items()}
+    total_ms = sum(t for _, t in kern.values()) / args.steps
+
+    # e2e through the public API: pinned host inputs in, results out, every step
+    hkey = key.cpu().pin_memory()
+    hval = val.cpu().pin_memory()
+    hval2 = val2.cpu().pin_memory()
+    dkey, dval, dval2 = torch.empty_like(key), torch.empty_like(val), torch.empty_like(val2)
+    out_bytes = [0]
+
+    def e2e_step():
+        dkey.copy_(hkey, non_blocking=True)
+        dval.copy_(hval, non_blocking=True)
+        dval2.copy_(hval2, non_blocking=True)
+        r1 = ctx.groupby_cols(dkey, dval, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+        r2 = ctx.groupby_cols(dkey, dval, dval2, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+        nb = 0
+        for t in (*r1, *r2):
+            h = t.cpu()
+            nb += h.numel() * h.element_size()
+        out_bytes[0] = nb
+
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) / e2e_steps * 1e3, world)
+    e2e = {"value": rows_per_step * world / (e2e_ms * 1e-3), "unit": "rows/s",
+           "h2d_bytes_per_step": 3 * N_ROWS * 4, "d2h_bytes_per_step": out_bytes[0], "ms_per_step": e2e_ms}
+
+    ops = {}
+    if not args.no_operators and rank == 0:
+        ops = operator_lines(ctx, args, peak, stream)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        host = {"key": hkey.numpy(), "val": hval.numpy(), "val2": hval2.numpy()}
+        cpu = cpu_baseline_groupby(host, 1 << 23)
+
+    if rank == 0:
+        line = {
+            "metric": "rows_per_s", "value": value, "unit": "rows/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32 in, int64 SUM/COUNT", "data": "synthetic (seeded)",
+            "config": {"workload": "config1: groupby SUM(int64)+COUNT and fused filter_aggregation "
+                                   "(value2<500), 64M rows, key Zipf(1.0) over 1M groups, output in key order",
+                       "rows_per_step": rows_per_step, "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs 768 MB per step > 129 MB L2 (no flush needed)"},
+            "roofline": roof, "roofline_kernels": roof_other, "peak_kind": peak_kind,
+            "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kern.items()},
+            "kernel_sum_ms_per_step": total_ms,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
+            "operators": ops,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def operator_lines(ctx, args, peak, stream):
+    """Per-operator rows/s and roofline for the filter and join configurations."""
+    import torch
+
+    from query_on_opencl_fpga_gb300 import datagen
+    from query_on_opencl_fpga_gb300.api import QG_ORDER_NONE
+
+    out = {}
+    steps = max(3, min(args.steps, 10))
+    # config 0: filter 16M rows
+    f = datagen.config0_filter(1 << 24, seed=0, device="cuda")
+    n = f["key"].numel()
+    res = {}
+
+    def fstep():
+        res["o"] = ctx.filter_cols(f["key"], f["payload"], f["lo"], f["hi"])
+
+    ms, kern, _ = timed(ctx, fstep, steps, 3, 1, stream)
+    sel = res["o"].shape[0]
+    out["filter_config0"] = {"rows_per_s": n / (ms * 1e-3), "ms_per_op": ms, "rows": n, "selected": sel,
+                             "roofline": roofline(kern, "k_filter_cols", n * 8 + sel * 8, peak)}
+    del f, res
+    # config 1 unordered variants
+    d = datagen.config1_groupby(N_ROWS, GROUPS, seed=0, device="cuda")
+
+    def gstep():
+        ctx.groupby_cols(d["key"], d["val"], None, d["lo2"], d["hi2"], cap=GROUPS * 2, order=QG_ORDER_NONE)
+
+    ms, kern, _ = timed(ctx, gstep, steps, 3, 1, stream)
+    out["groupby_config1_unordered"] = {"rows_per_s": N_ROWS / (ms * 1e-3), "ms_per_op": ms,
+                                        "op_frac_of_peak": (N_ROWS * 8 + GROUPS * 20) / (ms * 1e-3) / 1e9 / peak,
+                                        "roofline": roofline(kern, "k_groupby_hash", N_ROWS * 8, peak)}
+
+    def fgstep():
+        ctx.groupby_cols(d["key"], d["val"], d["val2"], d["lo2"], d["hi2"], cap=GROUPS * 2, order=QG_ORDER_NONE)
+
+    ms, kern, _ = timed(ctx, fgstep, steps, 3, 1, stream)
+    out["filter_groupby_config1_unordered"] = {
+        "rows_per_s": N_ROWS / (ms * 1e-3), "ms_per_op": ms,
+        "op_frac_of_peak": (N_ROWS * 12 + GROUPS * 20) / (ms * 1e-3) / 1e9 / peak,
+        "roofline": roofline(kern, "k_groupby_hash_fused", N_ROWS * 12, peak)}
+    del d
+    torch.cuda.empty_cache()
+    # config 2: join + filter + sort
+    j = datagen.config2_join(1 << 24, 1 << 28, seed=0, device="cuda")
+    res = {}
+
+    def jstep():
+        res["o"] = ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"], j["shi"],
+                                        cap=70_000_000)
+
+    ms, kern, _ = timed(ctx, jstep, steps, 2, 1, stream)
+    m = res["o"][0].numel()
+    nR, nS = 1 << 24, 1 << 28
+    alg = nR * 8 + nS * 8 + m * 12 + 2 * m * 12
+    out["join_config2"] = {"rows_per_s": nS / (ms * 1e-3), "ms_per_op": ms, "out_rows": m,
+                           "op_frac_of_peak": alg / (ms * 1e-3) / 1e9 / peak,
+                           "kernels_ms": {k: v[1] / steps for k, v in kern.items()},
+                           "roofline_probe": roofline(kern, "k_join_probe", nS * 8 + m * 12, peak)}
+    del j, res
+    torch.cuda.empty_cache()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-operators", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, rank, int(os.environ.get("WORLD_SIZE", "1")))
+        return
+    rank, world, local = dist_init(args.gpus)
+    run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

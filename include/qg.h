@@ -1,0 +1,157 @@
+/*
+ * qg.h -- C ABI of the GB300-native relational-operator library (libqg.so).
+ *
+ * Plain pointers and sizes only.  All data pointers are DEVICE pointers unless
+ * a parameter says "host".  Every entry point returns a qg_status; none calls
+ * exit().  Work is enqueued on the context's CUDA stream; entry points whose
+ * result count is returned through a host pointer synchronise that stream,
+ * the "_async" forms write the count to a device int64 instead.
+ *
+ * Record layout follows the reference: Record = uint2 {x, y}, y = key,
+ * x = payload / row id (host/host/common.h:27-28).  Range predicates are
+ * inclusive and signed, as in filterImpl_map_kernel
+ * (kernel/filter/filter_op.cl:19-21).
+ */
+#ifndef QG_H
+#define QG_H
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QG_API __attribute__((visibility("default")))
+
+typedef enum {
+    QG_OK = 0,
+    QG_ERR_INVALID = 1,     /* bad argument (null pointer, negative size, misalignment) */
+    QG_ERR_CUDA = 2,        /* a CUDA runtime call failed; see qg_last_error_message */
+    QG_ERR_CAPACITY = 3,    /* output larger than the capacity given; *out_n holds the size needed */
+    QG_ERR_TABLE_FULL = 4,  /* hash table probe gave up (more distinct keys than the table holds) */
+    QG_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up (look-back or pipeline barrier) */
+    QG_ERR_OOM = 6,         /* device scratch allocation failed */
+    QG_ERR_UNSUPPORTED = 7  /* size or option outside what the operator supports */
+} qg_status;
+
+/* Aggregation operators, same numbering as the reference (host/host/common.h:89-92). */
+enum { QG_REDUCE_SUM = 0, QG_REDUCE_MAX = 1, QG_REDUCE_MIN = 2, QG_REDUCE_AVERAGE = 3 };
+
+/* Output order of the column group-by. */
+enum { QG_ORDER_NONE = 0, QG_ORDER_KEY = 1 };
+
+typedef struct qg_ctx qg_ctx;
+
+/* ---- context --------------------------------------------------------- */
+/* One context per host thread of use; separate contexts are independent.
+ * `stream` is a cudaStream_t (NULL = the legacy default stream).  The device
+ * is the one current on the calling thread. */
+QG_API qg_status qg_ctx_create(qg_ctx **out, void *stream);
+QG_API qg_status qg_ctx_destroy(qg_ctx *ctx);
+QG_API qg_status qg_ctx_set_stream(qg_ctx *ctx, void *stream);
+QG_API qg_status qg_ctx_sync(qg_ctx *ctx);
+/* Device-side waits give up after this many polls and report QG_ERR_TIMEOUT. */
+QG_API qg_status qg_ctx_set_spin_limit(qg_ctx *ctx, uint32_t polls);
+/* Reads and clears the device error word; returns QG_OK or the first error
+ * any kernel of this context recorded since the last check.  Synchronises. */
+QG_API qg_status qg_ctx_check(qg_ctx *ctx);
+QG_API const char *qg_status_string(qg_status s);
+QG_API const char *qg_last_error_message(qg_ctx *ctx);
+/* Bytes of scratch the context currently holds. */
+QG_API size_t qg_ctx_scratch_bytes(qg_ctx *ctx);
+/* Reserve scratch up front (so later calls allocate nothing). */
+QG_API qg_status qg_ctx_reserve(qg_ctx *ctx, size_t bytes);
+/* Number of kernels this context has launched (for launch accounting). */
+QG_API uint64_t qg_ctx_launch_count(qg_ctx *ctx);
+/* Per-kernel timing: with timing on, CUDA events on the context's stream
+ * bracket every kernel launch (up to 512 between reports).  The report
+ * synchronises, writes one "kernel_name launches total_ms" line per kernel
+ * into buf and clears the log; it returns the number of lines or -1.  The
+ * reference timed stages with host wall-clock around clFinish
+ * (host/host/testFilter.cpp:110-141); this measures device time. */
+QG_API qg_status qg_ctx_enable_timing(qg_ctx *ctx, int on);
+QG_API int qg_ctx_timing_report(qg_ctx *ctx, char *buf, size_t len);
+
+/* Device buffers handed out by callee-allocates entry points. */
+QG_API qg_status qg_malloc(qg_ctx *ctx, void **ptr, size_t bytes);
+QG_API qg_status qg_free(qg_ctx *ctx, void *ptr);
+
+/* ---- filter (kernel/filter/filter_op.cl) ----------------------------- */
+/* Stable range selection over Records: keeps in[i] when lo <= (int)in[i].y <= hi,
+ * in input order.  Replaces filterImpl_map_kernel + ScanLargeArrays/prefixSum/
+ * blockAddition + filterImpl_outSize + filterImpl_write
+ * (kernel/filter/filter_op.cl:6-238, host/host/testFilter.cpp:92-154) with one
+ * single-pass kernel.  `out` holds `cap` records. */
+QG_API qg_status qg_filter_range_rec(qg_ctx *ctx, const void *in_records, int64_t n, int32_t lo,
+                                     int32_t hi, void *out_records, int64_t cap, int64_t *out_n);
+QG_API qg_status qg_filter_range_rec_async(qg_ctx *ctx, const void *in_records, int64_t n,
+                                           int32_t lo, int32_t hi, void *out_records, int64_t cap,
+                                           int64_t *d_out_n);
+/* Column form (config 0): keeps row i when lo <= key[i] <= hi and writes the
+ * int32 pair (i, payload[i]) in input order.  `out_pairs` holds `cap` pairs. */
+QG_API qg_status qg_filter_cols(qg_ctx *ctx, const int32_t *key, const int32_t *payload, int64_t n,
+                                int32_t lo, int32_t hi, int32_t *out_pairs, int64_t cap,
+                                int64_t *out_n);
+QG_API qg_status qg_filter_cols_async(qg_ctx *ctx, const int32_t *key, const int32_t *payload,
+                                      int64_t n, int32_t lo, int32_t hi, int32_t *out_pairs,
+                                      int64_t cap, int64_t *d_out_n);
+
+/* ---- scan (ScanLargeArrays/prefixSum/blockAddition, host/host/testScan.cpp:278-340) */
+/* Exclusive int32 prefix sum with two's-complement wrap; in == out allowed. */
+QG_API qg_status qg_scan_excl_i32(qg_ctx *ctx, const int32_t *in, int32_t *out, int64_t n);
+
+/* ---- sort (bitonicSortShared/bitonicMergeGlobal, host/host/testSort.cpp:24-136) */
+/* Ascending sort of Records by .y as unsigned, in place.  Order among equal
+ * keys is unspecified, as in the reference. */
+QG_API qg_status qg_sort_rec_by_y(qg_ctx *ctx, void *records, int64_t n);
+
+/* ---- group-by on Records (host/host/testGroupBy.cpp:81-154) ---------- */
+/* Sorts `in` by key into `sorted_out` (may equal `in`), then writes the first
+ * row index of each group to startPos (capacity `cap_groups`) and the group
+ * count to *num_groups. */
+QG_API qg_status qg_groupby_rec(qg_ctx *ctx, const void *in_records, int64_t n, void *sorted_out,
+                                int32_t *startPos, int64_t cap_groups, int64_t *num_groups);
+/* parallelAggregate_kernel (kernel/aggregation/1/group_by_cu_op_dp.cl:547-716):
+ * agg[g] = op over .x of rows [startPos[g], startPos[g+1] or n) of sorted records. */
+QG_API qg_status qg_aggregate_groups(qg_ctx *ctx, const void *sorted_records, int64_t n,
+                                     const int32_t *startPos, int64_t num_groups, int op,
+                                     int32_t *agg);
+
+/* ---- column group-by + aggregate, optionally fused with a filter (configs 1, 1-fused)
+ * Groups rows by key, SUM(val) as int64 and COUNT as int64.  When val2 is not
+ * NULL only rows with lo2 <= val2[i] <= hi2 take part (the fused
+ * filter_aggregation pipeline, kernel/filter_aggregation/
+ * filter_aggregation_cu_op_dp.cl).  Outputs hold `cap` groups; order is
+ * QG_ORDER_KEY (ascending unsigned key, the reference's sorted order) or
+ * QG_ORDER_NONE. */
+QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, const int32_t *val,
+                                 const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
+                                 int32_t *gkey, int64_t *gsum, int64_t *gcount, int64_t cap,
+                                 int order, int64_t *num_groups);
+QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key, const int32_t *val,
+                                       const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
+                                       int32_t *gkey, int64_t *gsum, int64_t *gcount, int64_t cap,
+                                       int order, int64_t *d_num_groups);
+
+/* ---- hash join + filter + sort (config 2; kernel/hj_filter_sort/1/hj_filter_sort_op.cl)
+ * Inner equi-join of R(rkey, rpay) and S(skey, spay) on uint key equality,
+ * keeping only S rows with slo <= spay <= shi, every match emitted (duplicate
+ * build keys allowed).  Output columns (key, R.payload, S.payload) sorted
+ * ascending by key (unsigned); order among equal keys unspecified. */
+QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay,
+                                     int64_t nR, const int32_t *skey, const int32_t *spay,
+                                     int64_t nS, int32_t slo, int32_t shi, int32_t *out_key,
+                                     int32_t *out_rpay, int32_t *out_spay, int64_t cap,
+                                     int64_t *out_n);
+/* Reference layout (buildHashTable/probeHashTable, hj_filter_sort_op.cl:25-109):
+ * r and s are interleaved uint (key, val) pairs; every match writes the pair
+ * (S.val, R.val).  Compacted output (the reference leaves holes); order
+ * unspecified. */
+QG_API qg_status qg_hash_join_ref(qg_ctx *ctx, const uint32_t *r_pairs, int64_t nR,
+                                  const uint32_t *s_pairs, int64_t nS, uint32_t *out_pairs,
+                                  int64_t cap, int64_t *out_n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QG_H */

@@ -1,0 +1,208 @@
+"""Torch-tensor front end over the C ABI (include/qg.h).
+
+Device memory and streams come from PyTorch; every operator runs in libqg.so.
+Records are int32 tensors of shape (n, 2) holding the reference's uint2
+{x, y} (y = key, x = payload / row id; host/host/common.h:27-28).
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_int64, c_void_p
+
+import torch
+
+from . import _lib
+from ._lib import QGError, QG_ERR_CAPACITY, QG_ORDER_KEY, QG_ORDER_NONE
+
+INT32_MIN = -(2 ** 31)
+INT32_MAX = 2 ** 31 - 1
+
+
+def _ptr(t: torch.Tensor | None) -> c_void_p:
+    if t is None:
+        return c_void_p(0)
+    return c_void_p(t.data_ptr())
+
+
+def _check_dev(*ts: torch.Tensor | None) -> None:
+    for t in ts:
+        if t is None:
+            continue
+        if not t.is_cuda:
+            raise ValueError("operator inputs must be CUDA tensors")
+        if not t.is_contiguous():
+            raise ValueError("operator inputs must be contiguous")
+
+
+class Context:
+    """A qg_ctx bound to a CUDA stream (default: torch's current stream)."""
+
+    def __init__(self, stream: torch.cuda.Stream | None = None):
+        self.lib = _lib.load()
+        self.stream = stream or torch.cuda.current_stream()
+        h = c_void_p()
+        st = self.lib.qg_ctx_create(byref(h), c_void_p(self.stream.cuda_stream))
+        if st != 0:
+            raise QGError(st, "qg_ctx_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.qg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st: int, where: str) -> None:
+        if st != 0:
+            msg = self.lib.qg_last_error_message(self.handle).decode(errors="replace")
+            raise QGError(st, where, msg)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.qg_ctx_launch_count(self.handle))
+
+    def enable_timing(self, on: bool = True) -> None:
+        """Bracket every kernel launch with CUDA events on this context's stream."""
+        self.check(self.lib.qg_ctx_enable_timing(self.handle, int(on)), "qg_ctx_enable_timing")
+
+    def timing_report(self) -> dict[str, tuple[int, float]]:
+        """{kernel name: (launches, total ms)} since the last report; clears the log."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        k = self.lib.qg_ctx_timing_report(self.handle, buf, len(buf))
+        if k < 0:
+            raise QGError(2, "qg_ctx_timing_report")
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split()
+            out[name] = (int(cnt), float(ms))
+        return out
+
+    def set_spin_limit(self, polls: int) -> None:
+        self.check(self.lib.qg_ctx_set_spin_limit(self.handle, polls), "qg_ctx_set_spin_limit")
+
+    def sync(self) -> None:
+        self.check(self.lib.qg_ctx_sync(self.handle), "qg_ctx_sync")
+
+    def device_check(self) -> None:
+        self.check(self.lib.qg_ctx_check(self.handle), "qg_ctx_check")
+
+    # ---- filter ---------------------------------------------------------
+    def filter_range_rec(self, rec: torch.Tensor, lo: int, hi: int, cap: int | None = None):
+        """Stable selection of records with lo <= (int)y <= hi (filterImpl)."""
+        _check_dev(rec)
+        n = rec.shape[0]
+        cap = n if cap is None else cap
+        out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=rec.device)
+        cnt = c_int64()
+        st = self.lib.qg_filter_range_rec(self.handle, _ptr(rec), n, lo, hi, _ptr(out), cap, byref(cnt))
+        self.check(st, "qg_filter_range_rec")
+        return out[: cnt.value]
+
+    def filter_cols(self, key: torch.Tensor, pay: torch.Tensor, lo: int, hi: int,
+                    cap: int | None = None):
+        """Rows with lo <= key <= hi as int32 (row_id, payload) pairs, input order."""
+        _check_dev(key, pay)
+        n = key.numel()
+        cap = n if cap is None else cap
+        out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=key.device)
+        cnt = c_int64()
+        st = self.lib.qg_filter_cols(self.handle, _ptr(key), _ptr(pay), n, lo, hi, _ptr(out), cap,
+                                     byref(cnt))
+        self.check(st, "qg_filter_cols")
+        return out[: cnt.value]
+
+    # ---- scan / sort ------------------------------------------------------
+    def scan_excl(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        _check_dev(x)
+        out = torch.empty_like(x) if out is None else out
+        self.check(self.lib.qg_scan_excl_i32(self.handle, _ptr(x), _ptr(out), x.numel()), "qg_scan_excl_i32")
+        return out
+
+    def sort_rec(self, rec: torch.Tensor) -> torch.Tensor:
+        """In-place ascending sort of records by unsigned y."""
+        _check_dev(rec)
+        self.check(self.lib.qg_sort_rec_by_y(self.handle, _ptr(rec), rec.shape[0]), "qg_sort_rec_by_y")
+        return rec
+
+    # ---- group-by ---------------------------------------------------------
+    def groupby_rec(self, rec: torch.Tensor, sorted_out: torch.Tensor | None = None):
+        """Sort by key, return (sorted records, startPos[numGroups])."""
+        _check_dev(rec)
+        n = rec.shape[0]
+        sorted_out = torch.empty_like(rec) if sorted_out is None else sorted_out
+        sp = torch.empty(max(n, 1), dtype=torch.int32, device=rec.device)
+        g = c_int64()
+        st = self.lib.qg_groupby_rec(self.handle, _ptr(rec), n, _ptr(sorted_out), _ptr(sp), n, byref(g))
+        self.check(st, "qg_groupby_rec")
+        return sorted_out, sp[: g.value]
+
+    def aggregate_groups(self, sorted_rec: torch.Tensor, start_pos: torch.Tensor, op: int):
+        _check_dev(sorted_rec, start_pos)
+        g = start_pos.numel()
+        agg = torch.empty(max(g, 1), dtype=torch.int32, device=sorted_rec.device)
+        st = self.lib.qg_aggregate_groups(self.handle, _ptr(sorted_rec), sorted_rec.shape[0],
+                                          _ptr(start_pos), g, op, _ptr(agg))
+        self.check(st, "qg_aggregate_groups")
+        return agg[:g]
+
+    def groupby_cols(self, key, val, val2=None, lo2: int = INT32_MIN, hi2: int = INT32_MAX,
+                     cap: int = 1 << 20, order: int = QG_ORDER_KEY):
+        """Per-group (key, SUM(val) int64, COUNT int64), optionally only rows with lo2<=val2<=hi2."""
+        _check_dev(key, val, val2)
+        n = key.numel()
+        dev = key.device
+        gk = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+        gs = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+        gc = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+        g = c_int64()
+        st = self.lib.qg_groupby_cols(self.handle, _ptr(key), _ptr(val), _ptr(val2), lo2, hi2, n,
+                                      _ptr(gk), _ptr(gs), _ptr(gc), cap, order, byref(g))
+        self.check(st, "qg_groupby_cols")
+        return gk[: g.value], gs[: g.value], gc[: g.value]
+
+    # ---- join ---------------------------------------------------------------
+    def join_filter_sort(self, rkey, rpay, skey, spay, slo: int = INT32_MIN, shi: int = INT32_MAX,
+                         cap: int | None = None):
+        """(key, R.payload, S.payload) of R join S on key, S filtered on payload, sorted by key."""
+        _check_dev(rkey, rpay, skey, spay)
+        nR, nS = rkey.numel(), skey.numel()
+        dev = skey.device
+        if cap is None:
+            cap = nS
+        while True:
+            ok = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+            orp = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+            osp = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+            m = c_int64()
+            st = self.lib.qg_join_filter_sort(self.handle, _ptr(rkey), _ptr(rpay), nR, _ptr(skey),
+                                              _ptr(spay), nS, slo, shi, _ptr(ok), _ptr(orp), _ptr(osp),
+                                              cap, byref(m))
+            if st == QG_ERR_CAPACITY and m.value > cap:
+                cap = m.value
+                continue
+            self.check(st, "qg_join_filter_sort")
+            return ok[: m.value], orp[: m.value], osp[: m.value]
+
+    def hash_join_ref(self, r_pairs: torch.Tensor, s_pairs: torch.Tensor, cap: int | None = None):
+        """Reference-layout join: (key, val) pairs in, (S.val, R.val) pairs out."""
+        _check_dev(r_pairs, s_pairs)
+        nR, nS = r_pairs.shape[0], s_pairs.shape[0]
+        cap = nS if cap is None else cap
+        while True:
+            out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=s_pairs.device)
+            m = c_int64()
+            st = self.lib.qg_hash_join_ref(self.handle, _ptr(r_pairs), nR, _ptr(s_pairs), nS,
+                                           _ptr(out), cap, byref(m))
+            if st == QG_ERR_CAPACITY and m.value > cap:
+                cap = m.value
+                continue
+            self.check(st, "qg_hash_join_ref")
+            return out[: m.value]
+
+
+__all__ = ["Context", "QGError", "QG_ORDER_KEY", "QG_ORDER_NONE", "INT32_MIN", "INT32_MAX"]

@@ -1,0 +1,269 @@
+// qg_internal.cuh -- context, scratch arena and device helpers shared by all
+// operator translation units of libqg.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include "qg.h"
+
+// ---------------------------------------------------------------------------
+// Device-resident control block (one per context).
+// ---------------------------------------------------------------------------
+struct qg_control {
+    int32_t err;        // first error code recorded by any kernel (0 = none)
+    int32_t err_site;   // which kernel recorded it
+    uint32_t epoch;     // look-back epoch; status words of older launches are stale
+    uint32_t tile_ctr;  // dynamic tile counter of the running single-pass kernel
+    uint32_t done_ctr;  // finished CTAs of the running single-pass kernel
+    uint32_t pad0;
+    unsigned long long counter[6];  // scratch counters (output cursors)
+};
+
+struct qg_ctx {
+    cudaStream_t stream;
+    int device;
+    int sm_count;
+    char *scratch;          // grow-only arena for per-call temporaries
+    size_t scratch_bytes;
+    char *table;            // grow-only hash-table arena; kept all-zero between calls
+    size_t table_bytes;
+    char *aux;              // grow-only arena for operator temporaries that must
+    size_t aux_bytes;       //   survive nested calls (e.g. a sort inside group-by)
+    qg_control *ctl;        // device
+    long long *pinned;      // host pinned readback slots (8)
+    uint32_t spin_limit;
+    uint64_t launches;
+    bool table_dirty;       // group-by table must be cleared before next use
+    char msg[256];
+    // Per-kernel CUDA-event timing (qg_ctx_enable_timing): a pair of events
+    // brackets every launch on the context's stream.
+    bool timing;
+    int ev_used;
+    cudaEvent_t ev[2 * 512];
+    const char *ev_name[512];
+};
+
+// Record the start event of the next launch (no-op unless timing is on).
+void qg_pre_launch(qg_ctx *ctx);
+
+// Site tags for the error word.
+enum {
+    QG_SITE_FILTER = 1, QG_SITE_SCAN = 2, QG_SITE_SORT = 3, QG_SITE_GROUPBY = 4,
+    QG_SITE_AGG = 5, QG_SITE_JOIN_BUILD = 6, QG_SITE_JOIN_PROBE = 7, QG_SITE_SORT_LOOKBACK = 8
+};
+
+qg_status qg_cuda_fail(qg_ctx *ctx, cudaError_t e, const char *what);
+// Ensure the scratch arena holds at least `bytes`; newly grown memory is zeroed.
+qg_status qg_scratch(qg_ctx *ctx, size_t bytes, char **out);
+// Ensure the operator-temporary arena holds at least `bytes` (not zeroed).
+qg_status qg_aux(qg_ctx *ctx, size_t bytes, char **out);
+// Ensure the hash-table arena holds at least `bytes` of zeroed memory.
+qg_status qg_table(qg_ctx *ctx, size_t bytes, char **out);
+// Copy a device int64 to host (synchronises the stream).
+qg_status qg_read_i64(qg_ctx *ctx, const long long *d, long long *h);
+qg_status qg_check_launch(qg_ctx *ctx, const char *what);
+// Read the device error word after a synchronisation, clear it and map it.
+qg_status qg_collect_error(qg_ctx *ctx);
+
+#define QG_TRY_CUDA(ctx, expr, what)                            \
+    do {                                                        \
+        cudaError_t _e = (expr);                                \
+        if (_e != cudaSuccess) return qg_cuda_fail(ctx, _e, what); \
+    } while (0)
+#define QG_TRY(expr)                        \
+    do {                                    \
+        qg_status _s = (expr);              \
+        if (_s != QG_OK) return _s;         \
+    } while (0)
+
+static inline size_t qg_align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+static inline int64_t qg_ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------------------
+// Device helpers
+// ---------------------------------------------------------------------------
+#define QG_FULL_MASK 0xffffffffu
+
+__device__ __forceinline__ void qg_record_error(qg_control *ctl, int code, int site) {
+    if (atomicCAS(&ctl->err, 0, code) == 0) ctl->err_site = site;
+}
+
+__device__ __forceinline__ unsigned long long qg_ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void qg_st_relaxed_u64(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t qg_ld_relaxed_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void qg_st_relaxed_u32(uint32_t *p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t qg_lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Streaming 128-bit load (read once, do not keep in L1).
+__device__ __forceinline__ int4 qg_ldg_stream(const int4 *p) {
+    int4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+// 32-bit integer mix (murmur3 finaliser constants from the public MurmurHash3).
+__device__ __forceinline__ uint32_t qg_hash32(uint32_t k) {
+    k ^= k >> 16;
+    k *= 0x85ebca6bu;
+    k ^= k >> 13;
+    k *= 0xc2b2ae35u;
+    k ^= k >> 16;
+    return k;
+}
+
+// ---------------------------------------------------------------------------
+// Decoupled look-back (single-pass prefix over tiles).
+//
+// Status word per tile (64 bit): [63:34] epoch, [33:32] flag, [31:0] value.
+// flag 1 = tile aggregate published, flag 2 = inclusive prefix published.
+// A word whose epoch differs from the running launch's epoch is "not yet
+// written".  Tile ids are handed out by an atomic counter in start order, so
+// every predecessor of a running tile has started and will publish.  The last
+// CTA to finish resets the counters and advances the epoch, so no memset is
+// needed between launches.
+// ---------------------------------------------------------------------------
+struct qg_lookback {
+    unsigned long long *status;
+    qg_control *ctl;
+    uint32_t spin_limit;
+    int site;
+};
+
+#define QG_LB_AGG 1ull
+#define QG_LB_PREFIX 2ull
+
+__device__ __forceinline__ unsigned long long qg_lb_word(uint32_t epoch, unsigned long long flag,
+                                                          uint32_t value) {
+    return ((unsigned long long)epoch << 34) | (flag << 32) | (unsigned long long)value;
+}
+
+// Called by all threads of the CTA at kernel start; returns the tile id and
+// the running epoch through shared memory.
+__device__ __forceinline__ void qg_lb_begin(const qg_lookback &lb, uint32_t *s_tile,
+                                            uint32_t *s_epoch) {
+    if (threadIdx.x == 0) {
+        *s_tile = atomicAdd(&lb.ctl->tile_ctr, 1u);
+        *s_epoch = *(volatile uint32_t *)&lb.ctl->epoch;
+    }
+    __syncthreads();
+}
+
+// Called by all threads of warp 0 only.  Publishes the tile aggregate, looks
+// back over predecessors and returns the exclusive prefix of this tile (mod 2^32).
+__device__ __forceinline__ uint32_t qg_lb_warp_exclusive(const qg_lookback &lb, uint32_t tile,
+                                                          uint32_t epoch, uint32_t aggregate) {
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) {
+        if (lane == 0) qg_st_relaxed_u64(&lb.status[0], qg_lb_word(epoch, QG_LB_PREFIX, aggregate));
+        return 0;
+    }
+    if (lane == 0) qg_st_relaxed_u64(&lb.status[tile], qg_lb_word(epoch, QG_LB_AGG, aggregate));
+    uint32_t excl = 0;
+    long long pred = (long long)tile - 1;
+    while (true) {
+        long long j = pred - lane;
+        unsigned long long flag = QG_LB_PREFIX;
+        uint32_t value = 0;
+        if (j >= 0) {
+            uint32_t spins = 0;
+            unsigned long long w;
+            while (true) {
+                w = qg_ld_relaxed_u64(&lb.status[j]);
+                if ((uint32_t)(w >> 34) == (epoch & 0x3fffffffu) && ((w >> 32) & 3ull) != 0) break;
+                if (++spins >= lb.spin_limit) {
+                    qg_record_error(lb.ctl, QG_ERR_TIMEOUT, lb.site);
+                    w = qg_lb_word(epoch, QG_LB_PREFIX, 0);
+                    break;
+                }
+                __nanosleep(32);
+            }
+            flag = (w >> 32) & 3ull;
+            value = (uint32_t)w;
+        }
+        uint32_t pmask = __ballot_sync(QG_FULL_MASK, flag == QG_LB_PREFIX);
+        int stop = pmask ? (__ffs(pmask) - 1) : 31;
+        uint32_t contrib = (lane <= stop) ? value : 0u;
+        excl += __reduce_add_sync(QG_FULL_MASK, contrib);
+        if (pmask) break;
+        pred -= 32;
+    }
+    if (lane == 0)
+        qg_st_relaxed_u64(&lb.status[tile], qg_lb_word(epoch, QG_LB_PREFIX, excl + aggregate));
+    return excl;
+}
+
+// Called by all threads at kernel end: the last CTA resets the counters.
+__device__ __forceinline__ void qg_lb_end(const qg_lookback &lb) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        uint32_t done = atomicAdd(&lb.ctl->done_ctr, 1u);
+        if (done == gridDim.x - 1) {
+            lb.ctl->tile_ctr = 0;
+            lb.ctl->done_ctr = 0;
+            lb.ctl->epoch = (lb.ctl->epoch + 1) & 0x3fffffffu;
+            __threadfence();
+        }
+    }
+}
+
+// Warp 0 of a single-pass compaction tile: exclusive scan of the E per-warp
+// counts in s_woff (in row order), look-back for the tile's output offset,
+// publish the total count from the last tile.  Leaves exclusive offsets in
+// s_woff and the tile offset in *s_excl.
+template <int E>
+__device__ __forceinline__ void qg_tile_compact_offsets(uint32_t *s_woff, const qg_lookback &lb,
+                                                        uint32_t tile, uint32_t epoch,
+                                                        uint32_t *s_excl, long long *d_count) {
+    const int lane = threadIdx.x & 31;
+    constexpr int PER = (E + 31) / 32;
+    uint32_t loc[PER];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        int e = lane * PER + k;
+        loc[k] = (e < E) ? s_woff[e] : 0u;
+        sum += loc[k];
+    }
+    uint32_t incl = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(QG_FULL_MASK, incl, d);
+        if (lane >= d) incl += t;
+    }
+    uint32_t total = __shfl_sync(QG_FULL_MASK, incl, 31);
+    uint32_t run = incl - sum;
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        int e = lane * PER + k;
+        if (e < E) s_woff[e] = run;
+        run += loc[k];
+    }
+    uint32_t excl = qg_lb_warp_exclusive(lb, tile, epoch, total);
+    if (lane == 0) {
+        *s_excl = excl;
+        if (tile == gridDim.x - 1 && d_count) *d_count = (long long)excl + total;
+    }
+}
+
+// Host side: status words needed for `tiles` tiles.
+static inline size_t qg_lb_bytes(int64_t tiles) { return (size_t)tiles * 8; }

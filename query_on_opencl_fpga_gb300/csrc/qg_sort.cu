@@ -1,0 +1,332 @@
+// qg_sort.cu -- LSD radix sort by an unsigned 32-bit key.
+//
+// Replaces the reference's bitonic sort (bitonicSortShared +
+// bitonicMergeGlobal, kernel/aggregation/1/group_by_cu_op_dp.cl:89-291,
+// driven by radixSortImpl_sm, host/host/testSort.cpp:24-136), which needs a
+// power-of-two n >= 2048 and O(n log^2 n) global passes.  Here:
+//   1. one histogram pass counts the 8-bit digits of every key position (or
+//      the producer of the data counted them already, as the join probe does);
+//   2. the host skips digit positions where all keys share one digit;
+//   3. each remaining position is one "onesweep" pass: a tile is ranked by
+//      digit in shared memory (warp ballots give peer masks), its per-digit
+//      global offsets come from a decoupled look-back over earlier tiles, and
+//      the tile is reordered in shared memory so that each digit's run is
+//      written with consecutive addresses.
+// Every pass is stable, so the LSD composition is a correct sort; the order
+// among equal keys is input order (the reference's is unspecified).
+//
+// Two item layouts:
+//   REC: 64-bit items, key = high 32 bits (a Record uint2 {x, y} read as one
+//        little-endian u64 has y in the high word).
+//   KV3: three u32 columns (key, a, b) -- the join output (key, R.payload,
+//        S.payload).
+#include <string.h>
+#include <vector>
+#include "qg_internal.cuh"
+#include "qg_sort.cuh"
+
+namespace {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;  // 4096
+
+constexpr uint32_t ST_AGG = 1u << 30;
+constexpr uint32_t ST_PRE = 2u << 30;
+constexpr uint32_t ST_VAL = (1u << 30) - 1;
+
+__global__ void __launch_bounds__(256)
+k_radix_hist(const uint32_t *__restrict__ kin, const unsigned long long *__restrict__ rin,
+             long long n, uint32_t key_off, int npos, uint32_t *__restrict__ ghist) {
+    __shared__ uint32_t sh[4][QG_RADIX];
+    for (int i = threadIdx.x; i < 4 * QG_RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
+    __syncthreads();
+    long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint32_t k = (kin ? __ldg(kin + i) : (uint32_t)(__ldg(rin + i) >> 32)) - key_off;
+        for (int p = 0; p < npos; p++) atomicAdd(&sh[p][(k >> (8 * p)) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npos * QG_RADIX; i += blockDim.x) {
+        uint32_t c = (&sh[0][0])[i];
+        if (c) atomicAdd(&ghist[i], c);
+    }
+}
+
+template <bool KV3>
+struct RsSmem {
+    uint32_t whist[RS_WARPS][QG_RADIX];
+    uint32_t dstart[QG_RADIX];
+    uint32_t goff[QG_RADIX];
+    uint32_t wsum[RS_WARPS];
+    uint32_t tile;
+    // REC: v holds the u64 items; KV3: v holds (a, b) pairs and k the keys
+    unsigned long long v[RS_TILE];
+    uint32_t k[KV3 ? RS_TILE : 1];
+};
+
+template <bool KV3>
+__global__ void __launch_bounds__(RS_THREADS)
+k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
+             const uint32_t *__restrict__ dbase, uint32_t *__restrict__ status, qg_control *ctl,
+             uint32_t spin_limit) {
+    extern __shared__ __align__(16) unsigned char rs_raw[];
+    RsSmem<KV3> &S = *reinterpret_cast<RsSmem<KV3> *>(rs_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) S.tile = atomicAdd(&ctl->tile_ctr, 1u);
+    for (int i = tid; i < RS_WARPS * QG_RADIX; i += RS_THREADS) (&S.whist[0][0])[i] = 0;
+    __syncthreads();
+    const uint32_t tile = S.tile;
+    const long long base = (long long)tile * RS_TILE;
+    const long long wbase = base + (long long)warp * 32 * RS_ITEMS;
+    const uint32_t lt = qg_lanemask_lt();
+
+    uint32_t key[RS_ITEMS];
+    unsigned long long val[RS_ITEMS];
+    uint32_t rank[RS_ITEMS];
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        long long idx = wbase + i * 32 + lane;
+        bool valid = idx < n;
+        if (valid) {
+            if (KV3) {
+                key[i] = src.k[idx];
+                val[i] = ((unsigned long long)src.b[idx] << 32) | src.a[idx];
+            } else {
+                val[i] = src.rec[idx];
+                key[i] = (uint32_t)(val[i] >> 32);
+            }
+        } else {
+            val[i] = 0;
+            key[i] = 0;
+        }
+        uint32_t d = ((key[i] - key_off) >> shift) & 255u;
+        uint32_t peers = __ballot_sync(QG_FULL_MASK, valid);
+#pragma unroll
+        for (int b = 0; b < 8; b++) {
+            uint32_t bal = __ballot_sync(QG_FULL_MASK, (d >> b) & 1u);
+            peers &= ((d >> b) & 1u) ? bal : ~bal;
+        }
+        uint32_t before = valid ? S.whist[warp][d] : 0u;
+        __syncwarp();
+        if (valid) {
+            rank[i] = before + __popc(peers & lt);
+            if (lane == 31 - __clz(peers)) S.whist[warp][d] = before + __popc(peers);
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        // Thread t owns digit t: offsets of each warp within the digit, the
+        // tile's count of the digit, then its place among the digits.
+        const int t = tid;
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; w++) {
+            uint32_t c = S.whist[w][t];
+            S.whist[w][t] = run;
+            run += c;
+        }
+        const uint32_t total = run;
+        uint32_t inc = total;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            uint32_t x = __shfl_up_sync(QG_FULL_MASK, inc, d);
+            if (lane >= d) inc += x;
+        }
+        if (lane == 31) S.wsum[warp] = inc;
+        __syncthreads();
+        uint32_t woff = 0;
+        for (int w = 0; w < warp; w++) woff += S.wsum[w];
+        const uint32_t dstart = woff + inc - total;
+        S.dstart[t] = dstart;
+
+        // Look-back for digit t over earlier tiles.
+        uint32_t *st = status + (size_t)tile * QG_RADIX + t;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            qg_st_relaxed_u32(st, ST_PRE | total);
+        } else {
+            qg_st_relaxed_u32(st, ST_AGG | total);
+            long long j = (long long)tile - 1;
+            while (j >= 0) {
+                const uint32_t *p = status + (size_t)j * QG_RADIX + t;
+                uint32_t w;
+                uint32_t spins = 0;
+                while (true) {
+                    w = qg_ld_relaxed_u32(p);
+                    if (w & (ST_AGG | ST_PRE)) break;
+                    if (++spins >= spin_limit) {
+                        qg_record_error(ctl, QG_ERR_TIMEOUT, QG_SITE_SORT_LOOKBACK);
+                        w = ST_PRE;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                excl += w & ST_VAL;
+                if (w & ST_PRE) break;
+                j--;
+            }
+            qg_st_relaxed_u32(st, ST_PRE | ((excl + total) & ST_VAL));
+        }
+        S.goff[t] = dbase[t] + excl - dstart;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        long long idx = wbase + i * 32 + lane;
+        if (idx < n) {
+            uint32_t d = ((key[i] - key_off) >> shift) & 255u;
+            uint32_t pos = S.dstart[d] + S.whist[warp][d] + rank[i];
+            S.v[pos] = val[i];
+            if (KV3) S.k[pos] = key[i];
+        }
+    }
+    __syncthreads();
+    long long cnt = n - base;
+    if (cnt > RS_TILE) cnt = RS_TILE;
+    for (int p = tid; p < cnt; p += RS_THREADS) {
+        unsigned long long v = S.v[p];
+        uint32_t k = KV3 ? S.k[p] : (uint32_t)(v >> 32);
+        uint32_t d = ((k - key_off) >> shift) & 255u;
+        uint32_t g = S.goff[d] + (uint32_t)p;
+        if (KV3) {
+            dst.k[g] = k;
+            dst.a[g] = (uint32_t)v;
+            dst.b[g] = (uint32_t)(v >> 32);
+        } else {
+            dst.rec[g] = v;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        uint32_t done = atomicAdd(&ctl->done_ctr, 1u);
+        if (done == gridDim.x - 1) {
+            ctl->tile_ctr = 0;
+            ctl->done_ctr = 0;
+            ctl->epoch = (ctl->epoch + 1) & 0x3fffffffu;
+            __threadfence();
+        }
+    }
+}
+
+}  // namespace
+
+int qg_sort_positions(int bits) {
+    int npos = (bits + 7) / 8;
+    if (npos < 1) npos = 1;
+    if (npos > 4) npos = 4;
+    return npos;
+}
+
+qg_status qg_radix_histogram(qg_ctx *ctx, const qg_sort_bufs &src, bool kv3, long long n,
+                             uint32_t key_off, int npos, uint32_t *d_hist) {
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(d_hist, 0, 4 * QG_RADIX * 4, ctx->stream), "memset hist");
+    if (n == 0) return QG_OK;
+    int hblocks = ctx->sm_count * 4;
+    long long maxb = (n + 255) / 256;
+    if (hblocks > maxb) hblocks = (int)maxb;
+    qg_pre_launch(ctx);
+    k_radix_hist<<<hblocks, 256, 0, ctx->stream>>>(kv3 ? src.k : nullptr, kv3 ? nullptr : src.rec,
+                                                   n, key_off, npos, d_hist);
+    return qg_check_launch(ctx, "k_radix_hist");
+}
+
+int qg_sort_plan(const uint32_t *h_hist, int npos, long long n, int *passes, uint32_t *bases) {
+    int np = 0;
+    for (int p = 0; p < npos; p++) {
+        bool trivial = false;
+        uint32_t run = 0;
+        for (int d = 0; d < QG_RADIX; d++) {
+            uint32_t c = h_hist[p * QG_RADIX + d];
+            if ((long long)c == n) trivial = true;
+            bases[p * QG_RADIX + d] = run;
+            run += c;
+        }
+        if (!trivial) passes[np++] = p;
+    }
+    return np;
+}
+
+qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
+                          uint32_t key_off, const int *passes, int np, const uint32_t *h_bases,
+                          bool *result_in_b) {
+    *result_in_b = false;
+    if (np == 0 || n <= 1) return QG_OK;
+    if (n >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
+    const long long tiles = (n + RS_TILE - 1) / RS_TILE;
+    size_t need = 4 * QG_RADIX * 4 + (size_t)tiles * QG_RADIX * 4;
+    char *scr;
+    QG_TRY(qg_scratch(ctx, need, &scr));
+    uint32_t *dbase = (uint32_t *)scr;
+    uint32_t *status = dbase + 4 * QG_RADIX;
+    // The bases go up through the context's pinned slots area: synchronous
+    // copy of 4 KB, issued in stream order.
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(dbase, h_bases, 4 * QG_RADIX * 4, cudaMemcpyHostToDevice, ctx->stream), "bases h2d");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
+    static bool attr_done[2] = {false, false};
+    if (!attr_done[kv3]) {
+        if (kv3)
+            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RsSmem<true>)), "attr");
+        else
+            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RsSmem<false>)), "attr");
+        attr_done[kv3] = true;
+    }
+    bool in_a = true;
+    for (int i = 0; i < np; i++) {
+        const int p = passes[i];
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(status, 0, (size_t)tiles * QG_RADIX * 4, ctx->stream), "memset status");
+        const qg_sort_bufs &s = in_a ? a : b;
+        const qg_sort_bufs &d = in_a ? b : a;
+        qg_pre_launch(ctx);
+        if (kv3)
+            k_radix_pass<true><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n, 8 * p, key_off, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+        else
+            k_radix_pass<false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n, 8 * p, key_off, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+        QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
+        in_a = !in_a;
+    }
+    *result_in_b = !in_a;
+    return QG_OK;
+}
+
+// Sort REC items in `data` (n u64) using `tmp` (n u64) as the ping-pong
+// buffer; the result ends in `data`.  Synchronises once to plan the passes.
+qg_status qg_sort_rec_inplace(qg_ctx *ctx, unsigned long long *data, unsigned long long *tmp,
+                              long long n) {
+    if (n <= 1) return QG_OK;
+    char *scr;
+    QG_TRY(qg_scratch(ctx, 4 * QG_RADIX * 4, &scr));
+    uint32_t *d_hist = (uint32_t *)scr;
+    qg_sort_bufs a{};
+    a.rec = data;
+    QG_TRY(qg_radix_histogram(ctx, a, false, n, 0u, 4, d_hist));
+    std::vector<uint32_t> h(4 * QG_RADIX), bases(4 * QG_RADIX);
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), d_hist, 4 * QG_RADIX * 4, cudaMemcpyDeviceToHost, ctx->stream), "hist d2h");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    int passes[4];
+    int np = qg_sort_plan(h.data(), 4, n, passes, bases.data());
+    qg_sort_bufs b{};
+    b.rec = tmp;
+    bool in_b = false;
+    QG_TRY(qg_radix_passes(ctx, false, a, b, n, 0u, passes, np, bases.data(), &in_b));
+    if (in_b)
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(data, tmp, (size_t)n * 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+    return QG_OK;
+}
+
+extern "C" QG_API qg_status qg_sort_rec_by_y(qg_ctx *ctx, void *records, int64_t n) {
+    if (!ctx || n < 0 || (n > 0 && !records)) return QG_ERR_INVALID;
+    if (((uintptr_t)records) & 7) return QG_ERR_INVALID;
+    if (n <= 1) return QG_OK;
+    if (n >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
+    char *tmp = nullptr;
+    QG_TRY(qg_aux(ctx, (size_t)n * 8, &tmp));
+    QG_TRY(qg_sort_rec_inplace(ctx, (unsigned long long *)records, (unsigned long long *)tmp, n));
+    return qg_ctx_check(ctx);
+}

@@ -1,0 +1,31 @@
+// qg_sort.cuh -- radix sort building blocks shared by group-by and join.
+#pragma once
+#include "qg_internal.cuh"
+
+constexpr int QG_RADIX = 256;
+
+// Buffers of one side of the ping-pong: REC uses `rec` (u64 items, key in the
+// high word); KV3 uses the three u32 columns k (key), a, b.
+struct qg_sort_bufs {
+    unsigned long long *rec;
+    uint32_t *k;
+    uint32_t *a;
+    uint32_t *b;
+};
+
+// Number of 8-bit digit positions covering `bits` key bits (1..4).
+int qg_sort_positions(int bits);
+// Device histogram of (key - key_off) digits for `npos` positions into d_hist[4][256].
+qg_status qg_radix_histogram(qg_ctx *ctx, const qg_sort_bufs &src, bool kv3, long long n,
+                             uint32_t key_off, int npos, uint32_t *d_hist);
+// From a host copy of the histogram: the non-trivial positions (returned
+// count) and every position's exclusive digit bases.
+int qg_sort_plan(const uint32_t *h_hist, int npos, long long n, int *passes, uint32_t *bases);
+// Run the planned passes, starting in `a` and alternating; *result_in_b tells
+// where the sorted data ended.
+qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
+                          uint32_t key_off, const int *passes, int np, const uint32_t *h_bases,
+                          bool *result_in_b);
+// Sort REC items in place with `tmp` as the second buffer (synchronises once).
+qg_status qg_sort_rec_inplace(qg_ctx *ctx, unsigned long long *data, unsigned long long *tmp,
+                              long long n);

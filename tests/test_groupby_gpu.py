@@ -1,0 +1,121 @@
+"""GPU parity: group-by (sorted contract + per-group aggregates, bit-exact) and
+the column hash group-by with int64 SUM + COUNT, plain and fused with the
+value2 predicate (bit-exact; compared in key order)."""
+import numpy as np
+import pytest
+import torch
+
+from query_on_opencl_fpga_gb300 import datagen
+from query_on_opencl_fpga_gb300.api import QG_ORDER_KEY, QG_ORDER_NONE
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def test_groupby_rec_golden(ctx, orc, golden):
+    meta, arrs = golden
+    c = meta["cases"]["groupby"]
+    rin = orc.generate_rand(64, c["n"], 0)
+    rin[:, 1] = np.mod(rin[:, 1], 64)
+    srt, sp = ctx.groupby_rec(dev(rin))
+    assert np.array_equal(sp.cpu().numpy(), arrs["groupby_startpos"])
+    assert np.array_equal(srt.cpu().numpy()[:, 1], orc.sort_rec(rin)[:, 1])
+
+
+@pytest.mark.parametrize("op,name", [(0, "sum"), (1, "max"), (2, "min"), (3, "avg")])
+def test_aggregate_golden(ctx, orc, golden, op, name):
+    meta, arrs = golden
+    c = meta["cases"]["aggregate"]
+    rin = orc.generate_rand(50, c["n"], 0)
+    rin[:, 1] = np.mod(rin[:, 1], 50)
+    srt, sp = ctx.groupby_rec(dev(rin))
+    agg = ctx.aggregate_groups(srt, sp, op).cpu().numpy()
+    assert np.array_equal(agg, arrs[f"agg_{name}"])
+
+
+@pytest.mark.parametrize("n,groups", [(1, 1), (5, 2), (4097, 7), (100003, 1000), (1 << 20, 40000),
+                                      (300000, 1)])
+@pytest.mark.parametrize("op", [0, 1, 2, 3])
+def test_aggregate_sizes(ctx, orc, n, groups, op):
+    rng = np.random.default_rng(n + op)
+    rin = np.stack([rng.integers(-(2 ** 31), 2 ** 31, n, dtype=np.int64),
+                    rng.integers(0, groups, n)], 1).astype(np.int32)
+    srt, sp = ctx.groupby_rec(dev(rin))
+    srt_h = srt.cpu().numpy()
+    sp_h = sp.cpu().numpy()
+    exp_sorted = orc.sort_rec(rin)
+    assert np.array_equal(srt_h[:, 1], exp_sorted[:, 1])
+    assert np.array_equal(sp_h, orc.group_startpos(exp_sorted))
+    agg = ctx.aggregate_groups(srt, sp, op).cpu().numpy()
+    assert np.array_equal(agg, orc.aggregate_groups(srt_h, sp_h, op))
+
+
+def check_groups(got, exp):
+    gk, gs, gc = [t.cpu().numpy() for t in got]
+    ek, es, ec = exp
+    assert np.array_equal(gk, ek)
+    assert np.array_equal(gs, es)
+    assert np.array_equal(gc, ec)
+
+
+@pytest.mark.parametrize("n,groups,fused", [(1, 1, False), (100, 7, True), (4099, 4099, False),
+                                            (1 << 18, 1 << 12, True), (1 << 20, 1 << 17, False),
+                                            (1 << 20, 1 << 17, True)])
+def test_groupby_cols_small(ctx, orc, n, groups, fused):
+    d = datagen.config1_groupby(n, groups, seed=n)
+    key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
+    v2 = val2 if fused else None
+    got = ctx.groupby_cols(dev(key), dev(val), dev(v2) if fused else None, d["lo2"], d["hi2"],
+                           cap=max(groups, 1) * 2)
+    exp = orc.groupby_cols(key, val, v2, d["lo2"], d["hi2"])
+    check_groups(got, exp)
+
+
+def test_groupby_cols_extreme_values(ctx, orc):
+    # key -1 (all-ones) and INT_MIN/INT_MAX values exercise the shared-memory
+    # sentinel path and the int64 sum.
+    rng = np.random.default_rng(4)
+    n = 1 << 16
+    key = rng.choice(np.array([-1, 0, 1, 2 ** 31 - 1, -(2 ** 31), 12345], np.int32), n)
+    val = rng.choice(np.array([-(2 ** 31), 2 ** 31 - 1, 0, -1], np.int32), n)
+    got = ctx.groupby_cols(dev(key), dev(val), cap=16)
+    check_groups(got, orc.groupby_cols(key, val))
+
+
+def test_groupby_cols_unordered_is_permutation(ctx, orc):
+    d = datagen.config1_groupby(1 << 20, 1 << 15, seed=3)
+    key, val = d["key"].numpy(), d["val"].numpy()
+    gk, gs, gc = ctx.groupby_cols(dev(key), dev(val), cap=1 << 16, order=QG_ORDER_NONE)
+    order = np.argsort(gk.cpu().numpy().view(np.uint32))
+    got = (gk.cpu()[order], gs.cpu()[order], gc.cpu()[order])
+    check_groups(got, orc.groupby_cols(key, val))
+
+
+def test_groupby_cols_capacity(ctx):
+    from query_on_opencl_fpga_gb300 import QGError
+
+    key = torch.arange(5000, dtype=torch.int32, device="cuda")
+    with pytest.raises(QGError) as e:
+        ctx.groupby_cols(key, key, cap=100)
+    assert e.value.status in (3, 4)
+    # usable afterwards (the table is cleared after an error)
+    gk, gs, gc = ctx.groupby_cols(key[:50], key[:50], cap=100)
+    assert gk.numel() == 50 and int(gc.sum()) == 50
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_groupby_config1_full_size(ctx, orc, fused):
+    # Full config-1 size: 64M rows, Zipf(1.0) over 1M groups, bit-exact.
+    d = datagen.config1_groupby(1 << 26, 1 << 20, seed=0, device="cuda")
+    got = ctx.groupby_cols(d["key"], d["val"], d["val2"] if fused else None, d["lo2"], d["hi2"],
+                           cap=1 << 21)
+    key, val, val2 = d["key"].cpu().numpy(), d["val"].cpu().numpy(), d["val2"].cpu().numpy()
+    exp = orc.groupby_cols(key, val, val2 if fused else None, d["lo2"], d["hi2"], cap=1 << 21, mt=True)
+    check_groups(got, exp)
+    # checksum of checksums: total count and sum equal the filtered column sums
+    m = (val2 <= 499) if fused else np.ones(key.size, bool)
+    assert int(got[2].sum()) == int(m.sum())
+    assert int(got[1].sum()) == int(val[m].astype(np.int64).sum())
