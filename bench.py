@@ -270,15 +270,16 @@ def run_ours(args, rank, world, local):
     rows_per_step = 2 * N_ROWS
     value = rows_per_step * world / (ms * 1e-3)
 
-    # dominant kernel: the hash aggregation (plain or fused, whichever takes longer in total)
-    names = {"k_groupby_hash": N_ROWS * 8, "k_groupby_hash_fused": N_ROWS * 12}
+    # dominant kernel: the group-by pass 1 (plain or fused, whichever takes
+    # longer in total); its algorithmic bytes are the input columns it reads.
+    names = {"k_gb_part": N_ROWS * 8, "k_gb_part_fused": N_ROWS * 12}
     dom = max(names, key=lambda n: kern.get(n, (0, 0.0))[1])
     roof = roofline(kern, dom, names[dom], peak)
     traffic_path = ROOT / "profiles" / "traffic.json"
     if roof and traffic_path.exists():
         roof["traffic"] = json.loads(traffic_path.read_text()).get(dom)
     roof_other = {n: roofline(kern, n, b, peak) for n, b in names.items()}
-    total_ms = sum(t for _, t in kern.values()) / args.steps
+    kern_avg = {k: {"launches": c, "avg_ms": t / c} for k, (c, t) in kern.items() if c}
 
     # e2e through the public API: pinned host inputs in, results out, every step
     hkey = key.cpu().pin_memory()
@@ -332,8 +333,7 @@ def run_ours(args, rank, world, local):
                        "rows_per_step": rows_per_step, "parallelism": "replicas" if world > 1 else "single",
                        "l2": "inputs 768 MB per step > 129 MB L2 (no flush needed)"},
             "roofline": roof, "roofline_kernels": roof_other, "peak_kind": peak_kind,
-            "kernel_ms_per_step": {k: v[1] / args.steps for k, v in kern.items()},
-            "kernel_sum_ms_per_step": total_ms,
+            "kernels": kern_avg,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks.summary(),
             "operators": ops,
         }
@@ -372,7 +372,8 @@ def operator_lines(ctx, args, peak, stream):
     ms, kern, _ = timed(ctx, gstep, steps, 3, 1, stream)
     out["groupby_config1_unordered"] = {"rows_per_s": N_ROWS / (ms * 1e-3), "ms_per_op": ms,
                                         "op_frac_of_peak": (N_ROWS * 8 + GROUPS * 20) / (ms * 1e-3) / 1e9 / peak,
-                                        "roofline": roofline(kern, "k_groupby_hash", N_ROWS * 8, peak)}
+                                        "path": ctx.groupby_stats()["path"],
+                                        "roofline": roofline(kern, "k_gb_part", N_ROWS * 8, peak)}
 
     def fgstep():
         ctx.groupby_cols(d["key"], d["val"], d["val2"], d["lo2"], d["hi2"], cap=GROUPS * 2, order=QG_ORDER_NONE)
@@ -381,7 +382,8 @@ def operator_lines(ctx, args, peak, stream):
     out["filter_groupby_config1_unordered"] = {
         "rows_per_s": N_ROWS / (ms * 1e-3), "ms_per_op": ms,
         "op_frac_of_peak": (N_ROWS * 12 + GROUPS * 20) / (ms * 1e-3) / 1e9 / peak,
-        "roofline": roofline(kern, "k_groupby_hash_fused", N_ROWS * 12, peak)}
+        "path": ctx.groupby_stats()["path"],
+        "roofline": roofline(kern, "k_gb_part_fused", N_ROWS * 12, peak)}
     del d
     torch.cuda.empty_cache()
     # config 2: join + filter + sort
@@ -405,10 +407,58 @@ def operator_lines(ctx, args, peak, stream):
     return out
 
 
+def run_only(args):
+    """One operator alone (for profiler captures): W warm-up + K timed calls."""
+    import torch
+
+    from query_on_opencl_fpga_gb300 import datagen
+    from query_on_opencl_fpga_gb300.api import QG_ORDER_NONE, Context
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    ctx = Context(stream)
+    rows = args.rows
+    if args.only in ("groupby", "fused"):
+        n = rows or N_ROWS
+        d = datagen.config1_groupby(n, GROUPS, seed=0, device="cuda")
+        v2 = d["val2"] if args.only == "fused" else None
+        fn = lambda: ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=GROUPS * 2,  # noqa: E731
+                                      order=QG_ORDER_NONE)
+    elif args.only == "filter":
+        n = rows or (1 << 24)
+        f = datagen.config0_filter(n, seed=0, device="cuda")
+        fn = lambda: ctx.filter_cols(f["key"], f["payload"], f["lo"], f["hi"])  # noqa: E731
+    elif args.only == "join":
+        n = rows or (1 << 28)
+        j = datagen.config2_join(min(1 << 24, max(n // 16, 1)), n, seed=0, device="cuda")
+        fn = lambda: ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"],  # noqa: E731
+                                          j["shi"], cap=int(n * 0.26) + 1024)
+    elif args.only == "sort":
+        n = rows or (1 << 26)
+        from query_on_opencl_fpga_gb300.datagen import records, uniform_i32
+
+        rec = records(uniform_i32(n, 0, 1 << 20, 0, "cuda"))
+        fn = lambda: ctx.sort_rec(rec)  # noqa: E731
+    else:
+        raise SystemExit(f"unknown --only {args.only}")
+    if args.variant >= 0:
+        ctx.check(ctx.lib.qg_filter_set_variant(args.variant), "qg_filter_set_variant")
+    ms, kern, launches = timed(ctx, fn, args.steps, args.warmup, 1, stream)
+    extra = {"groupby_stats": ctx.groupby_stats()} if args.only in ("groupby", "fused") else {}
+    print(json.dumps({"only": args.only, "rows": n, "variant": args.variant, "ms_per_op": ms,
+                      "rows_per_s": n / (ms * 1e-3),
+                      "kernels_ms_per_op": {k: v[1] / args.steps for k, v in kern.items()},
+                      "gpu_launches": launches, **extra}), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default=None, help="groupby|fused|filter|join|sort: one operator alone")
+    ap.add_argument("--rows", type=int, default=0, help="row count for --only (default: the config size)")
+    ap.add_argument("--variant", type=int, default=-1, help="column filter kernel variant for --only filter")
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-operators", action="store_true")
@@ -416,6 +466,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.only:
+        run_only(args)
+        return
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         run_reference(args, rank, int(os.environ.get("WORLD_SIZE", "1")))

@@ -64,7 +64,7 @@ QG_API qg_status qg_ctx_reserve(qg_ctx *ctx, size_t bytes);
 /* Number of kernels this context has launched (for launch accounting). */
 QG_API uint64_t qg_ctx_launch_count(qg_ctx *ctx);
 /* Per-kernel timing: with timing on, CUDA events on the context's stream
- * bracket every kernel launch (up to 512 between reports).  The report
+ * bracket every kernel launch (up to 4096 between reports).  The report
  * synchronises, writes one "kernel_name launches total_ms" line per kernel
  * into buf and clears the log; it returns the number of lines or -1.  The
  * reference timed stages with host wall-clock around clFinish
@@ -95,6 +95,11 @@ QG_API qg_status qg_filter_cols(qg_ctx *ctx, const int32_t *key, const int32_t *
 QG_API qg_status qg_filter_cols_async(qg_ctx *ctx, const int32_t *key, const int32_t *payload,
                                       int64_t n, int32_t lo, int32_t hi, int32_t *out_pairs,
                                       int64_t cap, int64_t *d_out_n);
+
+/* Column filter kernel choice (process-wide): 0 = one 4096-row tile per CTA
+ * held in registers, 1 = persistent CTAs streaming tiles through a 3-stage
+ * bulk-copy (TMA) ring.  Results are identical. */
+QG_API qg_status qg_filter_set_variant(int variant);
 
 /* ---- scan (ScanLargeArrays/prefixSum/blockAddition, host/host/testScan.cpp:278-340) */
 /* Exclusive int32 prefix sum with two's-complement wrap; in == out allowed. */
@@ -132,6 +137,19 @@ QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key, const in
                                        const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
                                        int32_t *gkey, int64_t *gsum, int64_t *gcount, int64_t cap,
                                        int order, int64_t *d_num_groups);
+
+/* Tuning of qg_groupby_cols (process-wide).  mode 0: two-pass shared-memory
+ * aggregation with the global-table kernel as automatic fallback; mode 1:
+ * global-table kernel only.  hot_slots_log2: per-SM shared-memory table
+ * (8..13); partitions_log2: spill partitions (0 = chosen from cap, else
+ * 1..13); bucket_cap: spill bucket capacity (0 = automatic; a small value
+ * forces the fallback, for testing). */
+QG_API qg_status qg_groupby_set_knobs(int mode, int hot_slots_log2, int partitions_log2,
+                                      uint32_t bucket_cap);
+/* Diagnostics of the context's last qg_groupby_cols call: out[0] = path
+ * (0 two-pass, 1 global table), out[1] = overflow flags (bit 0 spill bucket,
+ * bit 1 pass-2 table), out[2] = fullest spill bucket, out[3] = bucket capacity. */
+QG_API qg_status qg_groupby_stats(qg_ctx *ctx, uint32_t *out4);
 
 /* ---- hash join + filter + sort (config 2; kernel/hj_filter_sort/1/hj_filter_sort_op.cl)
  * Inner equi-join of R(rkey, rpay) and S(skey, spay) on uint key equality,

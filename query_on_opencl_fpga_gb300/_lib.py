@@ -48,6 +48,7 @@ SIGNATURES: dict[str, tuple] = {
                                c_int64, POINTER(c_int64)]),
     "qg_filter_cols_async": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_int32,
                                      c_void_p, c_int64, c_void_p]),
+    "qg_filter_set_variant": (c_int, [c_int]),
     "qg_scan_excl_i32": (c_int, [c_void_p, c_void_p, c_void_p, c_int64]),
     "qg_sort_rec_by_y": (c_int, [c_void_p, c_void_p, c_int64]),
     "qg_groupby_rec": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
@@ -57,6 +58,8 @@ SIGNATURES: dict[str, tuple] = {
                                 c_void_p, c_void_p, c_void_p, c_int64, c_int, POINTER(c_int64)]),
     "qg_groupby_cols_async": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
                                       c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p]),
+    "qg_groupby_set_knobs": (c_int, [c_int, c_int, c_int, c_uint32]),
+    "qg_groupby_stats": (c_int, [c_void_p, c_void_p]),
     "qg_join_filter_sort": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                     c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64,
                                     POINTER(c_int64)]),

@@ -53,7 +53,7 @@ QG_API qg_status qg_ctx_destroy(qg_ctx *ctx) {
     if (!ctx) return QG_ERR_INVALID;
     cudaStreamSynchronize(ctx->stream);
     if (ctx->ev[0])
-        for (int i = 0; i < 2 * 512; i++) cudaEventDestroy(ctx->ev[i]);
+        for (int i = 0; i < 2 * QG_MAX_TIMED; i++) cudaEventDestroy(ctx->ev[i]);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->table) cudaFree(ctx->table);
     if (ctx->aux) cudaFree(ctx->aux);
@@ -127,7 +127,7 @@ qg_status qg_cuda_fail(qg_ctx *ctx, cudaError_t e, const char *what) {
     return QG_ERR_CUDA;
 }
 
-static const int QG_MAX_TIMED = 512;
+
 
 void qg_pre_launch(qg_ctx *ctx) {
     if (!ctx->timing || ctx->ev_used >= QG_MAX_TIMED) return;

@@ -16,6 +16,7 @@ namespace {
 
 constexpr int FT_THREADS = 256;
 constexpr int FT_WARPS = FT_THREADS / 32;
+constexpr int FT_LB_WARPS = 4;  // warps doing the look-back: 128 predecessors per round
 
 // Records (uint2 {x, y}), two per 128-bit load.  ROUNDS loads per thread.
 template <int ROUNDS>
@@ -58,41 +59,11 @@ k_filter_rec(const uint4 *__restrict__ in, long long n, int32_t lo, int32_t hi,
         fl |= (uint32_t)f0 << (2 * r);
         fl |= (uint32_t)f1 << (2 * r + 1);
     }
-    __syncthreads();
-    if (warp == 0) {
-        // Exclusive scan of the ROUNDS*WARPS per-warp counts, round-major
-        // (the order of the rows they cover).
-        constexpr int E = ROUNDS * FT_WARPS;
-        constexpr int PER = (E + 31) / 32;
-        uint32_t loc[PER];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int k = 0; k < PER; k++) {
-            int e = lane * PER + k;
-            loc[k] = (e < E) ? s_woff[e] : 0u;
-            sum += loc[k];
-        }
-        uint32_t incl = sum;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            uint32_t t = __shfl_up_sync(QG_FULL_MASK, incl, d);
-            if (lane >= d) incl += t;
-        }
-        uint32_t total = __shfl_sync(QG_FULL_MASK, incl, 31);
-        uint32_t run = incl - sum;
-#pragma unroll
-        for (int k = 0; k < PER; k++) {
-            int e = lane * PER + k;
-            if (e < E) s_woff[e] = run;
-            run += loc[k];
-        }
-        uint32_t excl = qg_lb_warp_exclusive(lb, tile, s_epoch, total);
-        if (lane == 0) {
-            s_excl = excl;
-            if (tile == gridDim.x - 1) *d_count = (long long)excl + total;
-        }
-    }
-    __syncthreads();
+    // Exclusive offsets of the ROUNDS*WARPS per-warp counts, round-major (the
+    // order of the rows they cover), and the tile's offset from the look-back.
+    __shared__ uint32_t s_tmp[2 * FT_LB_WARPS + 1];
+    qg_tile_offsets_wide<ROUNDS * FT_WARPS, FT_LB_WARPS>(s_woff, lb, tile, s_epoch, &s_excl, s_tmp,
+                                                         d_count, gridDim.x - 1);
     const long long excl = s_excl;
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
@@ -156,39 +127,9 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
         if (lane == 0) s_woff[r * FT_WARPS + warp] = tot;
         fl |= f << (4 * r);
     }
-    __syncthreads();
-    if (warp == 0) {
-        constexpr int E = ROUNDS * FT_WARPS;
-        constexpr int PER = (E + 31) / 32;
-        uint32_t loc[PER];
-        uint32_t sum = 0;
-#pragma unroll
-        for (int k = 0; k < PER; k++) {
-            int e = lane * PER + k;
-            loc[k] = (e < E) ? s_woff[e] : 0u;
-            sum += loc[k];
-        }
-        uint32_t incl = sum;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            uint32_t t = __shfl_up_sync(QG_FULL_MASK, incl, d);
-            if (lane >= d) incl += t;
-        }
-        uint32_t total = __shfl_sync(QG_FULL_MASK, incl, 31);
-        uint32_t run = incl - sum;
-#pragma unroll
-        for (int k = 0; k < PER; k++) {
-            int e = lane * PER + k;
-            if (e < E) s_woff[e] = run;
-            run += loc[k];
-        }
-        uint32_t excl = qg_lb_warp_exclusive(lb, tile, s_epoch, total);
-        if (lane == 0) {
-            s_excl = excl;
-            if (tile == gridDim.x - 1) *d_count = (long long)excl + total;
-        }
-    }
-    __syncthreads();
+    __shared__ uint32_t s_tmp[2 * FT_LB_WARPS + 1];
+    qg_tile_offsets_wide<ROUNDS * FT_WARPS, FT_LB_WARPS>(s_woff, lb, tile, s_epoch, &s_excl, s_tmp,
+                                                         d_count, gridDim.x - 1);
     const long long excl = s_excl;
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
@@ -208,6 +149,120 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
 
 constexpr int REC_ROUNDS = 8;   // 4096 records per tile
 constexpr int COL_ROUNDS = 4;   // 4096 rows per tile
+
+// Persistent column filter: each CTA streams tiles of 4096 rows (keys and
+// payloads, 32 KB) through a 3-stage shared-memory ring filled by the bulk-copy
+// (TMA) engine, so the next tiles are in flight while a tile's look-back
+// resolves.  Tile ids come from the context's atomic counter in the order the
+// CTAs ask for them; a CTA processes its tiles in increasing order, so every
+// tile's predecessors belong to running CTAs and the look-back always ends.
+constexpr int FP_THREADS = 256;
+constexpr int FP_WARPS = FP_THREADS / 32;
+constexpr int FP_TILE = 4096;
+constexpr int FP_ROUNDS = FP_TILE / FP_THREADS;  // 16: one row per thread per round
+constexpr int FP_STAGES = 3;
+
+struct FpSmem {
+    int32_t k[FP_STAGES][FP_TILE];
+    int32_t p[FP_STAGES][FP_TILE];
+    unsigned long long bar[FP_STAGES];
+    uint32_t tile_of[FP_STAGES];
+    uint32_t woff[FP_ROUNDS * FP_WARPS];
+    uint32_t bal[FP_ROUNDS * FP_WARPS];
+    uint32_t lbtmp[2 * FT_LB_WARPS + 1];
+    uint32_t excl, epoch;
+};
+
+__device__ __forceinline__ void fp_issue(FpSmem &S, int s, const int32_t *key, const int32_t *pay,
+                                         long long n, uint32_t t) {
+    const long long base = (long long)t * FP_TILE;
+    long long rows = n - base;
+    if (rows > FP_TILE) rows = FP_TILE;
+    const uint32_t bytes = (uint32_t)(rows & ~3LL) * 4u;
+    if (bytes) {
+        qg_mbar_arrive_expect_tx(&S.bar[s], 2 * bytes);
+        qg_bulk_g2s(S.k[s], key + base, bytes, &S.bar[s]);
+        qg_bulk_g2s(S.p[s], pay + base, bytes, &S.bar[s]);
+    } else {
+        qg_mbar_arrive(&S.bar[s]);
+    }
+}
+
+__global__ void __launch_bounds__(FP_THREADS)
+k_filter_cols_tma(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, long long n,
+                  int32_t lo, int32_t hi, int2 *__restrict__ out, long long cap,
+                  long long *__restrict__ d_count, qg_lookback lb, uint32_t num_tiles) {
+    extern __shared__ __align__(128) unsigned char fp_raw[];
+    FpSmem &S = *reinterpret_cast<FpSmem *>(fp_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t lt = qg_lanemask_lt();
+    if (tid == 0) {
+        for (int s = 0; s < FP_STAGES; s++) qg_mbar_init(&S.bar[s], 1);
+        qg_mbar_fence_init();
+        S.epoch = *(volatile uint32_t *)&lb.ctl->epoch;
+        for (int s = 0; s < FP_STAGES; s++) {
+            const uint32_t t = atomicAdd(&lb.ctl->tile_ctr, 1u);
+            S.tile_of[s] = t;
+            if (t < num_tiles) fp_issue(S, s, key, pay, n, t);
+        }
+    }
+    __syncthreads();
+    for (uint32_t it = 0;; it++) {
+        const int s = (int)(it % FP_STAGES);
+        const uint32_t t = S.tile_of[s];
+        if (t >= num_tiles) break;
+        const uint32_t parity = (it / FP_STAGES) & 1u;
+        uint32_t w = 0;
+        bool landed = true;
+        while (!qg_mbar_try_wait(&S.bar[s], parity)) {
+            if (++w >= lb.spin_limit) {
+                // The copy never landed: report, and read the tile from global.
+                qg_record_error(lb.ctl, QG_ERR_TIMEOUT, lb.site);
+                landed = false;
+                break;
+            }
+        }
+        const long long base = (long long)t * FP_TILE;
+        long long rows_l = n - base;
+        const int rows = rows_l > FP_TILE ? FP_TILE : (int)rows_l;
+        const int bulk_rows = landed ? (rows & ~3) : 0;
+#pragma unroll
+        for (int r = 0; r < FP_ROUNDS; r++) {
+            const int row = r * FP_THREADS + tid;
+            bool f = false;
+            if (row < rows) {
+                const int32_t k = row < bulk_rows ? S.k[s][row] : key[base + row];
+                f = (k >= lo) & (k <= hi);
+            }
+            const uint32_t b = __ballot_sync(QG_FULL_MASK, f);
+            if (lane == 0) {
+                S.woff[r * FP_WARPS + warp] = __popc(b);
+                S.bal[r * FP_WARPS + warp] = b;
+            }
+        }
+        qg_tile_offsets_wide<FP_ROUNDS * FP_WARPS, FT_LB_WARPS>(S.woff, lb, t, S.epoch, &S.excl,
+                                                                S.lbtmp, d_count, num_tiles - 1);
+        const long long excl = S.excl;
+#pragma unroll
+        for (int r = 0; r < FP_ROUNDS; r++) {
+            const uint32_t b = S.bal[r * FP_WARPS + warp];
+            if ((b >> lane) & 1u) {
+                const int row = r * FP_THREADS + tid;
+                const long long pos = excl + S.woff[r * FP_WARPS + warp] + __popc(b & lt);
+                const int32_t pv = row < bulk_rows ? S.p[s][row] : pay[base + row];
+                if (pos < cap) out[pos] = make_int2((int32_t)(base + row), pv);
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t t2 = atomicAdd(&lb.ctl->tile_ctr, 1u);
+            S.tile_of[s] = t2;
+            if (t2 < num_tiles) fp_issue(S, s, key, pay, n, t2);
+        }
+        __syncthreads();
+    }
+    qg_lb_end(lb);
+}
 
 }  // namespace
 
@@ -239,6 +294,8 @@ qg_status qg_filter_rec_launch(qg_ctx *ctx, const void *in, int64_t n, int32_t l
     return qg_check_launch(ctx, "k_filter_rec");
 }
 
+static int g_filter_variant = 0;
+
 qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *pay, int64_t n,
                                 int32_t lo, int32_t hi, int32_t *out, int64_t cap,
                                 long long *d_count) {
@@ -254,10 +311,32 @@ qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *
     char *scr;
     QG_TRY(qg_scratch(ctx, qg_lb_bytes(tiles), &scr));
     qg_lookback lb{(unsigned long long *)scr, ctx->ctl, ctx->spin_limit, QG_SITE_FILTER};
+    if (g_filter_variant == 1) {
+        static bool attr = false;
+        if (!attr) {
+            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_filter_cols_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)sizeof(FpSmem)), "attr");
+            attr = true;
+        }
+        const long long ftiles = qg_ceil_div(n, FP_TILE);
+        const int grid = (int)(ftiles < ctx->sm_count * 2LL ? ftiles : ctx->sm_count * 2LL);
+        qg_pre_launch(ctx);
+        k_filter_cols_tma<<<grid, FP_THREADS, sizeof(FpSmem), ctx->stream>>>(
+            key, pay, n, lo, hi, (int2 *)out, cap, d_count, lb, (uint32_t)ftiles);
+        return qg_check_launch(ctx, "k_filter_cols_tma");
+    }
     qg_pre_launch(ctx);
     k_filter_cols<COL_ROUNDS><<<(unsigned)tiles, FT_THREADS, 0, ctx->stream>>>(
         key, pay, n, lo, hi, (int2 *)out, cap, d_count, lb);
     return qg_check_launch(ctx, "k_filter_cols");
+}
+
+// 0: one tile per CTA, rows staged in registers; 1: persistent CTAs with a
+// bulk-copy ring (both bit-identical; chosen by measurement).
+extern "C" QG_API qg_status qg_filter_set_variant(int variant) {
+    if (variant < 0 || variant > 1) return QG_ERR_INVALID;
+    g_filter_variant = variant;
+    return QG_OK;
 }
 
 extern "C" {

@@ -16,13 +16,15 @@
 //    predicate on a second column (configs 1 / 1-fused; the fused
 //    filter_aggregation image, kernel/filter_aggregation/
 //    filter_aggregation_cu_op_dp.cl).  Instead of sort -> label -> scan ->
-//    aggregate, rows are hashed once: each CTA keeps a private open-addressing
-//    table in shared memory for the keys it sees first (Zipf heavy hitters land
-//    there), other rows go to a global open-addressing table whose 32-byte
-//    slots {tag, sum, count} sit in one L2 sector and are updated with
-//    atomicCAS / 64-bit atomicAdd.  A final pass compacts the table into the
-//    output columns and clears it for the next call; QG_ORDER_KEY then sorts
-//    the groups by key (unsigned, the order groupByImpl's sorted array gives).
+//    aggregate, rows are hashed: the default path is two passes (k_gb_part,
+//    k_gb_merge, section 2' below) -- per-SM shared-memory tables absorb the
+//    heavy hitters, the remaining rows are spilled into hash partitions and
+//    each partition is summed by one CTA in shared memory.  The single-pass
+//    global-table kernel (k_groupby_hash: shared-memory table + global
+//    open-addressing table of 32-byte {tag, sum, count} slots updated with
+//    atomicCAS / 64-bit atomicAdd) is the fallback for inputs that overflow
+//    the spill buckets.  QG_ORDER_KEY then sorts the groups by key (unsigned,
+//    the order groupByImpl's sorted array gives).
 #include "qg_internal.cuh"
 #include "qg_sort.cuh"
 
@@ -317,6 +319,318 @@ __global__ void k_groupby_gather(const unsigned long long *__restrict__ rec, lon
     }
 }
 
+// ---------------------------------------------------------------------------
+// 2'. two-pass column group-by (default path)
+//
+// Pass 1 (k_gb_part): one CTA per SM reads a contiguous slice of the rows.
+// Keys that find a place in the CTA's shared-memory table (the heavy
+// hitters, which arrive first under skew) are summed there.  Every other row
+// is written as (key, value) into the CTA's own spill bucket for partition
+// hash(key) >> (32 - plog2) -- a shared-memory cursor per partition, no
+// global atomics; the scattered 8-byte stores merge in L2 because each
+// bucket is written sequentially.  At the end the CTA writes its per-
+// partition spill counts and its shared-memory table, counting-sorted by
+// partition, as (key, count, sum) partials.
+// Pass 2 (k_gb_merge): one CTA per partition gathers that partition's spill
+// rows and partials from every pass-1 CTA, sums them in a shared-memory table
+// and emits the final groups.  No global hash table, no global atomics on the
+// data path; the L2-atomic bound of a global table is gone.
+// A bucket that overflows its capacity (an adversarial key order) raises a
+// flag and the host reruns the call with the global-table kernel above.
+// ---------------------------------------------------------------------------
+struct GPartial {
+    uint32_t key;
+    uint32_t cnt;
+    long long sum;
+};
+
+struct GbSpill {
+    uint2 *miss;      // [C][P][capm] (key, value)
+    uint32_t *mcnt;   // [P][GB_MAX_C] rows in each bucket (clamped to capm)
+    GPartial *part;   // [C][S] shared-memory tables, partition-sorted
+    uint32_t *poff;   // [P+1][GB_MAX_C] partition offsets into part[c]
+    uint32_t capm;
+    int plog2;
+    int slog2;
+};
+
+constexpr int GB_MAX_C = 256;  // pass-1 CTAs (one per SM)
+constexpr int P1_THREADS = 1024;
+constexpr int P2_THREADS = 256;
+constexpr int P2_TLOG2 = 11;  // pass-2 table slots (2048) + 1 for key 0xffffffff
+constexpr int HOT_MAX_PROBE = 4;
+constexpr int GB_SKETCH_WORDS = 8192;  // 16K 16-bit admission counters (32 KB)
+
+// In-place exclusive scan of a[0..L) in shared memory by the whole CTA;
+// returns the total.  `wsum` holds one word per warp.
+__device__ uint32_t block_excl_scan(uint32_t *a, int L, uint32_t *wsum) {
+    const int T = blockDim.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int per = (L + T - 1) / T;
+    const int b = tid * per, e = min(b + per, L);
+    uint32_t s = 0;
+    for (int i = b; i < e; i++) s += a[i];
+    uint32_t inc = s;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t x = __shfl_up_sync(QG_FULL_MASK, inc, d);
+        if (lane >= d) inc += x;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    uint32_t woff = 0, total = 0;
+    for (int w = 0; w < (T >> 5); w++) {
+        uint32_t x = wsum[w];
+        if (w < warp) woff += x;
+        total += x;
+    }
+    uint32_t run = woff + inc - s;
+    for (int i = b; i < e; i++) {
+        uint32_t x = a[i];
+        a[i] = run;
+        run += x;
+    }
+    __syncthreads();
+    return total;
+}
+
+// 64-bit two's-complement accumulation with 32-bit shared-memory atomics:
+// the low word takes the addend, the high word takes the addend's sign
+// extension plus this add's carry out of the low word.  Each add is exact, so
+// the pair holds the int64 sum whatever the interleaving.
+__device__ __forceinline__ void smem_add_i64(uint32_t *lo, uint32_t *hi, long long v) {
+    const uint32_t vl = (uint32_t)v;
+    const uint32_t old = atomicAdd(lo, vl);
+    const uint32_t carry = (old + vl) < old ? 1u : 0u;
+    const uint32_t inc = (uint32_t)((unsigned long long)v >> 32) + carry;
+    if (inc) atomicAdd(hi, inc);
+}
+
+// L2 eviction policy for data read once: evicted first, so that the spill
+// buckets being filled stay resident and are written back as whole sectors.
+__device__ __forceinline__ unsigned long long l2_evict_first_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ int4 ldg_stream_ef(const int4 *p, unsigned long long pol) {
+    int4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.s32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+
+template <bool PRED>
+__global__ void __launch_bounds__(P1_THREADS, 1)
+k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
+          const int32_t *__restrict__ val2, int32_t lo2, int32_t hi2, long long n, GbSpill sp,
+          unsigned int *__restrict__ flags) {
+    extern __shared__ __align__(16) unsigned char p1_raw[];
+    __shared__ uint32_t wsum[32];
+    const int S = 1 << sp.slog2, P = 1 << sp.plog2;
+    const uint32_t smask = (uint32_t)S - 1, pshift = 32 - sp.plog2, capm = sp.capm;
+    uint32_t *hk = reinterpret_cast<uint32_t *>(p1_raw);
+    uint32_t *hc = hk + S;
+    uint32_t *hlo = hc + S;
+    uint32_t *hhi = hlo + S;
+    uint32_t *cur = hhi + S;
+    uint32_t *sk = cur + P;
+    const int tid = threadIdx.x;
+    for (int i = tid; i < S; i += P1_THREADS) {
+        hk[i] = SM_EMPTY;
+        hc[i] = 0;
+        hlo[i] = 0;
+        hhi[i] = 0;
+    }
+    for (int i = tid; i < P; i += P1_THREADS) cur[i] = 0;
+    for (int i = tid; i < GB_SKETCH_WORDS; i += P1_THREADS) sk[i] = 0;
+    __syncthreads();
+    const int c = blockIdx.x, C = gridDim.x;
+    uint2 *mine = sp.miss + (size_t)c * P * capm;
+    const unsigned long long pol = l2_evict_first_policy();
+
+    auto process = [&](int32_t k, int32_t v) {
+        const uint32_t uk = (uint32_t)k;
+        const uint32_t hh = qg_hash32(uk);
+        if (uk != SM_EMPTY) {
+            uint32_t h = hh & smask;
+            bool found = false;
+#pragma unroll
+            for (int p = 0; p < HOT_MAX_PROBE; p++) {
+                const uint32_t cu = hk[h];
+                if (cu == uk) { found = true; break; }
+                if (cu == SM_EMPTY) break;
+                h = (h + 1) & smask;
+            }
+            if (!found) {
+                // Admission: a key enters the table on its second sighting, so
+                // keys seen once (the cold tail) do not take the slots that
+                // frequent keys need.  Sketch = 16-bit counters, two per word.
+                const uint32_t sw = (hh >> 5) & (GB_SKETCH_WORDS - 1), sh = (hh & 16u);
+                const uint32_t old = atomicAdd(&sk[sw], 1u << sh);
+                if (((old >> sh) & 0xffffu) != 0) {
+                    h = hh & smask;
+#pragma unroll
+                    for (int p = 0; p < HOT_MAX_PROBE; p++) {
+                        uint32_t cu = hk[h];
+                        if (cu == SM_EMPTY) cu = atomicCAS(&hk[h], SM_EMPTY, uk);
+                        if (cu == SM_EMPTY || cu == uk) { found = true; break; }
+                        h = (h + 1) & smask;
+                    }
+                }
+            }
+            if (found) {
+                atomicAdd(&hc[h], 1u);
+                smem_add_i64(&hlo[h], &hhi[h], (long long)v);
+                return;
+            }
+        }
+        const uint32_t p = hh >> pshift;
+        const uint32_t pos = atomicAdd(&cur[p], 1u);
+        if (pos < capm) mine[(size_t)p * capm + pos] = make_uint2(uk, (uint32_t)v);
+        else atomicOr(flags, 1u);
+    };
+
+    const long long nv = n >> 2;
+    const long long qb = nv * c / C, qe = nv * (c + 1) / C;
+    for (long long q = qb + tid; q < qe; q += P1_THREADS) {
+        const int4 k4 = ldg_stream_ef(reinterpret_cast<const int4 *>(key) + q, pol);
+        const int4 v4 = ldg_stream_ef(reinterpret_cast<const int4 *>(val) + q, pol);
+        bool m0 = true, m1 = true, m2 = true, m3 = true;
+        if (PRED) {
+            const int4 w4 = ldg_stream_ef(reinterpret_cast<const int4 *>(val2) + q, pol);
+            m0 = (w4.x >= lo2) & (w4.x <= hi2);
+            m1 = (w4.y >= lo2) & (w4.y <= hi2);
+            m2 = (w4.z >= lo2) & (w4.z <= hi2);
+            m3 = (w4.w >= lo2) & (w4.w <= hi2);
+        }
+        if (m0) process(k4.x, v4.x);
+        if (m1) process(k4.y, v4.y);
+        if (m2) process(k4.z, v4.z);
+        if (m3) process(k4.w, v4.w);
+    }
+    if (c == C - 1) {
+        for (long long i = (nv << 2) + tid; i < n; i += P1_THREADS) {
+            if (PRED && !((val2[i] >= lo2) & (val2[i] <= hi2))) continue;
+            process(key[i], val[i]);
+        }
+    }
+    __syncthreads();
+    for (int p = tid; p < P; p += P1_THREADS) {
+        atomicMax(flags + 1, cur[p]);  // fullest bucket, for qg_groupby_stats
+        sp.mcnt[(size_t)p * GB_MAX_C + c] = min(cur[p], capm);
+        cur[p] = 0;
+    }
+    __syncthreads();
+    // Counting sort of the shared-memory table by partition.
+    for (int s = tid; s < S; s += P1_THREADS)
+        if (hc[s]) atomicAdd(&cur[qg_hash32(hk[s]) >> pshift], 1u);
+    __syncthreads();
+    const uint32_t total = block_excl_scan(cur, P, wsum);
+    for (int p = tid; p < P; p += P1_THREADS) sp.poff[(size_t)p * GB_MAX_C + c] = cur[p];
+    if (tid == 0) sp.poff[(size_t)P * GB_MAX_C + c] = total;
+    __syncthreads();
+    GPartial *pt = sp.part + (size_t)c * S;
+    for (int s = tid; s < S; s += P1_THREADS) {
+        if (!hc[s]) continue;
+        const uint32_t r = atomicAdd(&cur[qg_hash32(hk[s]) >> pshift], 1u);
+        GPartial g;
+        g.key = hk[s];
+        g.cnt = hc[s];
+        g.sum = (long long)(((unsigned long long)hhi[s] << 32) | hlo[s]);
+        pt[r] = g;
+    }
+}
+
+// Persistent: each CTA takes partitions from an atomic work counter.
+__global__ void __launch_bounds__(P2_THREADS)
+k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict__ gsum,
+           long long *__restrict__ gcnt, long long cap, unsigned long long *__restrict__ cursor,
+           unsigned long long *__restrict__ rec, unsigned int *__restrict__ flags,
+           unsigned int *__restrict__ work) {
+    constexpr int T = 1 << P2_TLOG2;
+    constexpr uint32_t TMASK = T - 1;
+    constexpr int W = P2_THREADS / 32;
+    __shared__ uint32_t tk[T + 1], tc[T + 1], tlo[T + 1], thi[T + 1];
+    __shared__ uint32_t s_part;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int P = 1 << sp.plog2, S = 1 << sp.slog2;
+    const uint32_t lt = qg_lanemask_lt();
+
+    auto insert = [&](uint32_t k, uint32_t cnt, long long sum) {
+        uint32_t s = T;  // the extra slot holds key 0xffffffff
+        if (k != SM_EMPTY) {
+            uint32_t h = qg_hash32(k) & TMASK;
+            uint32_t probes = 0;
+            while (true) {
+                uint32_t cu = tk[h];
+                if (cu == SM_EMPTY) cu = atomicCAS(&tk[h], SM_EMPTY, k);
+                if (cu == SM_EMPTY || cu == k) break;
+                h = (h + 1) & TMASK;
+                if (++probes >= T) {
+                    atomicOr(flags, 2u);
+                    return;
+                }
+            }
+            s = h;
+        } else {
+            tk[T] = k;
+        }
+        atomicAdd(&tc[s], cnt);
+        smem_add_i64(&tlo[s], &thi[s], sum);
+    };
+
+    while (true) {
+        __syncthreads();
+        if (tid == 0) s_part = atomicAdd(work, 1u);
+        for (int i = tid; i <= T; i += P2_THREADS) {
+            tk[i] = SM_EMPTY;
+            tc[i] = 0;
+            tlo[i] = 0;
+            thi[i] = 0;
+        }
+        __syncthreads();
+        const uint32_t p = s_part;
+        if (p >= (uint32_t)P) break;
+        const uint32_t *mcnt = sp.mcnt + (size_t)p * GB_MAX_C;
+        const uint32_t *po = sp.poff + (size_t)p * GB_MAX_C;
+        const uint32_t *po1 = sp.poff + (size_t)(p + 1) * GB_MAX_C;
+        // One warp per source CTA: its spill bucket, then its partials.
+        for (int cc = warp; cc < C; cc += W) {
+            const uint32_t m = mcnt[cc];
+            const uint2 *b = sp.miss + ((size_t)cc * P + p) * sp.capm;
+            for (uint32_t e = lane; e < m; e += 32) {
+                const uint2 r = b[e];
+                insert(r.x, 1u, (long long)(int32_t)r.y);
+            }
+            const uint32_t q0 = po[cc], q1 = po1[cc];
+            const GPartial *g = sp.part + (size_t)cc * S;
+            for (uint32_t e = q0 + lane; e < q1; e += 32) {
+                const GPartial x = g[e];
+                insert(x.key, x.cnt, x.sum);
+            }
+        }
+        __syncthreads();
+        for (int base = 0; base <= T; base += P2_THREADS) {
+            const int s = base + tid;
+            const bool occ = (s <= T) && tc[s] != 0;
+            const uint32_t b = __ballot_sync(QG_FULL_MASK, occ);
+            unsigned long long o = 0;
+            if (lane == 0 && b) o = atomicAdd(cursor, (unsigned long long)__popc(b));
+            o = __shfl_sync(QG_FULL_MASK, o, 0);
+            if (occ) {
+                const long long pos = (long long)o + __popc(b & lt);
+                if (pos < cap) {
+                    gkey[pos] = (int32_t)tk[s];
+                    gsum[pos] = (long long)(((unsigned long long)thi[s] << 32) | tlo[s]);
+                    gcnt[pos] = (long long)tc[s];
+                    if (rec) rec[pos] = ((unsigned long long)tk[s] << 32) | (unsigned long long)pos;
+                }
+            }
+        }
+    }
+}
+
 }  // namespace
 
 static int grid_for(qg_ctx *ctx, long long work, int per_block, int max_per_sm) {
@@ -392,26 +706,70 @@ extern "C" QG_API qg_status qg_aggregate_groups(qg_ctx *ctx, const void *sorted,
     return qg_ctx_check(ctx);
 }
 
+
 // ---------------------------------------------------------------------------
 // host: column hash group-by
 // ---------------------------------------------------------------------------
-static int g_gb_slog2 = 12;          // shared-memory table slots (log2)
-static int g_gb_blocks_per_sm = 2;
+static int g_gb_mode = 0;            // 0: two-pass (global table as fallback), 1: global table only
+static int g_gb_hot_slog2 = 13;      // pass-1 shared-memory table slots (log2)
+static int g_gb_plog2 = 0;           // spill partitions (log2); 0 = chosen from cap
+static uint32_t g_gb_capm = 0;       // spill bucket capacity override (0 = automatic)
+static uint32_t g_gb_last_capm = 0;  // bucket capacity of the last two-pass launch
+static const int g_gb_slog2 = 12;    // fallback kernel: shared-memory table slots (log2)
 
-extern "C" QG_API qg_status qg_groupby_set_knobs(int smem_slots_log2, int blocks_per_sm) {
-    if (smem_slots_log2 < 6 || smem_slots_log2 > 13 || blocks_per_sm < 1 || blocks_per_sm > 8)
+// Path and overflow diagnostics of the context's last qg_groupby_cols call:
+// out[0] = 0 two-pass / 1 global table, out[1] = overflow flags (bit 0 spill
+// bucket, bit 1 pass-2 table), out[2] = fullest spill bucket, out[3] = bucket capacity.
+extern "C" QG_API qg_status qg_groupby_stats(qg_ctx *ctx, uint32_t *out) {
+    if (!ctx || !out) return QG_ERR_INVALID;
+    for (int i = 0; i < 4; i++) out[i] = ctx->gb_stats[i];
+    return QG_OK;
+}
+static const int g_gb_blocks_per_sm = 2;
+
+extern "C" QG_API qg_status qg_groupby_set_knobs(int mode, int hot_slots_log2, int partitions_log2,
+                                                 uint32_t bucket_cap) {
+    if (mode < 0 || mode > 1 || hot_slots_log2 < 8 || hot_slots_log2 > 13 || partitions_log2 < 0 ||
+        partitions_log2 > 13)
         return QG_ERR_INVALID;
-    g_gb_slog2 = smem_slots_log2;
-    g_gb_blocks_per_sm = blocks_per_sm;
+    g_gb_mode = mode;
+    g_gb_hot_slog2 = hot_slots_log2;
+    g_gb_plog2 = partitions_log2;
+    g_gb_capm = bucket_cap;
     return QG_OK;
 }
 
-qg_status qg_groupby_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val,
-                                 const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
-                                 int32_t *gkey, int64_t *gsum, int64_t *gcnt, int64_t cap,
-                                 int order, long long *d_num, unsigned long long **rec_out,
-                                 long long **tsum_out, long long **tcnt_out) {
-    // Table: power of two >= 2 * cap slots, at least 1024.
+struct GbOut {
+    int32_t *k;
+    long long *s, *c;
+    unsigned long long *rec;  // non-null when the output is sorted afterwards
+};
+
+// Where the groups go: the caller's columns, or key-order temporaries in aux.
+static qg_status gb_outputs(qg_ctx *ctx, int32_t *gkey, int64_t *gsum, int64_t *gcnt, int64_t cap,
+                            int order, GbOut *o) {
+    o->k = gkey;
+    if (order == QG_ORDER_KEY) {
+        // rec | tsum | tcnt | sort ping-pong, in the aux arena so the sort's
+        // own scratch use cannot move them.
+        char *scr;
+        size_t cb = (size_t)(cap > 0 ? cap : 1);
+        QG_TRY(qg_aux(ctx, cb * 32, &scr));
+        o->rec = (unsigned long long *)scr;
+        o->s = (long long *)(o->rec + cb);
+        o->c = o->s + cb;
+    } else {
+        o->rec = nullptr;
+        o->s = (long long *)gsum;
+        o->c = (long long *)gcnt;
+    }
+    return QG_OK;
+}
+
+// Single-pass global-table path (fallback).
+static qg_status gb_launch_global(qg_ctx *ctx, const int32_t *key, const int32_t *val,
+                                  const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
+                                  const GbOut &o, int64_t cap, long long *d_num) {
     uint64_t slots = 1024;
     while (slots < (uint64_t)cap * 2) slots <<= 1;
     if (slots > (1ull << 31)) return QG_ERR_UNSUPPORTED;
@@ -420,14 +778,14 @@ qg_status qg_groupby_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t 
     GSlot *tab = (GSlot *)tabp;
     const int slog2 = g_gb_slog2;
     const size_t smem = ((size_t)1 << slog2) * 16;
-    static size_t attr_smem[2] = {0, 0};
+    static bool attr[2] = {false, false};
     const bool pred = val2 != nullptr;
-    if (attr_smem[pred] < smem) {
+    if (!attr[pred]) {
         if (pred)
             QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_groupby_hash<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
         else
             QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_groupby_hash<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
-        attr_smem[pred] = smem;
+        attr[pred] = true;
     }
     if (n > 0) {
         int blocks = grid_for(ctx, (n + 3) / 4, GB_THREADS, g_gb_blocks_per_sm);
@@ -440,31 +798,83 @@ qg_status qg_groupby_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t 
                 key, val, nullptr, 0, 0, n, tab, (uint32_t)(slots - 1), slog2, ctx->ctl);
         QG_TRY(qg_check_launch(ctx, pred ? "k_groupby_hash_fused" : "k_groupby_hash"));
     }
-    // Output: straight into the caller's columns, or into scratch for the sort.
     unsigned long long *cursor = (unsigned long long *)d_num;
     QG_TRY_CUDA(ctx, cudaMemsetAsync(cursor, 0, 8, ctx->stream), "memset cursor");
     int eb = grid_for(ctx, (long long)slots, 256, 8);
-    if (order == QG_ORDER_KEY) {
-        // rec | tsum | tcnt | sort ping-pong, all in the aux arena so the
-        // sort's own scratch use cannot move them.
-        char *scr;
-        size_t cb = (size_t)(cap > 0 ? cap : 1);
-        QG_TRY(qg_aux(ctx, cb * 32, &scr));
-        unsigned long long *rec = (unsigned long long *)scr;
-        long long *tsum = (long long *)(rec + cb);
-        long long *tcnt = tsum + cb;
-        qg_pre_launch(ctx);
-        k_groupby_emit<<<eb, 256, 0, ctx->stream>>>(tab, (long long)slots, gkey, tsum, tcnt, cap,
-                                                    cursor, rec);
-        *rec_out = rec;
-        *tsum_out = tsum;
-        *tcnt_out = tcnt;
-    } else {
-        qg_pre_launch(ctx);
-        k_groupby_emit<<<eb, 256, 0, ctx->stream>>>(tab, (long long)slots, gkey, (long long *)gsum, (long long *)gcnt, cap,
-                                                    cursor, nullptr);
-    }
+    qg_pre_launch(ctx);
+    k_groupby_emit<<<eb, 256, 0, ctx->stream>>>(tab, (long long)slots, o.k, o.s, o.c, cap, cursor, o.rec);
     return qg_check_launch(ctx, "k_groupby_emit");
+}
+
+// Two-pass path.  *d_flags != 0 afterwards means a spill bucket or a pass-2
+// table overflowed and the call must be redone with gb_launch_global.
+static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_t *val,
+                                   const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
+                                   const GbOut &o, int64_t cap, long long *d_num,
+                                   unsigned int *d_flags) {
+    int C = ctx->sm_count;
+    if (C > GB_MAX_C) C = GB_MAX_C;
+    const int slog2 = g_gb_hot_slog2;
+    const int S = 1 << slog2;
+    int plog2 = g_gb_plog2;
+    if (plog2 == 0) {
+        // at most ~1024 groups per partition when cap is the true group count
+        // (the pass-2 table has 2048 slots)
+        plog2 = 6;
+        while (plog2 < 13 && ((long long)1 << plog2) * 1024 < cap) plog2++;
+    }
+    const int P = 1 << plog2;
+    const long long rows_per_cta = (n + C - 1) / C;
+    // Spill buckets hold 4x the rows a bucket gets when every row spills and
+    // hashes evenly; mid-frequency keys that miss the hot table make buckets
+    // lumpy, and this headroom keeps the fallback for adversarial orders.
+    uint32_t capm = g_gb_capm ? g_gb_capm : (uint32_t)(rows_per_cta * 4 / P + 64);
+    g_gb_last_capm = capm;
+    // scratch: miss [C][P][capm] uint2 | mcnt [P][GB_MAX_C] | poff [P+1][GB_MAX_C] | part [C][S]
+    const size_t miss_b = qg_align_up((size_t)C * P * capm * 8, 256);
+    const size_t mcnt_b = qg_align_up((size_t)P * GB_MAX_C * 4, 256);
+    const size_t poff_b = qg_align_up((size_t)(P + 1) * GB_MAX_C * 4, 256);
+    const size_t part_b = qg_align_up((size_t)C * S * sizeof(GPartial), 256);
+    char *scr;
+    QG_TRY(qg_scratch(ctx, miss_b + mcnt_b + poff_b + part_b, &scr));
+    GbSpill sp;
+    sp.miss = (uint2 *)scr;
+    sp.mcnt = (uint32_t *)(scr + miss_b);
+    sp.poff = (uint32_t *)(scr + miss_b + mcnt_b);
+    sp.part = (GPartial *)(scr + miss_b + mcnt_b + poff_b);
+    sp.capm = capm;
+    sp.plog2 = plog2;
+    sp.slog2 = slog2;
+    const size_t smem1 = (size_t)S * 16 + (size_t)P * 4 + (size_t)GB_SKETCH_WORDS * 4;
+    static size_t attr[2] = {0, 0};
+    const bool pred = val2 != nullptr;
+    if (attr[pred] < smem1) {
+        if (pred)
+            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gb_part<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1), "attr");
+        else
+            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_gb_part<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1), "attr");
+        attr[pred] = smem1;
+    }
+    // d_flags is the low word of one control counter; the pass-2 work counter
+    // is the next counter (both cleared together).
+    unsigned int *work = d_flags + 2;
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(d_flags, 0, 16, ctx->stream), "memset flags");
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(d_num, 0, 8, ctx->stream), "memset cursor");
+    qg_pre_launch(ctx);
+    if (pred)
+        k_gb_part<true><<<C, P1_THREADS, smem1, ctx->stream>>>(key, val, val2, lo2, hi2, n, sp, d_flags);
+    else
+        k_gb_part<false><<<C, P1_THREADS, smem1, ctx->stream>>>(key, val, nullptr, 0, 0, n, sp, d_flags);
+    QG_TRY(qg_check_launch(ctx, pred ? "k_gb_part_fused" : "k_gb_part"));
+    const int g2 = P < ctx->sm_count * 6 ? P : ctx->sm_count * 6;
+    qg_pre_launch(ctx);
+    k_gb_merge<<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
+                                                   (unsigned long long *)d_num, o.rec, d_flags, work);
+    return qg_check_launch(ctx, "k_gb_merge");
+}
+
+__global__ void k_gb_flags_to_error(const unsigned int *flags, qg_control *ctl) {
+    if (*flags) qg_record_error(ctl, QG_ERR_TABLE_FULL, QG_SITE_GROUPBY);
 }
 
 extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key,
@@ -473,12 +883,19 @@ extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *ke
                                                   int32_t *gkey, int64_t *gsum, int64_t *gcnt,
                                                   int64_t cap, int order, int64_t *d_num) {
     if (!ctx || n < 0 || cap < 0 || !d_num || (n > 0 && (!key || !val))) return QG_ERR_INVALID;
-    if (order != QG_ORDER_NONE) return QG_ERR_UNSUPPORTED;  // sorted order needs the sync form
+    if (order != QG_ORDER_NONE) return QG_ERR_UNSUPPORTED;  // key order needs the synchronous form
     if ((((uintptr_t)key) | ((uintptr_t)val) | ((uintptr_t)val2)) & 15) return QG_ERR_INVALID;
-    unsigned long long *rec;
-    long long *ts, *tc;
-    return qg_groupby_cols_launch(ctx, key, val, val2, lo2, hi2, n, gkey, gsum, gcnt, cap, order,
-                                  (long long *)d_num, &rec, &ts, &tc);
+    if (n >= (1LL << 32)) return QG_ERR_UNSUPPORTED;
+    GbOut o;
+    QG_TRY(gb_outputs(ctx, gkey, gsum, gcnt, cap, order, &o));
+    if (g_gb_mode == 1)
+        return gb_launch_global(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num);
+    unsigned int *flags = (unsigned int *)&ctx->ctl->counter[2];
+    QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num, flags));
+    // An overflow cannot be redone without a host round trip here: report it
+    // through the error word (qg_ctx_check returns QG_ERR_TABLE_FULL).
+    k_gb_flags_to_error<<<1, 1, 0, ctx->stream>>>(flags, ctx->ctl);
+    return qg_check_launch(ctx, "k_gb_flags_to_error");
 }
 
 extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, const int32_t *val,
@@ -490,28 +907,48 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
         return QG_ERR_INVALID;
     if (order != QG_ORDER_NONE && order != QG_ORDER_KEY) return QG_ERR_INVALID;
     if ((((uintptr_t)key) | ((uintptr_t)val) | ((uintptr_t)val2)) & 15) return QG_ERR_INVALID;
+    if (n >= (1LL << 32)) return QG_ERR_UNSUPPORTED;
     long long *d_num = (long long *)&ctx->ctl->counter[1];
-    unsigned long long *rec = nullptr;
-    long long *tsum = nullptr, *tcnt = nullptr;
-    QG_TRY(qg_groupby_cols_launch(ctx, key, val, val2, lo2, hi2, n, gkey, gsum, gcnt, cap, order,
-                                  d_num, &rec, &tsum, &tcnt));
+    unsigned int *flags = (unsigned int *)&ctx->ctl->counter[2];
+    GbOut o;
+    QG_TRY(gb_outputs(ctx, gkey, gsum, gcnt, cap, order, &o));
     long long g = 0;
-    QG_TRY(qg_read_i64(ctx, d_num, &g));
+    bool global = g_gb_mode == 1;
+    if (!global) {
+        QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num, flags));
+        // counter[1] (groups) and counter[2] (flags) come back together.
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, d_num, 16, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
+        QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+        g = ctx->pinned[0];
+        global = (ctx->pinned[1] & 0xffffffffLL) != 0;
+        ctx->gb_stats[0] = global ? 1u : 0u;
+        ctx->gb_stats[1] = (uint32_t)ctx->pinned[1];
+        ctx->gb_stats[2] = (uint32_t)((unsigned long long)ctx->pinned[1] >> 32);
+        ctx->gb_stats[3] = g_gb_last_capm;
+    } else {
+        ctx->gb_stats[0] = 1u;
+        ctx->gb_stats[1] = ctx->gb_stats[2] = ctx->gb_stats[3] = 0;
+    }
+    if (global) {
+        QG_TRY(gb_launch_global(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num));
+        QG_TRY(qg_read_i64(ctx, d_num, &g));
+    }
     QG_TRY(qg_collect_error(ctx));
     *num_groups = g;
     if (g > cap) return QG_ERR_CAPACITY;
     if (order == QG_ORDER_KEY && g > 1) {
         // Sort (key, index) records, then gather the sums and counts.
-        unsigned long long *tmp = (unsigned long long *)(tcnt + cap);
-        QG_TRY(qg_sort_rec_inplace(ctx, rec, tmp, g));
+        unsigned long long *tmp = (unsigned long long *)(o.c + (cap > 0 ? cap : 1));
+        QG_TRY(qg_sort_rec_inplace(ctx, o.rec, tmp, g));
         int gb = grid_for(ctx, g, 256, 8);
         qg_pre_launch(ctx);
-        k_groupby_gather<<<gb, 256, 0, ctx->stream>>>(rec, g, tsum, tcnt, gkey, (long long *)gsum, (long long *)gcnt);
+        k_groupby_gather<<<gb, 256, 0, ctx->stream>>>(o.rec, g, o.s, o.c, gkey, (long long *)gsum,
+                                                      (long long *)gcnt);
         QG_TRY(qg_check_launch(ctx, "k_groupby_gather"));
         return qg_ctx_check(ctx);
     } else if (order == QG_ORDER_KEY && g == 1) {
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(gsum, tsum, 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(gcnt, tcnt, 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(gsum, o.s, 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(gcnt, o.c, 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
         return qg_ctx_check(ctx);
     }
     return QG_OK;

@@ -19,6 +19,7 @@ struct qg_control {
     unsigned long long counter[6];  // scratch counters (output cursors)
 };
 
+#define QG_MAX_TIMED 4096
 struct qg_ctx {
     cudaStream_t stream;
     int device;
@@ -34,13 +35,14 @@ struct qg_ctx {
     uint32_t spin_limit;
     uint64_t launches;
     bool table_dirty;       // group-by table must be cleared before next use
+    uint32_t gb_stats[4];   // last qg_groupby_cols: path, flags, fullest bucket, bucket cap
     char msg[256];
     // Per-kernel CUDA-event timing (qg_ctx_enable_timing): a pair of events
     // brackets every launch on the context's stream.
     bool timing;
     int ev_used;
-    cudaEvent_t ev[2 * 512];
-    const char *ev_name[512];
+    cudaEvent_t ev[2 * QG_MAX_TIMED];
+    const char *ev_name[QG_MAX_TIMED];
 };
 
 // Record the start event of the next launch (no-op unless timing is on).
@@ -211,6 +213,114 @@ __device__ __forceinline__ uint32_t qg_lb_warp_exclusive(const qg_lookback &lb, 
     return excl;
 }
 
+// Wide look-back: called by the NW*32 threads of warps 0..NW-1, which read
+// NW*32 predecessors per round (one each), synchronising on named barrier 1.
+// The inclusive-prefix frontier then advances NW*32 tiles per L2 round trip
+// instead of 32, which is what bounds a single-pass scan's throughput.
+// s_tmp needs 2*NW words.  Returns the tile's exclusive prefix to every caller.
+template <int NW>
+__device__ __forceinline__ uint32_t qg_lb_wide_exclusive(const qg_lookback &lb, uint32_t tile,
+                                                         uint32_t epoch, uint32_t aggregate,
+                                                         uint32_t *s_tmp) {
+    constexpr int NT = NW * 32;
+    const int t0 = threadIdx.x, lane = t0 & 31, warp = t0 >> 5;
+    if (tile == 0) {
+        if (t0 == 0) qg_st_relaxed_u64(&lb.status[0], qg_lb_word(epoch, QG_LB_PREFIX, aggregate));
+        return 0;
+    }
+    if (t0 == 0) qg_st_relaxed_u64(&lb.status[tile], qg_lb_word(epoch, QG_LB_AGG, aggregate));
+    uint32_t excl = 0;
+    long long pred = (long long)tile - 1;
+    while (true) {
+        const long long j = pred - t0;
+        unsigned long long flag = QG_LB_PREFIX;
+        uint32_t value = 0;
+        if (j >= 0) {
+            uint32_t spins = 0;
+            unsigned long long w;
+            while (true) {
+                w = qg_ld_relaxed_u64(&lb.status[j]);
+                if ((uint32_t)(w >> 34) == (epoch & 0x3fffffffu) && ((w >> 32) & 3ull) != 0) break;
+                if (++spins >= lb.spin_limit) {
+                    qg_record_error(lb.ctl, QG_ERR_TIMEOUT, lb.site);
+                    w = qg_lb_word(epoch, QG_LB_PREFIX, 0);
+                    break;
+                }
+                __nanosleep(20);
+            }
+            flag = (w >> 32) & 3ull;
+            value = (uint32_t)w;
+        }
+        const uint32_t pmask = __ballot_sync(QG_FULL_MASK, flag == QG_LB_PREFIX);
+        if (lane == 0) s_tmp[warp] = pmask ? (uint32_t)(warp * 32 + __ffs(pmask) - 1) : 0xffffffffu;
+        asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
+        uint32_t stop = 0xffffffffu;
+#pragma unroll
+        for (int w = 0; w < NW; w++) stop = min(stop, s_tmp[w]);
+        const uint32_t contrib = ((uint32_t)t0 <= stop) ? value : 0u;
+        const uint32_t ws = __reduce_add_sync(QG_FULL_MASK, contrib);
+        if (lane == 0) s_tmp[NW + warp] = ws;
+        asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
+#pragma unroll
+        for (int w = 0; w < NW; w++) excl += s_tmp[NW + w];
+        asm volatile("bar.sync 1, %0;" ::"r"(NT) : "memory");
+        if (stop != 0xffffffffu) break;
+        pred -= NT;
+    }
+    if (t0 == 0)
+        qg_st_relaxed_u64(&lb.status[tile], qg_lb_word(epoch, QG_LB_PREFIX, excl + aggregate));
+    return excl;
+}
+
+// Called by ALL threads of a single-pass compaction tile after the E per-warp
+// counts (in row order) are in s_woff: turns them into exclusive offsets,
+// runs the wide look-back on warps 0..NW-1 and leaves the tile's output
+// offset in *s_excl; the last tile stores the grand total in *d_count.
+// s_tmp needs 2*NW+1 words.
+template <int E, int NW>
+__device__ __forceinline__ void qg_tile_offsets_wide(uint32_t *s_woff, const qg_lookback &lb,
+                                                     uint32_t tile, uint32_t epoch,
+                                                     uint32_t *s_excl, uint32_t *s_tmp,
+                                                     long long *d_count, uint32_t last_tile) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int PER = (E + 31) / 32;
+        uint32_t loc[PER];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const int e = lane * PER + k;
+            loc[k] = (e < E) ? s_woff[e] : 0u;
+            sum += loc[k];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(QG_FULL_MASK, incl, d);
+            if (lane >= d) incl += t;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+            const int e = lane * PER + k;
+            if (e < E) s_woff[e] = run;
+            run += loc[k];
+        }
+        if (lane == 31) s_tmp[2 * NW] = incl;
+    }
+    __syncthreads();
+    if (warp < NW) {
+        const uint32_t total = s_tmp[2 * NW];
+        const uint32_t excl = qg_lb_wide_exclusive<NW>(lb, tile, epoch, total, s_tmp);
+        if (threadIdx.x == 0) {
+            *s_excl = excl;
+            if (tile == last_tile && d_count) *d_count = (long long)excl + total;
+        }
+    }
+    __syncthreads();
+}
+
 // Called by all threads at kernel end: the last CTA resets the counters.
 __device__ __forceinline__ void qg_lb_end(const qg_lookback &lb) {
     __syncthreads();
@@ -233,7 +343,9 @@ __device__ __forceinline__ void qg_lb_end(const qg_lookback &lb) {
 template <int E>
 __device__ __forceinline__ void qg_tile_compact_offsets(uint32_t *s_woff, const qg_lookback &lb,
                                                         uint32_t tile, uint32_t epoch,
-                                                        uint32_t *s_excl, long long *d_count) {
+                                                        uint32_t *s_excl, long long *d_count,
+                                                        uint32_t last_tile = 0xffffffffu) {
+    if (last_tile == 0xffffffffu) last_tile = gridDim.x - 1;
     const int lane = threadIdx.x & 31;
     constexpr int PER = (E + 31) / 32;
     uint32_t loc[PER];
@@ -261,8 +373,48 @@ __device__ __forceinline__ void qg_tile_compact_offsets(uint32_t *s_woff, const 
     uint32_t excl = qg_lb_warp_exclusive(lb, tile, epoch, total);
     if (lane == 0) {
         *s_excl = excl;
-        if (tile == gridDim.x - 1 && d_count) *d_count = (long long)excl + total;
+        if (tile == last_tile && d_count) *d_count = (long long)excl + total;
     }
+}
+
+// ---- mbarrier / bulk-copy (TMA engine) helpers (PTX ISA: mbarrier, cp.async.bulk)
+__device__ __forceinline__ uint32_t qg_smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void qg_mbar_init(unsigned long long *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(qg_smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void qg_mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void qg_mbar_arrive_expect_tx(unsigned long long *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(qg_smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void qg_mbar_arrive(unsigned long long *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(qg_smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool qg_mbar_try_wait(unsigned long long *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(qg_smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// 1-D bulk copy global -> shared; completes `bytes` of transaction count on
+// `bar`.  Source and destination 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void qg_bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                            unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            qg_smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(qg_smem_u32(bar))
+        : "memory");
 }
 
 // Host side: status words needed for `tiles` tiles.

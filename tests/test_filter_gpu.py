@@ -85,3 +85,16 @@ def test_lookback_timeout_reports_and_recovers(ctx, orc):
         ctx.set_spin_limit(1 << 22)
     got = ctx.filter_range_rec(dev(rin), 0, 50).cpu().numpy()
     assert np.array_equal(got, orc.filter_rec(rin, 0, 50))
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("n", [1, 4095, 4099, 300007, 1 << 22])
+def test_filter_cols_variants(ctx, orc, variant, n):
+    ctx.check(ctx.lib.qg_filter_set_variant(variant), "variant")
+    try:
+        d = datagen.config0_filter(n, seed=n + variant)
+        key, pay = d["key"].numpy(), d["payload"].numpy()
+        got = ctx.filter_cols(dev(key), dev(pay), d["lo"], d["hi"]).cpu().numpy()
+        assert np.array_equal(got, orc.filter_cols(key, pay, d["lo"], d["hi"]))
+    finally:
+        ctx.lib.qg_filter_set_variant(0)

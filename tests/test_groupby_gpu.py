@@ -119,3 +119,69 @@ def test_groupby_config1_full_size(ctx, orc, fused):
     m = (val2 <= 499) if fused else np.ones(key.size, bool)
     assert int(got[2].sum()) == int(m.sum())
     assert int(got[1].sum()) == int(val[m].astype(np.int64).sum())
+
+
+@pytest.fixture
+def knobs(ctx):
+    yield lambda *a: ctx.check(ctx.lib.qg_groupby_set_knobs(*a), "knobs")
+    ctx.lib.qg_groupby_set_knobs(0, 13, 0, 0)
+
+
+@pytest.mark.parametrize("fused", [False, True])
+def test_groupby_global_table_path(ctx, orc, knobs, fused):
+    # mode 1: the single-pass global-table kernel alone
+    knobs(1, 13, 0, 0)
+    d = datagen.config1_groupby(1 << 20, 1 << 16, seed=11)
+    key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
+    v2 = val2 if fused else None
+    got = ctx.groupby_cols(dev(key), dev(val), dev(v2) if fused else None, d["lo2"], d["hi2"], cap=1 << 17)
+    check_groups(got, orc.groupby_cols(key, val, v2, d["lo2"], d["hi2"]))
+
+
+def test_groupby_spill_overflow_falls_back(ctx, orc, knobs):
+    # bucket capacity 1 overflows at once: the call is redone on the global table
+    knobs(0, 8, 4, 1)
+    d = datagen.config1_groupby(1 << 18, 1 << 14, seed=12)
+    key, val = d["key"].numpy(), d["val"].numpy()
+    got = ctx.groupby_cols(dev(key), dev(val), cap=1 << 15)
+    check_groups(got, orc.groupby_cols(key, val))
+
+
+def test_groupby_async_overflow_reports_table_full(ctx, knobs):
+    from ctypes import c_void_p
+
+    from query_on_opencl_fpga_gb300 import QGError
+
+    knobs(0, 8, 4, 1)
+    n = 1 << 16
+    key = torch.arange(n, dtype=torch.int32, device="cuda")
+    out_k = torch.empty(n, dtype=torch.int32, device="cuda")
+    out_s = torch.empty(n, dtype=torch.int64, device="cuda")
+    out_c = torch.empty(n, dtype=torch.int64, device="cuda")
+    d_num = torch.zeros(1, dtype=torch.int64, device="cuda")
+    p = lambda t: c_void_p(t.data_ptr())  # noqa: E731
+    st = ctx.lib.qg_groupby_cols_async(ctx.handle, p(key), p(key), c_void_p(0), 0, 0, n, p(out_k), p(out_s),
+                                       p(out_c), n, QG_ORDER_NONE, p(d_num))
+    assert st == 0
+    with pytest.raises(QGError) as e:
+        ctx.device_check()
+    assert e.value.status == 4
+
+
+@pytest.mark.parametrize("hot,parts", [(8, 1), (10, 6), (13, 12), (13, 13)])
+def test_groupby_knob_sweep(ctx, orc, knobs, hot, parts):
+    knobs(0, hot, parts, 0)
+    d = datagen.config1_groupby(1 << 19, 1 << 15, seed=hot + parts)
+    key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
+    got = ctx.groupby_cols(dev(key), dev(val), dev(val2), d["lo2"], d["hi2"], cap=1 << 16)
+    check_groups(got, orc.groupby_cols(key, val, val2, d["lo2"], d["hi2"]))
+
+
+def test_groupby_config1_takes_two_pass_path(ctx):
+    # The full config-1 input must be handled by the two-pass path (no fallback).
+    d = datagen.config1_groupby(1 << 26, 1 << 20, seed=0, device="cuda")
+    for v2 in (None, d["val2"]):
+        ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=1 << 21, order=QG_ORDER_NONE)
+        st = ctx.groupby_stats()
+        assert st["path"] == "two_pass", st
+        assert st["fullest_bucket"] <= st["bucket_cap"], st
