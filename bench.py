@@ -441,8 +441,10 @@ def run_only(args):
         fn = lambda: ctx.sort_rec(rec)  # noqa: E731
     else:
         raise SystemExit(f"unknown --only {args.only}")
-    if args.variant >= 0:
+    if args.variant >= 0 and args.only == "filter":
         ctx.check(ctx.lib.qg_filter_set_variant(args.variant), "qg_filter_set_variant")
+    if args.variant >= 0 and args.only in ("groupby", "fused"):
+        ctx.check(ctx.lib.qg_groupby_set_knobs(args.variant, 13, 0, 0), "qg_groupby_set_knobs")
     ms, kern, launches = timed(ctx, fn, args.steps, args.warmup, 1, stream)
     extra = {"groupby_stats": ctx.groupby_stats()} if args.only in ("groupby", "fused") else {}
     print(json.dumps({"only": args.only, "rows": n, "variant": args.variant, "ms_per_op": ms,

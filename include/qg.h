@@ -140,7 +140,9 @@ QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key, const in
 
 /* Tuning of qg_groupby_cols (process-wide).  mode 0: two-pass shared-memory
  * aggregation with the global-table kernel as automatic fallback; mode 1:
- * global-table kernel only.  hot_slots_log2: per-SM shared-memory table
+ * global-table kernel only; mode 2: as 0 but the int64 sums use 64-bit shared
+ * atomics instead of two 32-bit words with explicit carry (slower on GB300,
+ * kept for comparison).  hot_slots_log2: per-SM shared-memory table
  * (8..13); partitions_log2: spill partitions (0 = chosen from cap, else
  * 1..13); bucket_cap: spill bucket capacity (0 = automatic; a small value
  * forces the fallback, for testing). */

@@ -168,9 +168,10 @@ def test_groupby_async_overflow_reports_table_full(ctx, knobs):
     assert e.value.status == 4
 
 
+@pytest.mark.parametrize("mode", [0, 2])
 @pytest.mark.parametrize("hot,parts", [(8, 1), (10, 6), (13, 12), (13, 13)])
-def test_groupby_knob_sweep(ctx, orc, knobs, hot, parts):
-    knobs(0, hot, parts, 0)
+def test_groupby_knob_sweep(ctx, orc, knobs, hot, parts, mode):
+    knobs(mode, hot, parts, 0)
     d = datagen.config1_groupby(1 << 19, 1 << 15, seed=hot + parts)
     key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
     got = ctx.groupby_cols(dev(key), dev(val), dev(val2), d["lo2"], d["hi2"], cap=1 << 16)
