@@ -96,6 +96,23 @@ QG_API qg_status qg_filter_cols_async(qg_ctx *ctx, const int32_t *key, const int
                                       int64_t n, int32_t lo, int32_t hi, int32_t *out_pairs,
                                       int64_t cap, int64_t *d_out_n);
 
+/* Column filter that allocates nothing.  No counterpart in the reference.
+ * For callers that cannot allocate device memory (inside an allocator or
+ * memory-pool callback, under a framework that owns all device memory, on a
+ * path that must not block on the allocator) and therefore cannot create a
+ * qg_ctx: same result as qg_filter_cols_async, but the kernel's scratch (its
+ * look-back status words and counters) is a fixed device array inside the
+ * library, sized for n <= 2^26 rows (larger n returns QG_ERR_UNSUPPORTED);
+ * each GPU that loads the library keeps about 128 KB for it until exit.  The
+ * first call on a device looks the array's address up (make that call before
+ * any stream capture).  All calls share the array: calls that overlap on the
+ * GPU race.  The selected-row count goes to the device int64 *d_out_n; a
+ * device-side wait that gave up is reported there as -QG_ERR_TIMEOUT.
+ * `stream` is a cudaStream_t (NULL = legacy default stream). */
+QG_API qg_status qg_filter_cols_noalloc(const int32_t *key, const int32_t *payload, int64_t n,
+                                        int32_t lo, int32_t hi, int32_t *out_pairs, int64_t cap,
+                                        int64_t *d_out_n, void *stream);
+
 /* Column filter kernel choice (process-wide): 0 = one 4096-row tile per CTA
  * held in registers, 1 = persistent CTAs streaming tiles through a 3-stage
  * bulk-copy (TMA) ring.  Results are identical. */

@@ -49,6 +49,8 @@ SIGNATURES: dict[str, tuple] = {
     "qg_filter_cols_async": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_int32,
                                      c_void_p, c_int64, c_void_p]),
     "qg_filter_set_variant": (c_int, [c_int]),
+    "qg_filter_cols_noalloc": (c_int, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int64,
+                                       c_void_p, c_void_p]),
     "qg_scan_excl_i32": (c_int, [c_void_p, c_void_p, c_void_p, c_int64]),
     "qg_sort_rec_by_y": (c_int, [c_void_p, c_void_p, c_int64]),
     "qg_groupby_rec": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,

@@ -374,3 +374,90 @@ QG_API qg_status qg_filter_cols(qg_ctx *ctx, const int32_t *key, const int32_t *
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Column filter that allocates nothing.
+//
+// For callers that cannot allocate device memory themselves -- code running
+// inside an allocator or memory-pool callback, in a process whose device
+// memory is carved up by a framework that forbids extra cudaMalloc calls, or
+// on a path that must never block on the allocator -- and so cannot create a
+// qg_ctx (qg_ctx_create allocates its control block and scratch).  The
+// look-back status words and the control block this kernel needs live in the
+// file-scope device array below instead, sized for at most
+// QG_NOALLOC_MAX_ROWS rows; every GPU that loads the library holds it
+// (about 128 KB) until the process exits.
+//
+// Host code only sees a stand-in for the array, not its device address, so
+// the first call on a device (with that device current) looks the address up
+// with cudaGetSymbolAddress and keeps it; make that first call before any
+// stream capture.  Every call shares the one array: the counters and the
+// status words the call uses are cleared at the start of each call (stream
+// ordered), and calls that overlap on the GPU (on different streams, or from
+// different threads without ordering) race on it.
+// ---------------------------------------------------------------------------
+#define QG_NOALLOC_MAX_ROWS (1LL << 26)
+#define QG_NOALLOC_MAX_TILES (QG_NOALLOC_MAX_ROWS / 4096)
+#define QG_NOALLOC_MAX_DEVICES 64
+
+struct qg_noalloc_scratch {
+    qg_control ctl;
+    unsigned long long status[QG_NOALLOC_MAX_TILES];
+};
+
+static __device__ __align__(256) qg_noalloc_scratch g_noalloc_scratch;
+
+static qg_noalloc_scratch *g_noalloc_addr[QG_NOALLOC_MAX_DEVICES];
+
+// Reports a device-side error of the call through the count (as -code) and
+// clears the error word for the next call.
+__global__ void k_noalloc_report(qg_noalloc_scratch *s, long long *d_count) {
+    const int e = s->ctl.err;
+    if (e) {
+        *d_count = -(long long)e;
+        s->ctl.err = 0;
+        s->ctl.err_site = 0;
+    }
+}
+
+extern "C" QG_API qg_status qg_filter_cols_noalloc(const int32_t *key, const int32_t *pay, int64_t n,
+                                                   int32_t lo, int32_t hi, int32_t *out,
+                                                   int64_t cap, int64_t *d_out_n, void *stream) {
+    constexpr int TILE = FT_THREADS * COL_ROUNDS * 4;
+    if (n < 0 || cap < 0 || !d_out_n || (n > 0 && (!key || !pay || !out))) return QG_ERR_INVALID;
+    if (n > QG_NOALLOC_MAX_ROWS) return QG_ERR_UNSUPPORTED;
+    if (((uintptr_t)key & 15) || ((uintptr_t)pay & 15) || ((uintptr_t)out & 7) ||
+        ((uintptr_t)d_out_n & 7))
+        return QG_ERR_INVALID;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= QG_NOALLOC_MAX_DEVICES) {
+        cudaGetLastError();
+        return QG_ERR_CUDA;
+    }
+    if (!g_noalloc_addr[dev]) {  // set-up, once per device
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return QG_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = (qg_noalloc_scratch *)p;
+    }
+    qg_noalloc_scratch *s = g_noalloc_addr[dev];
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n == 0)
+        return cudaMemsetAsync(d_out_n, 0, sizeof(long long), st) == cudaSuccess ? QG_OK : QG_ERR_CUDA;
+    const long long tiles = (n + TILE - 1) / TILE;
+    // Counters and error word start at zero; status words of this call's
+    // tiles are cleared so nothing from an earlier call can be read as ready.
+    if (cudaMemsetAsync(&s->ctl, 0, sizeof(qg_control), st) != cudaSuccess ||
+        cudaMemsetAsync(s->status, 0, (size_t)tiles * sizeof(unsigned long long), st) != cudaSuccess) {
+        cudaGetLastError();
+        return QG_ERR_CUDA;
+    }
+    qg_lookback lb{s->status, &s->ctl, 1u << 22, QG_SITE_FILTER};
+    k_filter_cols<COL_ROUNDS><<<(unsigned)tiles, FT_THREADS, 0, st>>>(
+        key, pay, n, lo, hi, (int2 *)out, cap, (long long *)d_out_n, lb);
+    k_noalloc_report<<<1, 1, 0, st>>>(s, (long long *)d_out_n);
+    if (cudaGetLastError() != cudaSuccess) return QG_ERR_CUDA;
+    return QG_OK;
+}
