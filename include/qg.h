@@ -138,6 +138,23 @@ QG_API qg_status qg_groupby_rec(qg_ctx *ctx, const void *in_records, int64_t n, 
 QG_API qg_status qg_aggregate_groups(qg_ctx *ctx, const void *sorted_records, int64_t n,
                                      const int32_t *startPos, int64_t num_groups, int op,
                                      int32_t *agg);
+/* The same for groups [first, first+count) only (parallelAggregate_init's
+ * blockOffset / numBlock chunks, host/host/testAggAfterGB.cpp:69-91);
+ * agg is indexed by absolute group number. */
+QG_API qg_status qg_aggregate_group_range(qg_ctx *ctx, const void *sorted_records, int64_t n,
+                                          const int32_t *startPos, int64_t num_groups,
+                                          int64_t first, int64_t count, int op, int32_t *agg);
+
+/* ---- gather / scatter (gatherImpl / scatterImpl, host/host/testScatter.cpp:63-137;
+ * optGather_kernel body: kernel/aggregation/1/group_by_cu_op_dp.cl:860-872)
+ * gather : S[i] = R[loc[i*loc_stride]] for i < sLen when 0 <= loc < rLen (else S[i] kept)
+ * scatter: S[loc[i*loc_stride]] = R[i] for i < rLen when 0 <= loc < sLen
+ * R and S are Records; loc_stride 2 with loc = (int32_t*)records + 0 uses the
+ * records' .x as the location. */
+QG_API qg_status qg_gather_rec(qg_ctx *ctx, const void *R, int64_t rLen, const int32_t *loc,
+                               int64_t loc_stride, int64_t sLen, void *S);
+QG_API qg_status qg_scatter_rec(qg_ctx *ctx, const void *R, int64_t rLen, const int32_t *loc,
+                                int64_t loc_stride, void *S, int64_t sLen);
 
 /* ---- column group-by + aggregate, optionally fused with a filter (configs 1, 1-fused)
  * Groups rows by key, SUM(val) as int64 and COUNT as int64.  When val2 is not

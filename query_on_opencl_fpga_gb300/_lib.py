@@ -56,6 +56,10 @@ SIGNATURES: dict[str, tuple] = {
     "qg_groupby_rec": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                POINTER(c_int64)]),
     "qg_aggregate_groups": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int, c_void_p]),
+    "qg_aggregate_group_range": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int64, c_int64,
+                                         c_int, c_void_p]),
+    "qg_gather_rec": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int64, c_void_p]),
+    "qg_scatter_rec": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64]),
     "qg_groupby_cols": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32, c_int64,
                                 c_void_p, c_void_p, c_void_p, c_int64, c_int, POINTER(c_int64)]),
     "qg_groupby_cols_async": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
@@ -68,6 +72,77 @@ SIGNATURES: dict[str, tuple] = {
     "qg_hash_join_ref": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64,
                                  POINTER(c_int64)]),
 }
+
+class QgBuf(ctypes.Structure):
+    """qg_buf (include/qg_ref.h): the cl_mem stand-in, device pointer + bytes."""
+    _fields_ = [("ptr", c_void_p), ("bytes", c_size_t)]
+
+
+class ScanPara(ctypes.Structure):
+    _fields_ = [("pass_", c_uint32), ("gLength", c_uint32), ("blockSize", c_uint32)]
+
+
+_PB = POINTER(QgBuf)
+_PI = POINTER(c_int)
+_c = c_int
+# The reference's operator surface (include/qg_ref.h).
+SIGNATURES.update({
+    "qg_ref_last_status": (c_int, []),
+    "qg_ref_default_ctx": (c_void_p, []),
+    "qg_buf_alloc": (c_int, [_PB, c_size_t]),
+    "qg_buf_free": (None, [_PB]),
+    "filterImpl": (None, [QgBuf, _c, _c, _PB, _PI, _c, _c, _c, _c, c_void_p]),
+    "range_selection": (c_int, [QgBuf, _c, _c, _c, _PB, _c, _c, c_void_p]),
+    "CL_RangeSelection": (c_int, [c_void_p, _c, _c, _c, POINTER(c_void_p), _c, _c, _c]),
+    "initScan": (None, [_c, POINTER(ScanPara)]),
+    "scanImpl": (None, [QgBuf, _c, QgBuf, POINTER(ScanPara), c_void_p]),
+    "closeScan": (None, [POINTER(ScanPara)]),
+    "radixSortImpl_sm": (None, [QgBuf, _c, _c, _c, _c, c_void_p]),
+    "CL_RadixSort": (None, [c_void_p, _c, c_void_p, _c, _c, _c]),
+    "groupByImpl": (c_int, [QgBuf, _c, QgBuf, _PB, _c, _c, c_void_p]),
+    "CL_GroupBy": (c_int, [c_void_p, _c, c_void_p, POINTER(c_void_p), _c, _c, _c]),
+    "parallelAggregate_init": (None, [QgBuf, QgBuf, QgBuf, _c, _c, _c, _c, _c, _c, _c, c_void_p]),
+    "aggAfterGroupByImpl": (None, [QgBuf, _c, QgBuf, _c, QgBuf, QgBuf, _c, _c, c_void_p]),
+    "CL_agg_max_afterGroupBy": (None, [c_void_p, _c, c_void_p, _c, c_void_p, c_void_p, _c, _c]),
+    "CL_agg_min_afterGroupBy": (None, [c_void_p, _c, c_void_p, _c, c_void_p, c_void_p, _c, _c]),
+    "CL_agg_sum_afterGroupBy": (None, [c_void_p, _c, c_void_p, _c, c_void_p, c_void_p, _c, _c]),
+    "CL_agg_avg_afterGroupBy": (None, [c_void_p, _c, c_void_p, _c, c_void_p, c_void_p, _c, _c]),
+    "gatherImpl": (None, [QgBuf, _c, QgBuf, QgBuf, _c, _c, _c, c_void_p]),
+    "scatterImpl": (None, [QgBuf, _c, QgBuf, QgBuf, _c, _c, c_void_p]),
+})
+
+PLAN_MAX_OPS = 16
+PLAN_MAX_IMAGES = 16
+
+
+class PlanKernel(ctypes.Structure):
+    _fields_ = [("kernel_id", c_int), ("variant", c_int)]
+
+
+class PlanImage(ctypes.Structure):
+    _fields_ = [("num_kernels", c_int), ("kernels", PlanKernel * PLAN_MAX_OPS),
+                ("luts", c_int), ("regs", c_int), ("rams", c_int), ("dsps", c_int),
+                ("total_unit_cost", ctypes.c_float), ("exec_time", ctypes.c_float),
+                ("freq", ctypes.c_float), ("mem_inc", ctypes.c_float), ("reconfig_time", ctypes.c_float)]
+
+
+class Plan(ctypes.Structure):
+    _fields_ = [("exec_time", ctypes.c_float), ("image_num", c_int), ("images", PlanImage * PLAN_MAX_IMAGES)]
+
+
+class PlanVariant(ctypes.Structure):
+    _fields_ = [("name", c_char_p), ("kernel_id", c_int), ("lut", c_int), ("reg", c_int), ("ram", c_int),
+                ("dsp", c_int), ("unit_cost", ctypes.c_float), ("mem_add", ctypes.c_float),
+                ("mem_sub", ctypes.c_float)]
+
+
+# The planner (include/qg_plan.h); host-only, needs no GPU.
+SIGNATURES.update({
+    "qg_plan_dp": (c_int, [POINTER(c_int), c_int, ctypes.c_float, POINTER(Plan)]),
+    "qg_plan_pipeline": (c_int, [c_int, ctypes.c_float, POINTER(Plan)]),
+    "qg_plan_variant_name": (c_char_p, [c_int, c_int]),
+    "qg_plan_set_table": (c_int, [POINTER(PlanVariant), c_int, c_int]),
+})
 
 _lib = None
 

@@ -99,31 +99,36 @@ __device__ __forceinline__ int32_t agg_identity(int op) {
     return op == QG_REDUCE_MIN ? (1 << 30) : 0;
 }
 
-__global__ void k_agg_init(int32_t *agg, long long g, int op) {
+__global__ void k_agg_init(int32_t *agg, long long g0, long long g1, int op) {
     long long stride = (long long)gridDim.x * blockDim.x;
     int32_t id = agg_identity(op);
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g; i += stride) agg[i] = id;
+    for (long long i = g0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g1; i += stride)
+        agg[i] = id;
 }
 
+// Groups [g0, g1) of G: rows [startPos[g0], startPos[g1] or n) in chunks of
+// AGG_CHUNK rows counted from the range start.
 __global__ void __launch_bounds__(256)
 k_agg_chunks(const uint2 *__restrict__ rec, long long n, const int32_t *__restrict__ startPos,
-             long long G, int op, int32_t *__restrict__ agg) {
+             long long G, long long g0, long long g1, int op, int32_t *__restrict__ agg) {
     const int lane = threadIdx.x & 31;
     const long long warp_id = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const long long nchunks = (n + AGG_CHUNK - 1) / AGG_CHUNK;
+    const long long rs = __ldg(&startPos[g0]);
+    const long long re = (g1 == G) ? n : (long long)__ldg(&startPos[g1]);
+    const long long nchunks = (re - rs + AGG_CHUNK - 1) / AGG_CHUNK;
     for (long long c = warp_id; c < nchunks; c += nwarps) {
-        const long long cs = c * AGG_CHUNK;
-        const long long ce = (cs + AGG_CHUNK < n) ? cs + AGG_CHUNK : n;
-        // last group starting at or before cs
-        long long lo = 0, hi = G - 1;
+        const long long cs = rs + c * AGG_CHUNK;
+        const long long ce = (cs + AGG_CHUNK < re) ? cs + AGG_CHUNK : re;
+        // last group of the range starting at or before cs
+        long long lo = g0, hi = g1 - 1;
         while (lo < hi) {
             long long mid = (lo + hi + 1) >> 1;
             if ((long long)__ldg(&startPos[mid]) <= cs) lo = mid; else hi = mid - 1;
         }
         long long g = lo;
         long long pos = cs;
-        while (pos < ce && g < G) {
+        while (pos < ce && g < g1) {
             const long long gs = __ldg(&startPos[g]);
             const long long ge = (g == G - 1) ? n : (long long)__ldg(&startPos[g + 1]);
             const long long se = ge < ce ? ge : ce;
@@ -156,11 +161,12 @@ k_agg_chunks(const uint2 *__restrict__ rec, long long n, const int32_t *__restri
 
 // AVG of groups that spanned chunks: the atomics left the wrapped sum.
 __global__ void k_agg_avg_finish(const int32_t *__restrict__ startPos, long long n, long long G,
-                                 int32_t *__restrict__ agg) {
+                                 long long g0, long long g1, int32_t *__restrict__ agg) {
     long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < G; g += stride) {
+    const long long rs = startPos[g0];
+    for (long long g = g0 + (long long)blockIdx.x * blockDim.x + threadIdx.x; g < g1; g += stride) {
         long long gs = startPos[g], ge = (g == G - 1) ? n : startPos[g + 1];
-        bool spans = (gs / AGG_CHUNK) != ((ge - 1) / AGG_CHUNK);
+        bool spans = ((gs - rs) / AGG_CHUNK) != ((ge - 1 - rs) / AGG_CHUNK);
         if (spans) agg[g] = agg[g] / (int32_t)(ge - gs);
     }
 }
@@ -729,27 +735,37 @@ extern "C" QG_API qg_status qg_groupby_rec(qg_ctx *ctx, const void *in, int64_t 
     return s;
 }
 
-extern "C" QG_API qg_status qg_aggregate_groups(qg_ctx *ctx, const void *sorted, int64_t n,
-                                                const int32_t *startPos, int64_t G, int op,
-                                                int32_t *agg) {
-    if (!ctx || n < 0 || G < 0 || op < 0 || op > 3) return QG_ERR_INVALID;
-    if (G == 0) return QG_OK;
+extern "C" QG_API qg_status qg_aggregate_group_range(qg_ctx *ctx, const void *sorted, int64_t n,
+                                                     const int32_t *startPos, int64_t G,
+                                                     int64_t first, int64_t count, int op,
+                                                     int32_t *agg) {
+    if (!ctx || n < 0 || G < 0 || op < 0 || op > 3 || first < 0 || count < 0 || first + count > G)
+        return QG_ERR_INVALID;
+    if (count == 0) return QG_OK;
     if (!sorted || !startPos || !agg || n == 0) return QG_ERR_INVALID;
-    int ib = grid_for(ctx, G, 256, 8);
+    const long long g0 = first, g1 = first + count;
+    int ib = grid_for(ctx, count, 256, 8);
     qg_pre_launch(ctx);
-    k_agg_init<<<ib, 256, 0, ctx->stream>>>(agg, G, op);
+    k_agg_init<<<ib, 256, 0, ctx->stream>>>(agg, g0, g1, op);
     QG_TRY(qg_check_launch(ctx, "k_agg_init"));
+    // The row range is only known on the device; size the grid for all rows.
     long long chunks = (n + AGG_CHUNK - 1) / AGG_CHUNK;
     int blocks = grid_for(ctx, chunks * 32, 256, 8);
     qg_pre_launch(ctx);
-    k_agg_chunks<<<blocks, 256, 0, ctx->stream>>>((const uint2 *)sorted, n, startPos, G, op, agg);
+    k_agg_chunks<<<blocks, 256, 0, ctx->stream>>>((const uint2 *)sorted, n, startPos, G, g0, g1, op, agg);
     QG_TRY(qg_check_launch(ctx, "k_agg_chunks"));
     if (op == QG_REDUCE_AVERAGE) {
         qg_pre_launch(ctx);
-        k_agg_avg_finish<<<ib, 256, 0, ctx->stream>>>(startPos, n, G, agg);
+        k_agg_avg_finish<<<ib, 256, 0, ctx->stream>>>(startPos, n, G, g0, g1, agg);
         QG_TRY(qg_check_launch(ctx, "k_agg_avg_finish"));
     }
     return qg_ctx_check(ctx);
+}
+
+extern "C" QG_API qg_status qg_aggregate_groups(qg_ctx *ctx, const void *sorted, int64_t n,
+                                                const int32_t *startPos, int64_t G, int op,
+                                                int32_t *agg) {
+    return qg_aggregate_group_range(ctx, sorted, n, startPos, G, 0, G, op, agg);
 }
 
 
