@@ -430,7 +430,8 @@ def run_only(args):
         fn = lambda: ctx.filter_cols(f["key"], f["payload"], f["lo"], f["hi"])  # noqa: E731
     elif args.only == "join":
         n = rows or (1 << 28)
-        j = datagen.config2_join(min(1 << 24, max(n // 16, 1)), n, seed=0, device="cuda")
+        nr = args.rows2 or min(1 << 24, max(n // 16, 1))
+        j = datagen.config2_join(nr, n, seed=0, device="cuda")
         fn = lambda: ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"],  # noqa: E731
                                           j["shi"], cap=int(n * 0.26) + 1024)
     elif args.only == "sort":
@@ -459,6 +460,7 @@ def main():
     ap.add_argument("--only", default=None, help="groupby|fused|filter|join|sort: one operator alone")
     ap.add_argument("--rows", type=int, default=0, help="row count for --only (default: the config size)")
     ap.add_argument("--variant", type=int, default=-1, help="column filter kernel variant for --only filter")
+    ap.add_argument("--rows2", type=int, default=0, help="build-side rows for --only join")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
