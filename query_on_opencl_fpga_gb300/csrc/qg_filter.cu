@@ -36,23 +36,26 @@ k_filter_rec(const uint4 *__restrict__ in, long long n, int32_t lo, int32_t hi,
     uint4 v[ROUNDS];
     uint32_t fl = 0;            // bit 2r: first record of round r, bit 2r+1: second
     uint32_t lpre[ROUNDS];      // selected records of lower lanes in this round
+    // Every load of the tile is issued before the first ballot, so the
+    // rounds' DRAM latencies overlap instead of adding up.
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         long long idx = base + (long long)(r * FT_THREADS + tid) * 2;
-        bool f0 = false, f1 = false;
         if (idx + 1 < n) {
             int4 t = qg_ldg_stream(reinterpret_cast<const int4 *>(in) + (idx >> 1));
             v[r] = make_uint4(t.x, t.y, t.z, t.w);
-            f0 = ((int32_t)v[r].y >= lo) & ((int32_t)v[r].y <= hi);
-            f1 = ((int32_t)v[r].w >= lo) & ((int32_t)v[r].w <= hi);
         } else if (idx < n) {
-            const uint2 *in2 = reinterpret_cast<const uint2 *>(in);
-            uint2 a = in2[idx];
+            uint2 a = reinterpret_cast<const uint2 *>(in)[idx];
             v[r] = make_uint4(a.x, a.y, 0, 0);
-            f0 = ((int32_t)a.y >= lo) & ((int32_t)a.y <= hi);
         } else {
             v[r] = make_uint4(0, 0, 0, 0);
         }
+    }
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        long long idx = base + (long long)(r * FT_THREADS + tid) * 2;
+        bool f0 = (idx < n) & ((int32_t)v[r].y >= lo) & ((int32_t)v[r].y <= hi);
+        bool f1 = (idx + 1 < n) & ((int32_t)v[r].w >= lo) & ((int32_t)v[r].w <= hi);
         uint32_t b0 = __ballot_sync(QG_FULL_MASK, f0), b1 = __ballot_sync(QG_FULL_MASK, f1);
         lpre[r] = __popc(b0 & lt) + __popc(b1 & lt);
         if (lane == 0) s_woff[r * FT_WARPS + warp] = __popc(b0) + __popc(b1);
@@ -98,10 +101,10 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
     int4 kv[ROUNDS], pv[ROUNDS];
     uint32_t fl = 0;  // bit 4r+j
     uint32_t lpre[ROUNDS];
+    // All loads first (see k_filter_rec), then the predicates and ballots.
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         long long idx = base + (long long)(r * FT_THREADS + tid) * 4;
-        uint32_t f = 0;
         if (idx + 3 < n) {
             kv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(key + idx));
             pv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(pay + idx));
@@ -112,6 +115,11 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
             kv[r] = make_int4(t[0], t[1], t[2], t[3]);
             pv[r] = make_int4(p[0], p[1], p[2], p[3]);
         }
+    }
+#pragma unroll
+    for (int r = 0; r < ROUNDS; r++) {
+        long long idx = base + (long long)(r * FT_THREADS + tid) * 4;
+        uint32_t f = 0;
         f |= (uint32_t)((kv[r].x >= lo) & (kv[r].x <= hi) & (idx + 0 < n)) << 0;
         f |= (uint32_t)((kv[r].y >= lo) & (kv[r].y <= hi) & (idx + 1 < n)) << 1;
         f |= (uint32_t)((kv[r].z >= lo) & (kv[r].z <= hi) & (idx + 2 < n)) << 2;

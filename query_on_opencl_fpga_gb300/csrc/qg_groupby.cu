@@ -50,22 +50,29 @@ k_group_bounds(const uint4 *__restrict__ in, long long n, int32_t *__restrict__ 
     const uint32_t lt = qg_lanemask_lt();
     const uint2 *in2 = reinterpret_cast<const uint2 *>(in);
     uint32_t fl = 0, lpre[GBD_ROUNDS];
+    // Loads of all rounds first (keys of the thread's pair and of the record
+    // before it), then the ballots, so the DRAM latencies overlap.
+    uint32_t k0[GBD_ROUNDS], k1[GBD_ROUNDS], kp[GBD_ROUNDS];
 #pragma unroll
     for (int r = 0; r < GBD_ROUNDS; r++) {
         long long idx = base + (long long)(r * GBD_THREADS + tid) * 2;
-        bool f0 = false, f1 = false;
+        k0[r] = k1[r] = kp[r] = 0;
         if (idx < n) {
-            uint32_t k0, k1 = 0;
             if (idx + 1 < n) {
                 int4 t = qg_ldg_stream(reinterpret_cast<const int4 *>(in) + (idx >> 1));
-                k0 = (uint32_t)t.y;
-                k1 = (uint32_t)t.w;
-                f1 = k1 != k0;
+                k0[r] = (uint32_t)t.y;
+                k1[r] = (uint32_t)t.w;
             } else {
-                k0 = in2[idx].y;
+                k0[r] = in2[idx].y;
             }
-            f0 = (idx == 0) || (__ldg(&in2[idx - 1].y) != k0);
+            if (idx > 0) kp[r] = __ldg(&in2[idx - 1].y);
         }
+    }
+#pragma unroll
+    for (int r = 0; r < GBD_ROUNDS; r++) {
+        long long idx = base + (long long)(r * GBD_THREADS + tid) * 2;
+        bool f0 = (idx < n) && ((idx == 0) || (kp[r] != k0[r]));
+        bool f1 = (idx + 1 < n) && (k1[r] != k0[r]);
         uint32_t b0 = __ballot_sync(QG_FULL_MASK, f0), b1 = __ballot_sync(QG_FULL_MASK, f1);
         lpre[r] = __popc(b0 & lt) + __popc(b1 & lt);
         if (lane == 0) s_woff[r * GBD_WARPS + warp] = __popc(b0) + __popc(b1);
@@ -432,6 +439,15 @@ __device__ __forceinline__ int4 ldg_stream_ef(const int4 *p, unsigned long long 
 __device__ __forceinline__ uint32_t gb_h1(uint32_t k) { return k * 0x9E3779B1u; }
 __device__ __forceinline__ uint32_t gb_h2(uint32_t k) { return (k ^ (k >> 16)) * 0x85EBCA77u; }
 
+// Word index of slot s's low and high sum halves in a table of `slots` slots.
+// SUM64 interleaves them (one 8-byte atomic per add); the carry scheme keeps
+// two separate arrays so that the low words of neighbouring slots fall in
+// different banks.
+template <bool SUM64>
+__device__ __forceinline__ uint32_t gb_lo(uint32_t s) { return SUM64 ? 2 * s : s; }
+template <bool SUM64>
+__device__ __forceinline__ uint32_t gb_hi(uint32_t s, uint32_t slots) { return SUM64 ? 2 * s + 1 : slots + s; }
+
 // Shared-memory accumulator update.  SUM64: one 64-bit shared atomic add;
 // otherwise the two-word carry scheme of smem_add_i64.
 template <bool SUM64>
@@ -469,8 +485,8 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
     for (int i = tid; i < S; i += P1_THREADS) {
         hk[i] = SM_EMPTY;
         hc[i] = 0;
-        hsum[2 * i] = 0;
-        hsum[2 * i + 1] = 0;
+        hsum[gb_lo<SUM64>(i)] = 0;
+        hsum[gb_hi<SUM64>(i, S)] = 0;
     }
     for (int i = tid; i < P; i += P1_THREADS) cur[i] = 0;
     for (int i = tid; i < GB_SKETCH_WORDS; i += P1_THREADS) sk[i] = 0;
@@ -479,8 +495,19 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
     uint2 *mine = sp.miss + (size_t)c * P * capm;
     const unsigned long long pol = l2_evict_first_policy();
 
-    auto process = [&](int32_t k, int32_t v) {
-        const uint32_t uk = (uint32_t)k;
+    // A row whose key is in the table only adds; any other row goes through
+    // admission and, failing that, the spill bucket of its partition.
+    auto try_hit = [&](uint32_t uk, int32_t v) -> bool {
+        if (uk == SM_EMPTY) return false;
+        const uint32_t b = gb_h1(uk) >> bshift;
+        const uint4 w = reinterpret_cast<const uint4 *>(hk)[b];
+        const int way = (w.x == uk) ? 0 : (w.y == uk) ? 1 : (w.z == uk) ? 2 : (w.w == uk) ? 3 : -1;
+        if (way < 0) return false;
+        const uint32_t s = b * 4 + way;
+        gb_acc<SUM64>(&hc[s], &hsum[gb_lo<SUM64>(s)], &hsum[gb_hi<SUM64>(s, S)], 1u, (long long)v);
+        return true;
+    };
+    auto miss = [&](uint32_t uk, int32_t v) {
         const uint32_t h = gb_h1(uk);
         const uint32_t b = h >> bshift;
         if (uk != SM_EMPTY) {
@@ -503,7 +530,7 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
             }
             if (way >= 0) {
                 const uint32_t s = b * 4 + way;
-                gb_acc<SUM64>(&hc[s], &hsum[2 * s], &hsum[2 * s + 1], 1u, (long long)v);
+                gb_acc<SUM64>(&hc[s], &hsum[gb_lo<SUM64>(s)], &hsum[gb_hi<SUM64>(s, S)], 1u, (long long)v);
                 return;
             }
         }
@@ -511,6 +538,9 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
         const uint32_t pos = atomicAdd(&cur[p], 1u);
         if (pos < capm) mine[(size_t)p * capm + pos] = make_uint2(uk, (uint32_t)v);
         else atomicOr(flags, 1u);
+    };
+    auto process = [&](int32_t k, int32_t v) {
+        if (!try_hit((uint32_t)k, v)) miss((uint32_t)k, v);
     };
 
     const long long nv = n >> 2;
@@ -530,17 +560,16 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
             v4n = ldg_stream_ef(reinterpret_cast<const int4 *>(val) + qn, pol);
             if (PRED) w4n = ldg_stream_ef(reinterpret_cast<const int4 *>(val2) + qn, pol);
         }
-        bool m0 = true, m1 = true, m2 = true, m3 = true;
+        const int32_t ks[4] = {k4.x, k4.y, k4.z, k4.w};
+        const int32_t vs[4] = {v4.x, v4.y, v4.z, v4.w};
+        uint32_t live = 0xfu;
         if (PRED) {
-            m0 = (w4.x >= lo2) & (w4.x <= hi2);
-            m1 = (w4.y >= lo2) & (w4.y <= hi2);
-            m2 = (w4.z >= lo2) & (w4.z <= hi2);
-            m3 = (w4.w >= lo2) & (w4.w <= hi2);
+            live = (uint32_t)((w4.x >= lo2) & (w4.x <= hi2)) | ((uint32_t)((w4.y >= lo2) & (w4.y <= hi2)) << 1) |
+                   ((uint32_t)((w4.z >= lo2) & (w4.z <= hi2)) << 2) | ((uint32_t)((w4.w >= lo2) & (w4.w <= hi2)) << 3);
         }
-        if (m0) process(k4.x, v4.x);
-        if (m1) process(k4.y, v4.y);
-        if (m2) process(k4.z, v4.z);
-        if (m3) process(k4.w, v4.w);
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if ((live >> j) & 1u) process(ks[j], vs[j]);
     }
     if (c == C - 1) {
         for (long long i = (nv << 2) + tid; i < n; i += P1_THREADS) {
@@ -570,7 +599,7 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
         GPartial g;
         g.key = hk[s];
         g.cnt = hc[s];
-        g.sum = (long long)(((unsigned long long)hsum[2 * s + 1] << 32) | hsum[2 * s]);
+        g.sum = (long long)(((unsigned long long)hsum[gb_hi<SUM64>(s, S)] << 32) | hsum[gb_lo<SUM64>(s)]);
         pt[r] = g;
     }
 }
@@ -621,7 +650,7 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
         } else {
             tk[T] = k;
         }
-        gb_acc<SUM64>(&tc[s], &tsum[2 * s], &tsum[2 * s + 1], cnt, sum);
+        gb_acc<SUM64>(&tc[s], &tsum[gb_lo<SUM64>(s)], &tsum[gb_hi<SUM64>(s, T + 1)], cnt, sum);
     };
 
     while (true) {
@@ -630,8 +659,8 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
         for (int i = tid; i <= T; i += P2_THREADS) {
             tk[i] = SM_EMPTY;
             tc[i] = 0;
-            tsum[2 * i] = 0;
-            tsum[2 * i + 1] = 0;
+            tsum[gb_lo<SUM64>(i)] = 0;
+            tsum[gb_hi<SUM64>(i, T + 1)] = 0;
         }
         __syncthreads();
         const uint32_t p = s_part;
@@ -674,7 +703,7 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
                 const long long pos = (long long)o + __popc(b & lt);
                 if (pos < cap) {
                     gkey[pos] = (int32_t)tk[s];
-                    gsum[pos] = (long long)(((unsigned long long)tsum[2 * s + 1] << 32) | tsum[2 * s]);
+                    gsum[pos] = (long long)(((unsigned long long)tsum[gb_hi<SUM64>(s, T + 1)] << 32) | tsum[gb_lo<SUM64>(s)]);
                     gcnt[pos] = (long long)tc[s];
                     if (rec) rec[pos] = ((unsigned long long)tk[s] << 32) | (unsigned long long)pos;
                 }

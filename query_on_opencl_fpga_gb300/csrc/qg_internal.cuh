@@ -188,14 +188,16 @@ __device__ __forceinline__ uint32_t qg_lb_warp_exclusive(const qg_lookback &lb, 
         if (j >= 0) {
             uint32_t spins = 0;
             unsigned long long w;
+            // spin_limit is the number of polls allowed: 0 gives up at once.
             while (true) {
-                w = qg_ld_relaxed_u64(&lb.status[j]);
-                if ((uint32_t)(w >> 34) == (epoch & 0x3fffffffu) && ((w >> 32) & 3ull) != 0) break;
-                if (++spins >= lb.spin_limit) {
+                if (spins >= lb.spin_limit) {
                     qg_record_error(lb.ctl, QG_ERR_TIMEOUT, lb.site);
                     w = qg_lb_word(epoch, QG_LB_PREFIX, 0);
                     break;
                 }
+                w = qg_ld_relaxed_u64(&lb.status[j]);
+                if ((uint32_t)(w >> 34) == (epoch & 0x3fffffffu) && ((w >> 32) & 3ull) != 0) break;
+                spins++;
                 __nanosleep(32);
             }
             flag = (w >> 32) & 3ull;
@@ -238,14 +240,16 @@ __device__ __forceinline__ uint32_t qg_lb_wide_exclusive(const qg_lookback &lb, 
         if (j >= 0) {
             uint32_t spins = 0;
             unsigned long long w;
+            // spin_limit is the number of polls allowed: 0 gives up at once.
             while (true) {
-                w = qg_ld_relaxed_u64(&lb.status[j]);
-                if ((uint32_t)(w >> 34) == (epoch & 0x3fffffffu) && ((w >> 32) & 3ull) != 0) break;
-                if (++spins >= lb.spin_limit) {
+                if (spins >= lb.spin_limit) {
                     qg_record_error(lb.ctl, QG_ERR_TIMEOUT, lb.site);
                     w = qg_lb_word(epoch, QG_LB_PREFIX, 0);
                     break;
                 }
+                w = qg_ld_relaxed_u64(&lb.status[j]);
+                if ((uint32_t)(w >> 34) == (epoch & 0x3fffffffu) && ((w >> 32) & 3ull) != 0) break;
+                spins++;
                 __nanosleep(20);
             }
             flag = (w >> 32) & 3ull;
@@ -375,6 +379,12 @@ __device__ __forceinline__ void qg_tile_compact_offsets(uint32_t *s_woff, const 
         *s_excl = excl;
         if (tile == last_tile && d_count) *d_count = (long long)excl + total;
     }
+}
+
+// Bulk prefetch of [p, p + bytes) into L2 by the TMA engine (no registers,
+// no shared memory).  p 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void qg_prefetch_l2_bulk(const void *p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
 }
 
 // ---- mbarrier / bulk-copy (TMA engine) helpers (PTX ISA: mbarrier, cp.async.bulk)

@@ -39,6 +39,10 @@ k_scan_excl(const int32_t *in, int32_t *out, long long n, qg_lookback lb) {
 #pragma unroll
             for (int j = 0; j < 4; j++) v[r][j] = (idx + j < n) ? (uint32_t)in[idx + j] : 0u;
         }
+    }
+    // Loads of all rounds are in flight before the first shared store.
+#pragma unroll
+    for (int r = 0; r < SC_ROUNDS; r++) {
         uint32_t s = v[r][0] + v[r][1] + v[r][2] + v[r][3];
         uint32_t inc = s;
 #pragma unroll

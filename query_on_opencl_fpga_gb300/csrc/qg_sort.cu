@@ -31,6 +31,7 @@ constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;  // 4096
+constexpr int RS_LB = 8;  // predecessors read per look-back round
 
 constexpr uint32_t ST_AGG = 1u << 30;
 constexpr uint32_t ST_PRE = 2u << 30;
@@ -85,22 +86,29 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
     uint32_t key[RS_ITEMS];
     unsigned long long val[RS_ITEMS];
     uint32_t rank[RS_ITEMS];
+    // All loads are issued before any ranking: __syncwarp orders memory, so
+    // a load placed after one in program order cannot be hoisted above it,
+    // and interleaving would pay one DRAM latency per item.
 #pragma unroll
     for (int i = 0; i < RS_ITEMS; i++) {
         long long idx = wbase + i * 32 + lane;
-        bool valid = idx < n;
-        if (valid) {
+        if (idx < n) {
             if (KV3) {
-                key[i] = src.k[idx];
-                val[i] = ((unsigned long long)src.b[idx] << 32) | src.a[idx];
+                key[i] = __ldcs(src.k + idx);
+                val[i] = ((unsigned long long)__ldcs(src.b + idx) << 32) | __ldcs(src.a + idx);
             } else {
-                val[i] = src.rec[idx];
+                val[i] = __ldcs(src.rec + idx);
                 key[i] = (uint32_t)(val[i] >> 32);
             }
         } else {
             val[i] = 0;
             key[i] = 0;
         }
+    }
+#pragma unroll
+    for (int i = 0; i < RS_ITEMS; i++) {
+        long long idx = wbase + i * 32 + lane;
+        bool valid = idx < n;
         uint32_t d = ((key[i] - key_off) >> shift) & 255u;
         uint32_t peers = __ballot_sync(QG_FULL_MASK, valid);
 #pragma unroll
@@ -149,24 +157,34 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
             qg_st_relaxed_u32(st, ST_PRE | total);
         } else {
             qg_st_relaxed_u32(st, ST_AGG | total);
+            // Windowed look-back: RS_LB predecessors' words are loaded
+            // together, so a chain of tiles that only published aggregates
+            // costs one L2 round trip per RS_LB tiles instead of per tile.
             long long j = (long long)tile - 1;
-            while (j >= 0) {
-                const uint32_t *p = status + (size_t)j * QG_RADIX + t;
-                uint32_t w;
-                uint32_t spins = 0;
-                while (true) {
-                    w = qg_ld_relaxed_u32(p);
-                    if (w & (ST_AGG | ST_PRE)) break;
-                    if (++spins >= spin_limit) {
-                        qg_record_error(ctl, QG_ERR_TIMEOUT, QG_SITE_SORT_LOOKBACK);
-                        w = ST_PRE;
-                        break;
+            bool done = false;
+            while (!done) {
+                uint32_t w[RS_LB];
+#pragma unroll
+                for (int u = 0; u < RS_LB; u++)
+                    w[u] = (j - u >= 0) ? qg_ld_relaxed_u32(status + (size_t)(j - u) * QG_RADIX + t) : ST_PRE;
+#pragma unroll
+                for (int u = 0; u < RS_LB; u++) {
+                    if (done) break;
+                    uint32_t spins = 0;
+                    while (!(w[u] & (ST_AGG | ST_PRE))) {
+                        if (spins >= spin_limit) {
+                            qg_record_error(ctl, QG_ERR_TIMEOUT, QG_SITE_SORT_LOOKBACK);
+                            w[u] = ST_PRE;
+                            break;
+                        }
+                        spins++;
+                        __nanosleep(32);
+                        w[u] = qg_ld_relaxed_u32(status + (size_t)(j - u) * QG_RADIX + t);
                     }
-                    __nanosleep(32);
+                    excl += w[u] & ST_VAL;
+                    if (w[u] & ST_PRE) done = true;
                 }
-                excl += w & ST_VAL;
-                if (w & ST_PRE) break;
-                j--;
+                j -= RS_LB;
             }
             qg_st_relaxed_u32(st, ST_PRE | ((excl + total) & ST_VAL));
         }
