@@ -197,6 +197,39 @@ QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey, const int
                                      int64_t nS, int32_t slo, int32_t shi, int32_t *out_key,
                                      int32_t *out_rpay, int32_t *out_spay, int64_t cap,
                                      int64_t *out_n);
+/* Join algorithm knobs (process-wide).  variant: 0 auto -- range
+ * partitioning by radix over the key, switching to the learned CDF partition
+ * function when radix leaves more than 2% of the rows in buckets too large
+ * for shared memory and the model does better on the same counts; 1 radix
+ * only; 2 learned only; 3 the global hash table + radix sort of the output.
+ * buckets_log2: 0 = from the input size (about 2560 rows per bucket), else
+ * 1..15.  bucket_s_max / bucket_r_max: rows of a bucket that the shared-memory
+ * bucket kernel takes (0 = its capacity, 4096 / 2048); smaller values send
+ * more buckets to the recursive path (testing).  No reference counterpart:
+ * the reference has a single join kernel pair. */
+QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucket_s_max,
+                                   uint32_t bucket_r_max);
+/* Diagnostics of the context's last qg_join_filter_sort: out[0] path
+ * (1 radix, 2 learned, 3 hash join + sort, 0 nothing to join), out[1]
+ * buckets, out[2] buckets handled outside the bucket kernel, out[3] their
+ * rows, out[4] deepest recursion level, out[5] knots of the learned model,
+ * out[6] heavy keys among them, out[7] 1 when the automatic choice moved
+ * from radix to the learned function. */
+QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8);
+
+/* ---- learned partition function (no reference counterpart) ----
+ * A piecewise-linear model of a key CDF (1024 fp32 segments plus heavy-key
+ * knots) mapping keys to nbuckets buckets, non-decreasing in the unsigned
+ * key; fitted on the GPU from a sample of up to 2^20 of the keys.  d_model is
+ * a device buffer of qg_part_model_bytes() bytes. */
+QG_API int64_t qg_part_model_bytes(void);
+QG_API qg_status qg_part_learn(qg_ctx *ctx, const uint32_t *keys, int64_t n, uint32_t nbuckets,
+                               void *d_model);
+/* Buckets of n keys: under the learned model d_model, or (d_model NULL) the
+ * radix function (key - kmin) >> shift. */
+QG_API qg_status qg_part_eval(qg_ctx *ctx, const void *d_model, uint32_t kmin, int shift,
+                              const uint32_t *keys, int64_t n, uint32_t *buckets);
+
 /* Reference layout (buildHashTable/probeHashTable, hj_filter_sort_op.cl:25-109):
  * r and s are interleaved uint (key, val) pairs; every match writes the pair
  * (S.val, R.val).  Compacted output (the reference leaves holes); order

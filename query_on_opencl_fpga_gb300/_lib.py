@@ -71,6 +71,11 @@ SIGNATURES: dict[str, tuple] = {
                                     POINTER(c_int64)]),
     "qg_hash_join_ref": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64,
                                  POINTER(c_int64)]),
+    "qg_join_set_knobs": (c_int, [c_int, c_int, c_uint32, c_uint32]),
+    "qg_join_stats": (c_int, [c_void_p, c_void_p]),
+    "qg_part_model_bytes": (c_int64, []),
+    "qg_part_learn": (c_int, [c_void_p, c_void_p, c_int64, c_uint32, c_void_p]),
+    "qg_part_eval": (c_int, [c_void_p, c_void_p, c_uint32, c_int, c_void_p, c_int64, c_void_p]),
 }
 
 class QgBuf(ctypes.Structure):

@@ -195,6 +195,39 @@ class Context:
             self.check(st, "qg_join_filter_sort")
             return ok[: m.value], orp[: m.value], osp[: m.value]
 
+    def join_set_knobs(self, variant: int = 0, buckets_log2: int = 0, bucket_s_max: int = 0,
+                       bucket_r_max: int = 0):
+        """Join algorithm: 0 auto, 1 radix partitions, 2 learned partitions, 3 hash + sort."""
+        self.check(self.lib.qg_join_set_knobs(variant, buckets_log2, bucket_s_max, bucket_r_max),
+                   "qg_join_set_knobs")
+
+    def join_stats(self) -> dict:
+        """Path and partition diagnostics of the last join_filter_sort call."""
+        out = (ctypes.c_uint32 * 8)()
+        self.check(self.lib.qg_join_stats(self.handle, out), "qg_join_stats")
+        names = {0: "none", 1: "radix", 2: "learned", 3: "hash_sort"}
+        return {"path": names.get(out[0], str(out[0])), "buckets": out[1], "outside_buckets": out[2],
+                "outside_rows": out[3], "depth": out[4], "knots": out[5], "heavy_keys": out[6],
+                "auto_switched": out[7]}
+
+    def part_learn(self, keys: torch.Tensor, nbuckets: int) -> torch.Tensor:
+        """Fit the learned partition function on int32/uint32 keys; returns the device model."""
+        _check_dev(keys)
+        model = torch.empty(int(self.lib.qg_part_model_bytes()), dtype=torch.uint8, device=keys.device)
+        self.check(self.lib.qg_part_learn(self.handle, _ptr(keys), keys.numel(), nbuckets, _ptr(model)),
+                   "qg_part_learn")
+        return model
+
+    def part_eval(self, keys: torch.Tensor, model: torch.Tensor | None = None, kmin: int = 0,
+                  shift: int = 0) -> torch.Tensor:
+        """Bucket of each key under the learned model, or radix (key - kmin) >> shift."""
+        _check_dev(keys)
+        out = torch.empty(keys.numel(), dtype=torch.int32, device=keys.device)
+        mp = _ptr(model) if model is not None else None
+        self.check(self.lib.qg_part_eval(self.handle, mp, kmin & 0xFFFFFFFF, shift, _ptr(keys), keys.numel(),
+                                         _ptr(out)), "qg_part_eval")
+        return out
+
     def hash_join_ref(self, r_pairs: torch.Tensor, s_pairs: torch.Tensor, cap: int | None = None):
         """Reference-layout join: (key, val) pairs in, (S.val, R.val) pairs out."""
         _check_dev(r_pairs, s_pairs)

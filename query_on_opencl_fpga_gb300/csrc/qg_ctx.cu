@@ -55,6 +55,7 @@ QG_API qg_status qg_ctx_destroy(qg_ctx *ctx) {
     if (ctx->ev[0])
         for (int i = 0; i < 2 * QG_MAX_TIMED; i++) cudaEventDestroy(ctx->ev[i]);
     if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->lbstat) cudaFree(ctx->lbstat);
     if (ctx->table) cudaFree(ctx->table);
     if (ctx->aux) cudaFree(ctx->aux);
     if (ctx->ctl) cudaFree(ctx->ctl);
@@ -208,6 +209,29 @@ qg_status qg_scratch(qg_ctx *ctx, size_t bytes, char **out) {
         ctx->scratch_bytes = want;
     }
     *out = ctx->scratch;
+    return QG_OK;
+}
+
+qg_status qg_lb_make(qg_ctx *ctx, int64_t tiles, int site, qg_lookback *out) {
+    const size_t words = (size_t)(tiles > 0 ? tiles : 1);
+    if (words > ctx->lbstat_words) {
+        const size_t want = words + words / 4 + 1024;
+        QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        if (ctx->lbstat) cudaFree(ctx->lbstat);
+        ctx->lbstat = nullptr;
+        ctx->lbstat_words = 0;
+        cudaError_t e = cudaMalloc((void **)&ctx->lbstat, want * 8);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            snprintf(ctx->msg, sizeof(ctx->msg), "look-back status cudaMalloc(%zu): %s", want * 8,
+                     cudaGetErrorString(e));
+            return QG_ERR_OOM;
+        }
+        QG_TRY_CUDA(ctx, cudaMemset(ctx->lbstat, 0, want * 8), "cudaMemset look-back status");
+        QG_TRY_CUDA(ctx, cudaDeviceSynchronize(), "cudaDeviceSynchronize");
+        ctx->lbstat_words = want;
+    }
+    *out = qg_lookback{ctx->lbstat, ctx->ctl, ctx->spin_limit, site};
     return QG_OK;
 }
 

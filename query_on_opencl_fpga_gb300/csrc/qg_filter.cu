@@ -293,9 +293,8 @@ qg_status qg_filter_rec_launch(qg_ctx *ctx, const void *in, int64_t n, int32_t l
     if (((uintptr_t)in & 15) != 0 || ((uintptr_t)out & 7) != 0) return QG_ERR_INVALID;
     int64_t tiles = qg_ceil_div(n, TILE);
     if (tiles > 0x7fffffff) return QG_ERR_UNSUPPORTED;
-    char *scr;
-    QG_TRY(qg_scratch(ctx, qg_lb_bytes(tiles), &scr));
-    qg_lookback lb{(unsigned long long *)scr, ctx->ctl, ctx->spin_limit, QG_SITE_FILTER};
+    qg_lookback lb;
+    QG_TRY(qg_lb_make(ctx, tiles, QG_SITE_FILTER, &lb));
     qg_pre_launch(ctx);
     k_filter_rec<REC_ROUNDS><<<(unsigned)tiles, FT_THREADS, 0, ctx->stream>>>(
         (const uint4 *)in, n, lo, hi, (uint2 *)out, cap, d_count, lb);
@@ -316,9 +315,8 @@ qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *
         return QG_ERR_INVALID;
     int64_t tiles = qg_ceil_div(n, TILE);
     if (tiles > 0x7fffffff || n > 0x7fffffffLL) return QG_ERR_UNSUPPORTED;
-    char *scr;
-    QG_TRY(qg_scratch(ctx, qg_lb_bytes(tiles), &scr));
-    qg_lookback lb{(unsigned long long *)scr, ctx->ctl, ctx->spin_limit, QG_SITE_FILTER};
+    qg_lookback lb;
+    QG_TRY(qg_lb_make(ctx, tiles, QG_SITE_FILTER, &lb));
     if (g_filter_variant == 1) {
         static bool attr = false;
         if (!attr) {

@@ -743,10 +743,9 @@ extern "C" QG_API qg_status qg_groupby_rec(qg_ctx *ctx, const void *in, int64_t 
     if (s == QG_OK) {
         constexpr int TILE = GBD_THREADS * GBD_ROUNDS * 2;
         int64_t tiles = qg_ceil_div(n, TILE);
-        char *scr;
-        s = qg_scratch(ctx, qg_lb_bytes(tiles), &scr);
+        qg_lookback lb;
+        s = qg_lb_make(ctx, tiles, QG_SITE_GROUPBY, &lb);
         if (s == QG_OK) {
-            qg_lookback lb{(unsigned long long *)scr, ctx->ctl, ctx->spin_limit, QG_SITE_GROUPBY};
             long long *d_count = (long long *)&ctx->ctl->counter[0];
             qg_pre_launch(ctx);
             k_group_bounds<<<(unsigned)tiles, GBD_THREADS, 0, ctx->stream>>>(

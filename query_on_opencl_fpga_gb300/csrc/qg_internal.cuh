@@ -30,12 +30,15 @@ struct qg_ctx {
     size_t table_bytes;
     char *aux;              // grow-only arena for operator temporaries that must
     size_t aux_bytes;       //   survive nested calls (e.g. a sort inside group-by)
+    unsigned long long *lbstat;  // look-back status words, used by nothing else
+    size_t lbstat_words;
     qg_control *ctl;        // device
     long long *pinned;      // host pinned readback slots (8)
     uint32_t spin_limit;
     uint64_t launches;
     bool table_dirty;       // group-by table must be cleared before next use
     uint32_t gb_stats[4];   // last qg_groupby_cols: path, flags, fullest bucket, bucket cap
+    uint32_t pj_stats[8];   // last qg_join_filter_sort (see qg_join_stats)
     char msg[256];
     // Per-kernel CUDA-event timing (qg_ctx_enable_timing): a pair of events
     // brackets every launch on the context's stream.
@@ -51,7 +54,8 @@ void qg_pre_launch(qg_ctx *ctx);
 // Site tags for the error word.
 enum {
     QG_SITE_FILTER = 1, QG_SITE_SCAN = 2, QG_SITE_SORT = 3, QG_SITE_GROUPBY = 4,
-    QG_SITE_AGG = 5, QG_SITE_JOIN_BUILD = 6, QG_SITE_JOIN_PROBE = 7, QG_SITE_SORT_LOOKBACK = 8
+    QG_SITE_AGG = 5, QG_SITE_JOIN_BUILD = 6, QG_SITE_JOIN_PROBE = 7, QG_SITE_SORT_LOOKBACK = 8,
+    QG_SITE_PJ_HIST = 9, QG_SITE_PJ_FILTER = 10, QG_SITE_PJ_BUCKET = 11
 };
 
 qg_status qg_cuda_fail(qg_ctx *ctx, cudaError_t e, const char *what);
@@ -61,6 +65,12 @@ qg_status qg_scratch(qg_ctx *ctx, size_t bytes, char **out);
 qg_status qg_aux(qg_ctx *ctx, size_t bytes, char **out);
 // Ensure the hash-table arena holds at least `bytes` of zeroed memory.
 qg_status qg_table(qg_ctx *ctx, size_t bytes, char **out);
+// Look-back descriptor for a single-pass kernel of `tiles` tiles.  Its status
+// words live in an arena of their own: a word there is either zero or was
+// written by an earlier look-back launch (an older epoch), never by other
+// data that could mimic a current-epoch word.
+struct qg_lookback;
+qg_status qg_lb_make(qg_ctx *ctx, int64_t tiles, int site, qg_lookback *out);
 // Copy a device int64 to host (synchronises the stream).
 qg_status qg_read_i64(qg_ctx *ctx, const long long *d, long long *h);
 qg_status qg_check_launch(qg_ctx *ctx, const char *what);

@@ -418,12 +418,12 @@ static qg_status join_build(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpa
     return QG_OK;
 }
 
-extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey,
-                                                const int32_t *rpay, int64_t nR,
-                                                const int32_t *skey, const int32_t *spay,
-                                                int64_t nS, int32_t slo, int32_t shi,
-                                                int32_t *out_key, int32_t *out_rpay,
-                                                int32_t *out_spay, int64_t cap, int64_t *out_n) {
+// Hash join + filter + radix sort of the output (the variant of
+// qg_join_filter_sort selected by qg_join_set_knobs(3, ...)).
+qg_status qg_join_hash_sort(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay, int64_t nR,
+                            const int32_t *skey, const int32_t *spay, int64_t nS, int32_t slo,
+                            int32_t shi, int32_t *out_key, int32_t *out_rpay, int32_t *out_spay,
+                            int64_t cap, int64_t *out_n) {
     if (!ctx || nR < 0 || nS < 0 || cap < 0 || !out_n) return QG_ERR_INVALID;
     if ((nR > 0 && (!rkey || !rpay)) || (nS > 0 && (!skey || !spay)) ||
         (cap > 0 && (!out_key || !out_rpay || !out_spay)))

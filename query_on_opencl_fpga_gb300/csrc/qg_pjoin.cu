@@ -1,0 +1,1162 @@
+// qg_pjoin.cu -- range-partitioned join + filter + sort (the default path of
+// qg_join_filter_sort).
+//
+// Reference operators this replaces: buildHashTable / probeHashTable and the
+// filter + bitonic sort of the matches (kernel/hj_filter_sort/1/
+// hj_filter_sort_op.cl:25-109, :117-564).  Output contract: every pair
+// (R row, S row) with equal uint keys whose S.payload passes the filter,
+// emitted as (key, R.payload, S.payload), ordered by the unsigned key; the
+// order among equal keys is unspecified (the reference's bitonic sort is not
+// stable either).
+//
+// Pipeline (one GPU, all data in HBM):
+//   1. R columns -> R records (key << 32 | payload) and R's key range.
+//   2. S: filter on S.payload and on R's key range, compacted in one pass
+//      (decoupled look-back) into S' records (key << 32 | S.payload).
+//   3. A partition function maps keys to B buckets (key ranges): radix over
+//      (k - kmin), or a learned piecewise-linear CDF model fitted on a sample
+//      (qg_part.cuh).  Bucket histograms of R and S', then one or two stable
+//      onesweep radix passes over the bucket id (qg_sort.cu) put both sides
+//      in bucket order.
+//   4. One CTA per bucket (tickets in bucket order): the bucket's R rows go
+//      into a shared-memory chained table, its S' rows are counting-sorted by
+//      key in shared memory (bitonic sort when the bucket's key span is
+//      wide), every S' row is probed, the bucket's output count is published
+//      and its output offset found by decoupled look-back, and the matches are
+//      written in key order.  Buckets are key ranges, so the output is sorted
+//      with no global sort pass.
+//   5. Buckets too large for shared memory: a bucket with one key is a cross
+//      product (k_pj_cross); any other is joined recursively with its own
+//      partition into a temporary and copied into place (k_pj_place).  Both
+//      read the bucket's output offset that step 4 published.
+#include <algorithm>
+#include <string.h>
+#include <vector>
+#include "qg_internal.cuh"
+#include "qg_part.cuh"
+#include "qg_sort.cuh"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// 1. R columns -> records, key range
+// ---------------------------------------------------------------------------
+struct PjRange {
+    uint32_t kmin, kmax;
+    unsigned long long count;  // S' rows (step 2)
+};
+
+__global__ void k_pj_range_init(PjRange *r) {
+    r->kmin = 0xffffffffu;
+    r->kmax = 0;
+    r->count = 0;
+}
+
+__global__ void __launch_bounds__(256)
+k_pj_rrec(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, long long nR,
+          unsigned long long *__restrict__ rec, PjRange *range) {
+    uint32_t lmin = 0xffffffffu, lmax = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += stride) {
+        const uint32_t k = (uint32_t)__ldg(rkey + i);
+        const uint32_t p = (uint32_t)__ldg(rpay + i);
+        rec[i] = ((unsigned long long)k << 32) | p;
+        lmin = min(lmin, k);
+        lmax = max(lmax, k);
+    }
+    lmin = __reduce_min_sync(QG_FULL_MASK, lmin);
+    lmax = __reduce_max_sync(QG_FULL_MASK, lmax);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&range->kmin, lmin);
+        atomicMax(&range->kmax, lmax);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2. S filter + range test, compacted into S' records (stable)
+// ---------------------------------------------------------------------------
+constexpr int SF_THREADS = 256;
+constexpr int SF_WARPS = SF_THREADS / 32;
+constexpr int SF_ROUNDS = 4;  // int4 of keys + int4 of payloads per round: 4096 rows per tile
+constexpr int SF_LB_WARPS = 4;
+
+__global__ void __launch_bounds__(SF_THREADS)
+k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay, long long n,
+             int32_t slo, int32_t shi, uint32_t kmin, uint32_t kmax,
+             unsigned long long *__restrict__ out, long long *__restrict__ d_count, qg_lookback lb) {
+    constexpr int TILE = SF_THREADS * SF_ROUNDS * 4;
+    __shared__ uint32_t s_tile, s_epoch, s_excl;
+    __shared__ uint32_t s_woff[SF_ROUNDS * SF_WARPS];
+    __shared__ uint32_t s_tmp[2 * SF_LB_WARPS + 1];
+    qg_lb_begin(lb, &s_tile, &s_epoch);
+    const uint32_t tile = s_tile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const long long base = (long long)tile * TILE;
+    const uint32_t lt = qg_lanemask_lt();
+    int4 kv[SF_ROUNDS], pv[SF_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < SF_ROUNDS; r++) {
+        const long long idx = base + (long long)(r * SF_THREADS + tid) * 4;
+        if (idx + 3 < n) {
+            kv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(skey + idx));
+            pv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(spay + idx));
+        } else {
+            int t[4] = {0, 0, 0, 0}, p[4] = {0, 0, 0, 0};
+            for (int j = 0; j < 4; j++)
+                if (idx + j < n) { t[j] = skey[idx + j]; p[j] = spay[idx + j]; }
+            kv[r] = make_int4(t[0], t[1], t[2], t[3]);
+            pv[r] = make_int4(p[0], p[1], p[2], p[3]);
+        }
+    }
+    uint32_t fl = 0, lpre[SF_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < SF_ROUNDS; r++) {
+        const long long idx = base + (long long)(r * SF_THREADS + tid) * 4;
+        const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
+        const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
+        uint32_t f = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t u = (uint32_t)kk[j];
+            f |= (uint32_t)((idx + j < n) & (pp[j] >= slo) & (pp[j] <= shi) & (u >= kmin) & (u <= kmax)) << j;
+        }
+        uint32_t c = 0, tot = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const uint32_t b = __ballot_sync(QG_FULL_MASK, (f >> j) & 1u);
+            c += __popc(b & lt);
+            tot += __popc(b);
+        }
+        lpre[r] = c;
+        if (lane == 0) s_woff[r * SF_WARPS + warp] = tot;
+        fl |= f << (4 * r);
+    }
+    qg_tile_offsets_wide<SF_ROUNDS * SF_WARPS, SF_LB_WARPS>(s_woff, lb, tile, s_epoch, &s_excl, s_tmp,
+                                                           d_count, gridDim.x - 1);
+    const long long excl = s_excl;
+#pragma unroll
+    for (int r = 0; r < SF_ROUNDS; r++) {
+        long long pos = excl + s_woff[r * SF_WARPS + warp] + lpre[r];
+        const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
+        const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            if ((fl >> (4 * r + j)) & 1u) {
+                if (pos < n) out[pos] = ((unsigned long long)(uint32_t)kk[j] << 32) | (uint32_t)pp[j];
+                else qg_record_error(lb.ctl, QG_ERR_INVALID, QG_SITE_PJ_FILTER);
+                pos++;
+            }
+    }
+    qg_lb_end(lb);
+}
+
+// ---------------------------------------------------------------------------
+// 3. bucket histogram (shared-memory privatised), CDF sample and fit
+// ---------------------------------------------------------------------------
+constexpr int PJ_MAX_BUCKETS = 1 << 15;
+
+__global__ void __launch_bounds__(1024)
+k_pj_hist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn pf, uint32_t nb,
+          uint32_t *__restrict__ counts, qg_control *ctl) {
+    extern __shared__ uint32_t h[];
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint32_t k = (uint32_t)(__ldg(rec + i) >> 32);
+        const uint32_t b = qg_part_bucket(pf, k);
+        if (b >= nb) {  // a key outside the partition function's domain
+            qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_HIST);
+            continue;
+        }
+        atomicAdd(&h[b], 1u);
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
+        if (h[i]) atomicAdd(&counts[i], h[i]);
+}
+
+// Sample m keys spread evenly over both inputs (proportionally to their
+// sizes), as u64 items with the key in the high word for the radix sort.
+__global__ void k_cdf_sample(const unsigned long long *__restrict__ r, long long nR,
+                             const unsigned long long *__restrict__ s, long long nS, long long mR,
+                             long long m, unsigned long long *__restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        unsigned long long v;
+        if (i < mR) v = __ldg(r + (i * nR) / mR);
+        else v = __ldg(s + ((i - mR) * nS) / (m - mR));
+        out[i] = v & 0xffffffff00000000ull;
+    }
+}
+
+__device__ __forceinline__ uint32_t smp_key(const unsigned long long *s, long long i) {
+    return (uint32_t)(s[i] >> 32);
+}
+// First index with key >= u / > u in the sorted sample.
+__device__ long long smp_lower(const unsigned long long *s, long long m, uint32_t u) {
+    long long lo = 0, hi = m;
+    while (lo < hi) {
+        long long mid = (lo + hi) >> 1;
+        if (smp_key(s, mid) < u) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+__device__ long long smp_upper(const unsigned long long *s, long long m, uint32_t u) {
+    long long lo = 0, hi = m;
+    while (lo < hi) {
+        long long mid = (lo + hi) >> 1;
+        if (smp_key(s, mid) <= u) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Training of the learned partition function from the sorted sample (one CTA).
+//   knots: the keys at the 1025 sample quantiles i/1024, plus every key that
+//          holds at least `hthr` sample entries (heavy), deduplicated;
+//   bucket of a knot: floor(B * rank / m), rank = first sample index of the
+//          knot's key (heavy keys: the middle of their run), so that buckets
+//          are filled in proportion to the sample mass;
+//   between knots: linear in the key with an fp32 slope, clamped so that the
+//          function stays non-decreasing and a heavy key's bucket holds no
+//          other key.
+constexpr int FIT_THREADS = 1024;
+constexpr int FIT_SORT = 2048;  // >= QG_CDF_MAX_KNOTS, power of two
+
+__global__ void __launch_bounds__(FIT_THREADS)
+k_cdf_fit(const unsigned long long *__restrict__ smp, long long m, uint32_t nb, long long hthr,
+          qg_cdf_model *__restrict__ model) {
+    __shared__ uint32_t cand[FIT_SORT];
+    __shared__ uint32_t ncand;
+    __shared__ uint32_t s_heavy_n;
+    const int tid = threadIdx.x;
+    if (tid == 0) { ncand = 0; s_heavy_n = 0; }
+    for (int i = tid; i < FIT_SORT; i += FIT_THREADS) cand[i] = 0xffffffffu;
+    __syncthreads();
+    // quantile knots
+    for (int i = tid; i <= QG_CDF_SEGMENTS; i += FIT_THREADS) {
+        const long long si = (long long)i * (m - 1) / QG_CDF_SEGMENTS;
+        cand[i] = smp_key(smp, si);
+    }
+    if (tid == 0) ncand = QG_CDF_SEGMENTS + 1;
+    __syncthreads();
+    // heavy keys: runs of at least hthr equal keys in the sorted sample
+    for (long long i = tid; i < m; i += FIT_THREADS) {
+        const uint32_t u = smp_key(smp, i);
+        if (i > 0 && smp_key(smp, i - 1) == u) continue;
+        if (i + hthr - 1 >= m || smp_key(smp, i + hthr - 1) != u) continue;
+        const uint32_t h = atomicAdd(&s_heavy_n, 1u);
+        if (h < QG_CDF_MAX_HEAVY) cand[QG_CDF_SEGMENTS + 1 + h] = u;
+    }
+    __syncthreads();
+    // bitonic sort of the candidates (unused entries are 0xffffffff and sort last)
+    for (int k = 2; k <= FIT_SORT; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < FIT_SORT; i += FIT_THREADS) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const uint32_t a = cand[i], b = cand[l];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) { cand[i] = b; cand[l] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const uint32_t nreal = QG_CDF_SEGMENTS + 1 + min(s_heavy_n, (uint32_t)QG_CDF_MAX_HEAVY);
+    // deduplicate: keep the first of each run (a real 0xffffffff key among the
+    // first nreal entries is kept once)
+    __shared__ uint32_t keep_idx[FIT_SORT];
+    __shared__ uint32_t wsum[FIT_THREADS / 32];
+    {
+        // two entries per thread
+        uint32_t f[2], c = 0;
+        for (int q = 0; q < 2; q++) {
+            const int i = tid * 2 + q;
+            f[q] = (i < (int)nreal) && (i == 0 || cand[i] != cand[i - 1]);
+            c += f[q];
+        }
+        uint32_t inc = c;
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t x = __shfl_up_sync(QG_FULL_MASK, inc, d);
+            if (lane >= d) inc += x;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        uint32_t off = 0, tot = 0;
+        for (int w = 0; w < FIT_THREADS / 32; w++) {
+            if (w < warp) off += wsum[w];
+            tot += wsum[w];
+        }
+        uint32_t pos = off + inc - c;
+        const uint32_t k0 = cand[tid * 2], k1 = cand[tid * 2 + 1];
+        __syncthreads();
+        if (f[0]) keep_idx[pos++] = k0;
+        if (f[1]) keep_idx[pos++] = k1;
+        if (tid == 0) ncand = tot;
+    }
+    __syncthreads();
+    const uint32_t K = ncand;
+    // per-knot bucket and heavy flag
+    __shared__ uint32_t bk[QG_CDF_MAX_KNOTS];
+    __shared__ uint8_t hv[QG_CDF_MAX_KNOTS];
+    for (uint32_t i = tid; i < K; i += FIT_THREADS) {
+        const uint32_t u = keep_idx[i];
+        const long long lo = smp_lower(smp, m, u), hi = smp_upper(smp, m, u);
+        const bool heavy = (hi - lo) >= hthr;
+        const long long rank2 = heavy ? (lo + hi) : 2 * lo;  // twice the rank
+        long long b = (long long)((unsigned long long)rank2 * nb / (2ull * (unsigned long long)m));
+        if (b > (long long)nb - 1) b = nb - 1;
+        bk[i] = (uint32_t)b;
+        hv[i] = heavy;
+        model->x[i] = u;
+        model->bk[i] = (uint32_t)b;
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < K; i += FIT_THREADS) {
+        if (i + 1 < K) {
+            const uint32_t x0 = keep_idx[i], x1 = keep_idx[i + 1];
+            uint32_t lowB = bk[i] + (hv[i] ? 1u : 0u);
+            uint32_t highB = hv[i + 1] ? (bk[i + 1] > 0 ? bk[i + 1] - 1u : 0u) : bk[i + 1];
+            if (lowB > bk[i + 1]) lowB = bk[i + 1];
+            if (highB < lowB) highB = lowB;
+            const uint32_t inner = x1 - x0 - 1u;  // keys strictly between the knots
+            model->b0[i] = lowB;
+            model->b1[i] = highB;
+            model->slope[i] = inner ? (float)(highB - lowB + 1u) / (float)inner : 0.0f;
+        } else {
+            model->b0[i] = bk[i];
+            model->b1[i] = bk[i];
+            model->slope[i] = 0.0f;
+        }
+    }
+    // top-level index
+    const uint32_t x0 = keep_idx[0], xl = keep_idx[K - 1];
+    const uint32_t range = xl - x0;
+    uint32_t ishift = 0;
+    while ((range >> ishift) >= (uint32_t)QG_CDF_INDEX) ishift++;
+    for (int t = tid; t <= QG_CDF_INDEX; t += FIT_THREADS) {
+        const unsigned long long kt = (unsigned long long)x0 + ((unsigned long long)t << ishift);
+        const uint32_t key = kt > xl ? xl : (uint32_t)kt;
+        // largest knot index with x <= key
+        uint32_t lo = 0, hi = K;  // first index with x > key
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (keep_idx[mid] <= key) lo = mid + 1;
+            else hi = mid;
+        }
+        model->idx[t] = lo ? lo - 1 : 0;
+    }
+    if (tid == 0) {
+        model->nknots = K;
+        model->nbuckets = nb;
+        model->ishift = ishift;
+        model->nheavy = min(s_heavy_n, (uint32_t)QG_CDF_MAX_HEAVY);
+    }
+}
+
+// Buckets of an array of keys under a partition function (for tests/tools).
+__global__ void k_part_eval(const uint32_t *__restrict__ keys, long long n, qg_part_fn pf,
+                            uint32_t *__restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = qg_part_bucket(pf, keys[i]);
+}
+
+// ---------------------------------------------------------------------------
+// 4. per-bucket join (one CTA per bucket, tickets in bucket order)
+// ---------------------------------------------------------------------------
+constexpr int PB_THREADS = 512;
+constexpr int PB_WARPS = PB_THREADS / 32;
+constexpr int PB_SMAX = 4096;  // S' rows of a bucket held in shared memory
+constexpr int PB_RMAX = 2048;  // R rows of a bucket
+constexpr int PB_HEADS_LOG2 = 12;
+constexpr int PB_HEADS = 1 << PB_HEADS_LOG2;
+constexpr int PB_CSPAN = 8192;  // widest key span that is counting-sorted
+constexpr int PB_IPT = PB_SMAX / PB_THREADS;
+
+struct PbSmem {
+    unsigned long long s[PB_SMAX];  // the bucket's S' rows (key << 32 | S.payload), sorted by key
+    uint32_t cnt[PB_CSPAN];         // counting-sort counters, then start offsets
+    uint32_t rk[PB_RMAX];
+    uint32_t rp[PB_RMAX];
+    uint32_t head[PB_HEADS];        // 1 + first R row of each chain, 0 = empty
+    uint32_t next[PB_RMAX];         // 1 + next R row of the chain, 0 = end
+    uint32_t wsum[PB_WARPS];
+    uint32_t red[2 * PB_WARPS];
+    uint32_t tile, epoch, excl, pad;
+};
+
+struct PbArgs {
+    const unsigned long long *R;  // bucket-ordered R records
+    const unsigned long long *S;  // bucket-ordered S' records
+    const uint32_t *rbeg;         // [nb + 1]
+    const uint32_t *sbeg;         // [nb + 1]
+    const uint32_t *big;          // [nb] 1: handled outside, its count in bigcnt
+    const unsigned long long *bigcnt;
+    unsigned long long *off;      // [nb] output offset of each outside bucket (written)
+    unsigned long long *total;    // output rows of all buckets (written by the last bucket)
+    uint32_t *out_k, *out_a, *out_b;
+    long long cap;
+};
+
+__device__ __forceinline__ uint32_t pb_hash(uint32_t k) {
+    return (k * 0x9E3779B1u) >> (32 - PB_HEADS_LOG2);
+}
+
+// Exclusive prefix of v over the CTA in thread order; *total = sum.
+__device__ __forceinline__ uint32_t pb_excl(uint32_t v, uint32_t *wsum, uint32_t *total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t inc = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t x = __shfl_up_sync(QG_FULL_MASK, inc, d);
+        if (lane >= d) inc += x;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    uint32_t off = 0, tot = 0;
+#pragma unroll
+    for (int w = 0; w < PB_WARPS; w++) {
+        const uint32_t x = wsum[w];
+        if (w < warp) off += x;
+        tot += x;
+    }
+    __syncthreads();
+    *total = tot;
+    return off + inc - v;
+}
+
+__global__ void __launch_bounds__(PB_THREADS, 2)
+k_pj_join(PbArgs a, qg_lookback lb) {
+    extern __shared__ __align__(16) unsigned char pb_raw[];
+    PbSmem &S = *reinterpret_cast<PbSmem *>(pb_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    qg_lb_begin(lb, &S.tile, &S.epoch);
+    const uint32_t b = S.tile;
+    const uint32_t rb = a.rbeg[b], rn = a.rbeg[b + 1] - rb;
+    const uint32_t sb = a.sbeg[b], sn = a.sbeg[b + 1] - sb;
+    const bool outside = a.big[b] != 0;
+    bool work = !outside && rn > 0 && sn > 0;
+    if (work && (rn > (uint32_t)PB_RMAX || sn > (uint32_t)PB_SMAX)) {  // host sends these outside
+        if (tid == 0) qg_record_error(lb.ctl, QG_ERR_INVALID, QG_SITE_PJ_BUCKET);
+        work = false;
+    }
+    uint32_t my_cnt = 0;      // matches of this thread's rows
+    uint32_t q = 0, r0 = 0;   // this thread's block of sorted rows
+    if (work) {
+        // R rows -> chained table
+        for (uint32_t i = tid; i < PB_HEADS; i += PB_THREADS) S.head[i] = 0;
+        for (uint32_t i = tid; i < rn; i += PB_THREADS) {
+            const unsigned long long v = __ldg(a.R + rb + i);
+            S.rk[i] = (uint32_t)(v >> 32);
+            S.rp[i] = (uint32_t)v;
+        }
+        // S' rows -> registers, key range of the bucket
+        unsigned long long it[PB_IPT];
+        uint32_t kmn = 0xffffffffu, kmx = 0;
+#pragma unroll
+        for (int j = 0; j < PB_IPT; j++) {
+            const uint32_t i = j * PB_THREADS + tid;
+            it[j] = i < sn ? __ldg(a.S + sb + i) : 0ull;
+            if (i < sn) {
+                const uint32_t k = (uint32_t)(it[j] >> 32);
+                kmn = min(kmn, k);
+                kmx = max(kmx, k);
+            }
+        }
+        kmn = __reduce_min_sync(QG_FULL_MASK, kmn);
+        kmx = __reduce_max_sync(QG_FULL_MASK, kmx);
+        if (lane == 0) { S.red[warp] = kmn; S.red[PB_WARPS + warp] = kmx; }
+        __syncthreads();
+        for (uint32_t i = tid; i < rn; i += PB_THREADS)
+            S.next[i] = atomicExch(&S.head[pb_hash(S.rk[i])], i + 1);
+        kmn = 0xffffffffu;
+        kmx = 0;
+#pragma unroll
+        for (int w = 0; w < PB_WARPS; w++) {
+            kmn = min(kmn, S.red[w]);
+            kmx = max(kmx, S.red[PB_WARPS + w]);
+        }
+        const uint32_t span1 = kmx - kmn;  // span - 1
+        if (span1 < (uint32_t)PB_CSPAN) {
+            // counting sort by (key - kmn); the order among equal keys is free
+            for (uint32_t i = tid; i <= span1; i += PB_THREADS) S.cnt[i] = 0;
+            __syncthreads();
+            uint32_t rk[PB_IPT];
+#pragma unroll
+            for (int j = 0; j < PB_IPT; j++) {
+                const uint32_t i = j * PB_THREADS + tid;
+                if (i < sn) rk[j] = atomicAdd(&S.cnt[(uint32_t)(it[j] >> 32) - kmn], 1u);
+            }
+            __syncthreads();
+            constexpr int PER = PB_CSPAN / PB_THREADS;
+            const uint32_t c0 = tid * PER;
+            uint32_t loc[PER], sum = 0;
+#pragma unroll
+            for (int e = 0; e < PER; e++) {
+                loc[e] = (c0 + e <= span1) ? S.cnt[c0 + e] : 0u;
+                sum += loc[e];
+            }
+            uint32_t tot;
+            uint32_t run = pb_excl(sum, S.wsum, &tot);
+#pragma unroll
+            for (int e = 0; e < PER; e++) {
+                if (c0 + e <= span1) S.cnt[c0 + e] = run;
+                run += loc[e];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < PB_IPT; j++) {
+                const uint32_t i = j * PB_THREADS + tid;
+                if (i < sn) S.s[S.cnt[(uint32_t)(it[j] >> 32) - kmn] + rk[j]] = it[j];
+            }
+        } else {
+            // wide key span: bitonic sort of the rows, padded with all-ones
+            uint32_t P = 1;
+            while (P < sn) P <<= 1;
+#pragma unroll
+            for (int j = 0; j < PB_IPT; j++) {
+                const uint32_t i = j * PB_THREADS + tid;
+                if (i < P) S.s[i] = i < sn ? it[j] : ~0ull;
+            }
+            __syncthreads();
+            for (uint32_t k = 2; k <= P; k <<= 1) {
+                for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+                    for (uint32_t i = tid; i < P; i += PB_THREADS) {
+                        const uint32_t l = i ^ j;
+                        if (l > i) {
+                            const unsigned long long x = S.s[i], y = S.s[l];
+                            if ((x > y) == ((i & k) == 0)) { S.s[i] = y; S.s[l] = x; }
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+        }
+        __syncthreads();
+        // probe: thread t owns sorted rows [r0, r0 + q)
+        const uint32_t qq = (sn + PB_THREADS - 1) / PB_THREADS;
+        r0 = min(sn, tid * qq);
+        q = min(sn, r0 + qq) - r0;
+        for (uint32_t r = r0; r < r0 + q; r++) {
+            const uint32_t k = (uint32_t)(S.s[r] >> 32);
+            for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) my_cnt += (S.rk[e - 1] == k);
+        }
+    }
+    uint32_t total;
+    const uint32_t my_off = pb_excl(my_cnt, S.wsum, &total);
+    const uint32_t bucket_cnt = outside ? (uint32_t)a.bigcnt[b] : total;
+    if (warp == 0) {
+        const uint32_t excl = qg_lb_warp_exclusive(lb, b, S.epoch, bucket_cnt);
+        if (lane == 0) {
+            S.excl = excl;
+            if (b == gridDim.x - 1) *a.total = (unsigned long long)excl + bucket_cnt;
+            if (outside) a.off[b] = excl;
+        }
+    }
+    __syncthreads();
+    if (work && my_cnt) {
+        long long o = (long long)S.excl + my_off;
+        for (uint32_t r = r0; r < r0 + q; r++) {
+            const unsigned long long v = S.s[r];
+            const uint32_t k = (uint32_t)(v >> 32);
+            for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) {
+                if (S.rk[e - 1] != k) continue;
+                if (o < a.cap) {
+                    a.out_k[o] = k;
+                    a.out_a[o] = S.rp[e - 1];
+                    a.out_b[o] = (uint32_t)v;
+                }
+                o++;
+            }
+        }
+    }
+    qg_lb_end(lb);
+}
+
+// ---------------------------------------------------------------------------
+// 5. buckets handled outside the bucket kernel
+// ---------------------------------------------------------------------------
+struct PjCross {  // a bucket with one key: every R row times every S' row
+    uint32_t b, rb, rn, sb, sn;
+};
+struct PjPlace {  // a bucket joined recursively into a temporary
+    uint32_t b;
+    const uint32_t *k, *a, *c;
+    unsigned long long m;
+};
+
+__global__ void k_pj_cross(const PjCross *__restrict__ list, const unsigned long long *__restrict__ R,
+                           const unsigned long long *__restrict__ S, const unsigned long long *__restrict__ off,
+                           uint32_t *__restrict__ ok, uint32_t *__restrict__ oa, uint32_t *__restrict__ ob,
+                           long long cap) {
+    const PjCross e = list[blockIdx.y];
+    const unsigned long long m = (unsigned long long)e.rn * e.sn;
+    const unsigned long long base = off[e.b];
+    for (unsigned long long o = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; o < m;
+         o += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long g = base + o;
+        if (g >= (unsigned long long)cap) break;
+        const unsigned long long si = o / e.rn, rj = o - si * e.rn;
+        const unsigned long long sv = __ldg(S + e.sb + si), rv = __ldg(R + e.rb + rj);
+        ok[g] = (uint32_t)(sv >> 32);
+        oa[g] = (uint32_t)rv;
+        ob[g] = (uint32_t)sv;
+    }
+}
+
+__global__ void k_pj_place(const PjPlace *__restrict__ list, const unsigned long long *__restrict__ off,
+                           uint32_t *__restrict__ ok, uint32_t *__restrict__ oa, uint32_t *__restrict__ ob,
+                           long long cap) {
+    const PjPlace e = list[blockIdx.y];
+    const unsigned long long base = off[e.b];
+    for (unsigned long long o = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; o < e.m;
+         o += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long g = base + o;
+        if (g >= (unsigned long long)cap) break;
+        ok[g] = e.k[o];
+        oa[g] = e.a[o];
+        ob[g] = e.c[o];
+    }
+}
+
+// Key range of each listed bucket over its R and S' rows: mm[2i] = min, mm[2i+1] = max.
+__global__ void k_pj_minmax(const PjCross *__restrict__ list, const unsigned long long *__restrict__ R,
+                            const unsigned long long *__restrict__ S, uint32_t *__restrict__ mm) {
+    __shared__ uint32_t red[2 * 8];
+    const PjCross e = list[blockIdx.x];
+    uint32_t mn = 0xffffffffu, mx = 0;
+    for (uint32_t i = threadIdx.x; i < e.rn; i += blockDim.x) {
+        const uint32_t k = (uint32_t)(__ldg(R + e.rb + i) >> 32);
+        mn = min(mn, k);
+        mx = max(mx, k);
+    }
+    for (uint32_t i = threadIdx.x; i < e.sn; i += blockDim.x) {
+        const uint32_t k = (uint32_t)(__ldg(S + e.sb + i) >> 32);
+        mn = min(mn, k);
+        mx = max(mx, k);
+    }
+    mn = __reduce_min_sync(QG_FULL_MASK, mn);
+    mx = __reduce_max_sync(QG_FULL_MASK, mx);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { red[w] = mn; red[8 + w] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 1; i < (int)(blockDim.x >> 5); i++) {
+            mn = min(mn, red[i]);
+            mx = max(mx, red[8 + i]);
+        }
+        mm[2 * blockIdx.x] = mn;
+        mm[2 * blockIdx.x + 1] = mx;
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+// host
+// ===========================================================================
+qg_status qg_join_hash_sort(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay, int64_t nR,
+                            const int32_t *skey, const int32_t *spay, int64_t nS, int32_t slo,
+                            int32_t shi, int32_t *out_key, int32_t *out_rpay, int32_t *out_spay,
+                            int64_t cap, int64_t *out_n);
+
+namespace {
+
+int g_pj_variant = 0;  // 0 auto (radix, learned when radix leaves big buckets), 1 radix, 2 learned, 3 hash join + sort
+int g_pj_blog2 = 0;    // 0: bucket count from the input size
+uint32_t g_pj_smax = PB_SMAX, g_pj_rmax = PB_RMAX;
+constexpr long long PB_TARGET = 2560;     // R + S' rows per bucket aimed at
+constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit the learned model
+
+struct PjLevel {
+    PjRange *range;
+    uint32_t *cnt;  // [2 * nb]: R counts, then S' counts
+    uint32_t *rbeg, *sbeg, *big, *mm;
+    unsigned long long *bigcnt, *off, *total, *smp, *smp2;
+    qg_cdf_model *model;
+    PjCross *cross;
+    PjPlace *place;
+};
+
+size_t pj_level_bytes(uint32_t nb) {
+    size_t b = 0;
+    auto add = [&](size_t x) { b += qg_align_up(x, 256); };
+    add(sizeof(PjRange));
+    add((size_t)2 * nb * 4);
+    add((size_t)(nb + 1) * 4);
+    add((size_t)(nb + 1) * 4);
+    add((size_t)nb * 4);
+    add((size_t)2 * nb * 4);
+    add((size_t)nb * 8);
+    add((size_t)nb * 8);
+    add(8);
+    add((size_t)CDF_SAMPLE * 8);
+    add((size_t)CDF_SAMPLE * 8);
+    add(sizeof(qg_cdf_model));
+    add((size_t)nb * sizeof(PjCross));
+    add((size_t)nb * sizeof(PjPlace));
+    return b;
+}
+
+void pj_level_carve(char *p, uint32_t nb, PjLevel *L) {
+    auto take = [&](size_t x) { char *q = p; p += qg_align_up(x, 256); return q; };
+    L->range = (PjRange *)take(sizeof(PjRange));
+    L->cnt = (uint32_t *)take((size_t)2 * nb * 4);
+    L->rbeg = (uint32_t *)take((size_t)(nb + 1) * 4);
+    L->sbeg = (uint32_t *)take((size_t)(nb + 1) * 4);
+    L->big = (uint32_t *)take((size_t)nb * 4);
+    L->mm = (uint32_t *)take((size_t)2 * nb * 4);
+    L->bigcnt = (unsigned long long *)take((size_t)nb * 8);
+    L->off = (unsigned long long *)take((size_t)nb * 8);
+    L->total = (unsigned long long *)take(8);
+    L->smp = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
+    L->smp2 = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
+    L->model = (qg_cdf_model *)take(sizeof(qg_cdf_model));
+    L->cross = (PjCross *)take((size_t)nb * sizeof(PjCross));
+    L->place = (PjPlace *)take((size_t)nb * sizeof(PjPlace));
+}
+
+qg_status pj_attrs(qg_ctx *ctx) {
+    static bool done = false;
+    if (!done) {
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, PJ_MAX_BUCKETS * 4), "attr hist");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PbSmem)), "attr join");
+        done = true;
+    }
+    return QG_OK;
+}
+
+int pj_grid(qg_ctx *ctx, long long work, int per_block, int per_sm) {
+    long long b = (work + per_block - 1) / per_block;
+    const long long c = (long long)ctx->sm_count * per_sm;
+    if (b > c) b = c;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+// Bucket counts of both sides into h[0 .. 2 nb) (R then S'); synchronises.
+qg_status pj_hist(qg_ctx *ctx, const qg_part_fn &pf, uint32_t nb, const unsigned long long *r,
+                  long long nR, const unsigned long long *s, long long nS, uint32_t *d_cnt,
+                  std::vector<uint32_t> &h) {
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, (size_t)2 * nb * 4, ctx->stream), "memset counts");
+    const size_t smem = (size_t)nb * 4;
+    qg_pre_launch(ctx);
+    k_pj_hist<<<pj_grid(ctx, nR, 1024, 1), 1024, smem, ctx->stream>>>(r, nR, pf, nb, d_cnt, ctx->ctl);
+    QG_TRY(qg_check_launch(ctx, "k_pj_hist"));
+    qg_pre_launch(ctx);
+    k_pj_hist<<<pj_grid(ctx, nS, 1024, 1), 1024, smem, ctx->stream>>>(s, nS, pf, nb, d_cnt + nb, ctx->ctl);
+    QG_TRY(qg_check_launch(ctx, "k_pj_hist"));
+    h.resize((size_t)2 * nb);
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), d_cnt, (size_t)2 * nb * 4, cudaMemcpyDeviceToHost, ctx->stream), "counts d2h");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    return qg_collect_error(ctx);
+}
+
+// Rows in buckets that do not fit the bucket kernel.
+long long pj_oversize_rows(const std::vector<uint32_t> &h, uint32_t nb, uint32_t *nbig) {
+    long long rows = 0;
+    uint32_t c = 0;
+    for (uint32_t b = 0; b < nb; b++) {
+        const uint32_t rc = h[b], sc = h[nb + b];
+        if (rc && sc && (rc > g_pj_rmax || sc > g_pj_smax)) {
+            rows += (long long)rc + sc;
+            c++;
+        }
+    }
+    if (nbig) *nbig = c;
+    return rows;
+}
+
+// Fit the learned model on a sample of both sides' keys (records).
+qg_status pj_train(qg_ctx *ctx, const PjLevel &L, uint32_t nb, const unsigned long long *r, long long nR,
+                   const unsigned long long *s, long long nS) {
+    const long long n = nR + nS;
+    const long long m = n < CDF_SAMPLE ? n : CDF_SAMPLE;
+    long long mR = nR ? (m * nR) / n : 0;
+    if (nR && mR < 1) mR = 1;
+    if (nS && mR >= m) mR = m - 1;
+    qg_pre_launch(ctx);
+    k_cdf_sample<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(r, nR, s, nS, mR, m, L.smp);
+    QG_TRY(qg_check_launch(ctx, "k_cdf_sample"));
+    QG_TRY(qg_sort_rec_inplace(ctx, L.smp, L.smp2, m));
+    long long hthr = (3 * m + nb - 1) / nb;
+    if (hthr < 2) hthr = 2;
+    qg_pre_launch(ctx);
+    k_cdf_fit<<<1, FIT_THREADS, 0, ctx->stream>>>(L.smp, m, nb, hthr, L.model);
+    return qg_check_launch(ctx, "k_cdf_fit");
+}
+
+struct PjTemp {
+    uint32_t *k = nullptr, *a = nullptr, *c = nullptr;
+    void release() {
+        if (k) cudaFree(k);
+        if (a) cudaFree(a);
+        if (c) cudaFree(c);
+        k = a = c = nullptr;
+    }
+};
+
+qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
+                  unsigned long long *s, unsigned long long *ssp, long long nS, uint32_t kmin,
+                  uint32_t kmax, int variant, uint32_t *ok, uint32_t *oa, uint32_t *ob, long long cap,
+                  long long *M_out, int depth, char *lvl_mem);
+
+// Join one oversize multi-key bucket into freshly allocated columns.
+qg_status pj_sub(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
+                 unsigned long long *s, unsigned long long *ssp, long long nS, uint32_t kmin,
+                 uint32_t kmax, int variant, int depth, PjTemp *t, long long *M) {
+    long long capt = nS + nR + 1024;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        t->release();
+        if (cudaMalloc((void **)&t->k, (size_t)capt * 4) != cudaSuccess ||
+            cudaMalloc((void **)&t->a, (size_t)capt * 4) != cudaSuccess ||
+            cudaMalloc((void **)&t->c, (size_t)capt * 4) != cudaSuccess) {
+            cudaGetLastError();
+            t->release();
+            return QG_ERR_OOM;
+        }
+        QG_TRY(pj_core(ctx, r, rsp, nR, s, ssp, nS, kmin, kmax, variant, t->k, t->a, t->c, capt, M,
+                       depth, nullptr));
+        if (*M <= capt) return QG_OK;
+        capt = *M;
+    }
+    return QG_ERR_CAPACITY;
+}
+
+struct PjLevelMem {
+    char *p = nullptr;
+    bool own = false;
+    ~PjLevelMem() {
+        if (own && p) cudaFree(p);
+    }
+};
+
+qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
+                  unsigned long long *s, unsigned long long *ssp, long long nS, uint32_t kmin,
+                  uint32_t kmax, int variant, uint32_t *ok, uint32_t *oa, uint32_t *ob, long long cap,
+                  long long *M_out, int depth, char *lvl_mem) {
+    *M_out = 0;
+    if (nR == 0 || nS == 0) return QG_OK;
+    if (depth > 6) return QG_ERR_UNSUPPORTED;
+    QG_TRY(pj_attrs(ctx));
+    const long long ntot = nR + nS;
+    // Buckets: about PB_TARGET rows each, and room for twice the rows of each
+    // side at the bucket kernel's capacity.  A nested level splits its key
+    // range at least 256 ways, so that every level narrows it and the
+    // recursion ends in single-key buckets.
+    uint32_t nb = depth > 0 ? 256u : 1u;
+    if (g_pj_blog2 > 0 && depth == 0) nb = 1u << g_pj_blog2;
+    else
+        while (nb < (uint32_t)PJ_MAX_BUCKETS &&
+               ((long long)nb * PB_TARGET < ntot || (long long)nb * g_pj_smax < 2 * nS ||
+                (long long)nb * g_pj_rmax < 2 * nR))
+            nb <<= 1;
+    int lb2 = 0;
+    while ((1u << lb2) < nb) lb2++;
+    const uint32_t range = kmax - kmin;
+    const int bits = range ? 32 - __builtin_clz(range) : 0;
+    const int shift = bits > lb2 ? bits - lb2 : 0;
+    const uint32_t nb_radix = (uint32_t)(((unsigned long long)range >> shift) + 1);
+
+    PjLevelMem lm;
+    lm.p = lvl_mem;
+    if (!lm.p) {
+        if (cudaMalloc((void **)&lm.p, pj_level_bytes(nb)) != cudaSuccess) {
+            cudaGetLastError();
+            return QG_ERR_OOM;
+        }
+        lm.own = true;
+    }
+    PjLevel L;
+    pj_level_carve(lm.p, nb, &L);
+    const qg_part_fn radix{0, kmin, shift, nullptr};
+    const qg_part_fn learned{1, 0u, 0, L.model};
+
+    std::vector<uint32_t> h;
+    QG_TRY(pj_hist(ctx, radix, nb_radix, r, nR, s, nS, L.cnt, h));
+    uint32_t nbig = 0;
+    const long long over_radix = pj_oversize_rows(h, nb_radix, &nbig);
+    bool use_learned = variant == 2;
+    bool judged = false;
+    if (variant == 0 && depth == 0 && over_radix * 50 > ntot) use_learned = judged = true;
+    uint32_t nbu = nb_radix;
+    if (use_learned) {
+        QG_TRY(pj_train(ctx, L, nb, r, nR, s, nS));
+        std::vector<uint32_t> h2;
+        QG_TRY(pj_hist(ctx, learned, nb, r, nR, s, nS, L.cnt, h2));
+        uint32_t nbig2 = 0;
+        const long long over_learned = pj_oversize_rows(h2, nb, &nbig2);
+        // Radix partitioning judges the learned model: keep radix when the
+        // model does not leave fewer rows in oversize buckets.
+        if (judged && over_learned >= over_radix) {
+            use_learned = false;
+        } else {
+            h.swap(h2);
+            nbu = nb;
+            nbig = nbig2;
+        }
+    }
+    const qg_part_fn &pf = use_learned ? learned : radix;
+
+    // bucket offsets and digit bases of the partition passes
+    std::vector<uint32_t> rbeg(nbu + 1), sbeg(nbu + 1);
+    uint32_t hr[4 * QG_RADIX] = {0}, hs[4 * QG_RADIX] = {0};
+    int bb = 0;
+    while ((1u << bb) < nbu) bb++;
+    const int npos = (bb + 7) / 8;
+    {
+        uint32_t rr = 0, ss = 0;
+        for (uint32_t b = 0; b < nbu; b++) {
+            rbeg[b] = rr;
+            sbeg[b] = ss;
+            rr += h[b];
+            ss += h[nbu + b];
+            for (int p = 0; p < npos; p++) {
+                hr[p * QG_RADIX + ((b >> (8 * p)) & 255u)] += h[b];
+                hs[p * QG_RADIX + ((b >> (8 * p)) & 255u)] += h[nbu + b];
+            }
+        }
+        rbeg[nbu] = rr;
+        sbeg[nbu] = ss;
+    }
+    // partition both sides by bucket
+    if (npos > 0) {
+        int passes[4], np;
+        uint32_t bases[4 * QG_RADIX];
+        bool in_b = false;
+        np = qg_sort_plan(hr, npos, nR, passes, bases);
+        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{r, nullptr, nullptr, nullptr},
+                                  qg_sort_bufs{rsp, nullptr, nullptr, nullptr}, nR, pf, passes, np, bases,
+                                  &in_b));
+        if (in_b) std::swap(r, rsp);
+        np = qg_sort_plan(hs, npos, nS, passes, bases);
+        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{s, nullptr, nullptr, nullptr},
+                                  qg_sort_bufs{ssp, nullptr, nullptr, nullptr}, nS, pf, passes, np, bases,
+                                  &in_b));
+        if (in_b) std::swap(s, ssp);
+    }
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.rbeg, rbeg.data(), (size_t)(nbu + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "rbeg h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.sbeg, sbeg.data(), (size_t)(nbu + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "sbeg h2d");
+
+    // buckets handled outside the bucket kernel
+    std::vector<uint32_t> big(nbu, 0);
+    std::vector<unsigned long long> bigcnt(nbu, 0);
+    std::vector<PjCross> over, cross;
+    std::vector<PjPlace> place;
+    std::vector<PjTemp> temps;
+    int depth_max = depth;
+    for (uint32_t b = 0; b < nbu; b++) {
+        const uint32_t rc = h[b], sc = h[nbu + b];
+        if (rc && sc && (rc > g_pj_rmax || sc > g_pj_smax)) over.push_back(PjCross{b, rbeg[b], rc, sbeg[b], sc});
+    }
+    qg_status st = QG_OK;
+    if (!over.empty()) {
+        std::vector<uint32_t> mm(2 * over.size());
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, over.data(), over.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "list h2d");
+        qg_pre_launch(ctx);
+        k_pj_minmax<<<(unsigned)over.size(), 256, 0, ctx->stream>>>(L.cross, r, s, L.mm);
+        QG_TRY(qg_check_launch(ctx, "k_pj_minmax"));
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(mm.data(), L.mm, mm.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "mm d2h");
+        QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+        temps.reserve(over.size());
+        for (size_t i = 0; i < over.size() && st == QG_OK; i++) {
+            const PjCross &e = over[i];
+            big[e.b] = 1;
+            if (mm[2 * i] == mm[2 * i + 1]) {
+                bigcnt[e.b] = (unsigned long long)e.rn * e.sn;
+                cross.push_back(e);
+            } else {
+                temps.emplace_back();
+                long long Mb = 0;
+                const int sub_variant = variant == 2 ? 2 : 1;
+                st = pj_sub(ctx, r + e.rb, rsp + e.rb, e.rn, s + e.sb, ssp + e.sb, e.sn, mm[2 * i],
+                            mm[2 * i + 1], sub_variant, depth + 1, &temps.back(), &Mb);
+                bigcnt[e.b] = (unsigned long long)Mb;
+                place.push_back(PjPlace{e.b, temps.back().k, temps.back().a, temps.back().c,
+                                        (unsigned long long)Mb});
+                if (ctx->pj_stats[4] > (uint32_t)depth_max) depth_max = (int)ctx->pj_stats[4];
+            }
+        }
+    }
+    if (st != QG_OK) {
+        for (auto &t : temps) t.release();
+        return st;
+    }
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.big, big.data(), (size_t)nbu * 4, cudaMemcpyHostToDevice, ctx->stream), "big h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.bigcnt, bigcnt.data(), (size_t)nbu * 8, cudaMemcpyHostToDevice, ctx->stream), "bigcnt h2d");
+
+    // the bucket kernel (look-back status from the scratch arena, taken after
+    // the nested calls, which use the arena themselves)
+    qg_lookback lb;
+    QG_TRY(qg_lb_make(ctx, nbu, QG_SITE_JOIN_PROBE, &lb));
+    PbArgs args{r, s, L.rbeg, L.sbeg, L.big, L.bigcnt, L.off, L.total, ok, oa, ob, cap};
+    qg_pre_launch(ctx);
+    k_pj_join<<<nbu, PB_THREADS, sizeof(PbSmem), ctx->stream>>>(args, lb);
+    QG_TRY(qg_check_launch(ctx, "k_pj_join"));
+    if (!cross.empty()) {
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, cross.data(), cross.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "cross h2d");
+        qg_pre_launch(ctx);
+        k_pj_cross<<<dim3((unsigned)pj_grid(ctx, 1LL << 24, 256, 4), (unsigned)cross.size()), 256, 0, ctx->stream>>>(
+            L.cross, r, s, L.off, ok, oa, ob, cap);
+        QG_TRY(qg_check_launch(ctx, "k_pj_cross"));
+    }
+    if (!place.empty()) {
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.place, place.data(), place.size() * sizeof(PjPlace), cudaMemcpyHostToDevice, ctx->stream), "place h2d");
+        qg_pre_launch(ctx);
+        k_pj_place<<<dim3((unsigned)pj_grid(ctx, 1LL << 24, 256, 4), (unsigned)place.size()), 256, 0, ctx->stream>>>(
+            L.place, L.off, ok, oa, ob, cap);
+        QG_TRY(qg_check_launch(ctx, "k_pj_place"));
+    }
+    unsigned long long total = 0;
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    total = (unsigned long long)ctx->pinned[0];
+    for (auto &t : temps) t.release();
+    // The look-back sums are 32-bit: recompute the total in 64 bits from the
+    // outside buckets when they alone could wrap it.
+    *M_out = (long long)total;
+    {
+        unsigned long long outside = 0;
+        for (uint32_t b = 0; b < nbu; b++) outside += bigcnt[b];
+        if (outside >= (1ull << 32)) *M_out = (long long)outside;  // capacity error follows
+    }
+    if (depth == 0) {
+        ctx->pj_stats[0] = use_learned ? 2 : 1;
+        ctx->pj_stats[1] = nbu;
+        ctx->pj_stats[2] = (uint32_t)over.size();
+        long long orows = 0;
+        for (auto &e : over) orows += (long long)e.rn + e.sn;
+        ctx->pj_stats[3] = orows > 0xffffffffLL ? 0xffffffffu : (uint32_t)orows;
+        ctx->pj_stats[5] = 0;
+        ctx->pj_stats[6] = 0;
+        if (use_learned) {
+            uint32_t hk[4];
+            cudaMemcpy(hk, L.model, 16, cudaMemcpyDeviceToHost);
+            ctx->pj_stats[5] = hk[0];
+            ctx->pj_stats[6] = hk[3];
+        }
+        ctx->pj_stats[7] = judged ? 1 : 0;
+    }
+    ctx->pj_stats[4] = (uint32_t)depth_max;
+    return QG_OK;
+}
+
+}  // namespace
+
+extern "C" QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucket_s_max,
+                                              uint32_t bucket_r_max) {
+    if (variant < 0 || variant > 3 || buckets_log2 < 0 || buckets_log2 > 15) return QG_ERR_INVALID;
+    if (bucket_s_max > (uint32_t)PB_SMAX || bucket_r_max > (uint32_t)PB_RMAX) return QG_ERR_INVALID;
+    g_pj_variant = variant;
+    g_pj_blog2 = buckets_log2;
+    g_pj_smax = bucket_s_max ? bucket_s_max : PB_SMAX;
+    g_pj_rmax = bucket_r_max ? bucket_r_max : PB_RMAX;
+    return QG_OK;
+}
+
+extern "C" QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8) {
+    if (!ctx || !out8) return QG_ERR_INVALID;
+    memcpy(out8, ctx->pj_stats, sizeof(ctx->pj_stats));
+    return QG_OK;
+}
+
+extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay,
+                                                int64_t nR, const int32_t *skey, const int32_t *spay,
+                                                int64_t nS, int32_t slo, int32_t shi, int32_t *out_key,
+                                                int32_t *out_rpay, int32_t *out_spay, int64_t cap,
+                                                int64_t *out_n) {
+    if (!ctx || nR < 0 || nS < 0 || cap < 0 || !out_n) return QG_ERR_INVALID;
+    if ((nR > 0 && (!rkey || !rpay)) || (nS > 0 && (!skey || !spay)) ||
+        (cap > 0 && (!out_key || !out_rpay || !out_spay)))
+        return QG_ERR_INVALID;
+    if ((((uintptr_t)skey) | ((uintptr_t)spay)) & 15) return QG_ERR_INVALID;
+    if (cap >= (1LL << 30) || nS >= (1LL << 40)) return QG_ERR_UNSUPPORTED;
+    if (g_pj_variant == 3 || nS >= (1LL << 30) || nR >= (1LL << 30))
+        return qg_join_hash_sort(ctx, rkey, rpay, nR, skey, spay, nS, slo, shi, out_key, out_rpay,
+                                 out_spay, cap, out_n);
+    *out_n = 0;
+    memset(ctx->pj_stats, 0, sizeof(ctx->pj_stats));
+    if (nR == 0 || nS == 0) return QG_OK;
+    // aux: R records + spare, S' records + spare, level-0 arrays
+    const size_t rb = qg_align_up((size_t)nR * 8, 256), sb = qg_align_up((size_t)nS * 8, 256);
+    char *aux;
+    QG_TRY(qg_aux(ctx, 2 * rb + 2 * sb + pj_level_bytes(PJ_MAX_BUCKETS), &aux));
+    unsigned long long *R = (unsigned long long *)aux, *Rsp = (unsigned long long *)(aux + rb);
+    unsigned long long *S = (unsigned long long *)(aux + 2 * rb), *Ssp = (unsigned long long *)(aux + 2 * rb + sb);
+    char *lvl = aux + 2 * rb + 2 * sb;
+    PjRange *range = (PjRange *)lvl;  // first member of the level-0 arrays
+    qg_pre_launch(ctx);
+    k_pj_range_init<<<1, 1, 0, ctx->stream>>>(range);
+    QG_TRY(qg_check_launch(ctx, "k_pj_range_init"));
+    qg_pre_launch(ctx);
+    k_pj_rrec<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, R, range);
+    QG_TRY(qg_check_launch(ctx, "k_pj_rrec"));
+    PjRange hr;
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(&hr, range, sizeof(hr), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    constexpr int SF_TILE = SF_THREADS * SF_ROUNDS * 4;
+    const long long tiles = (nS + SF_TILE - 1) / SF_TILE;
+    qg_lookback lbs;
+    QG_TRY(qg_lb_make(ctx, tiles, QG_SITE_FILTER, &lbs));
+    qg_pre_launch(ctx);
+    k_pj_sfilter<<<(unsigned)tiles, SF_THREADS, 0, ctx->stream>>>(skey, spay, nS, slo, shi, hr.kmin, hr.kmax, S,
+                                                                 (long long *)&range->count, lbs);
+    QG_TRY(qg_check_launch(ctx, "k_pj_sfilter"));
+    long long ns1 = 0;
+    QG_TRY(qg_read_i64(ctx, (const long long *)&range->count, &ns1));
+    QG_TRY(qg_collect_error(ctx));
+    long long M = 0;
+    QG_TRY(pj_core(ctx, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, g_pj_variant, (uint32_t *)out_key,
+                   (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M, 0, lvl));
+    QG_TRY(qg_collect_error(ctx));
+    *out_n = M;
+    return M > cap ? QG_ERR_CAPACITY : QG_OK;
+}
+
+// ---- learned partition function as a stand-alone tool ---------------------
+extern "C" QG_API int64_t qg_part_model_bytes(void) { return (int64_t)sizeof(qg_cdf_model); }
+
+namespace {
+__global__ void k_keys_to_items(const uint32_t *__restrict__ keys, long long n, long long m,
+                                unsigned long long *__restrict__ out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = (unsigned long long)__ldg(keys + (i * n) / m) << 32;
+}
+}  // namespace
+
+extern "C" QG_API qg_status qg_part_learn(qg_ctx *ctx, const uint32_t *keys, int64_t n, uint32_t nbuckets,
+                                          void *d_model) {
+    if (!ctx || !keys || n <= 0 || !d_model || nbuckets < 1 || nbuckets > (uint32_t)PJ_MAX_BUCKETS)
+        return QG_ERR_INVALID;
+    const long long m = n < CDF_SAMPLE ? n : CDF_SAMPLE;
+    char *aux;
+    QG_TRY(qg_aux(ctx, (size_t)m * 16 + 256, &aux));
+    unsigned long long *smp = (unsigned long long *)aux, *smp2 = smp + m;
+    qg_pre_launch(ctx);
+    k_keys_to_items<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(keys, n, m, smp);
+    QG_TRY(qg_check_launch(ctx, "k_keys_to_items"));
+    QG_TRY(qg_sort_rec_inplace(ctx, smp, smp2, m));
+    long long hthr = (3 * m + nbuckets - 1) / nbuckets;
+    if (hthr < 2) hthr = 2;
+    qg_pre_launch(ctx);
+    k_cdf_fit<<<1, FIT_THREADS, 0, ctx->stream>>>(smp, m, nbuckets, hthr, (qg_cdf_model *)d_model);
+    QG_TRY(qg_check_launch(ctx, "k_cdf_fit"));
+    return qg_ctx_check(ctx);
+}
+
+extern "C" QG_API qg_status qg_part_eval(qg_ctx *ctx, const void *d_model, uint32_t kmin, int shift,
+                                         const uint32_t *keys, int64_t n, uint32_t *buckets) {
+    if (!ctx || n < 0 || shift < 0 || shift > 31 || (n > 0 && (!keys || !buckets))) return QG_ERR_INVALID;
+    if (n == 0) return QG_OK;
+    qg_part_fn pf{d_model ? 1 : 0, kmin, shift, (const qg_cdf_model *)d_model};
+    qg_pre_launch(ctx);
+    k_part_eval<<<pj_grid(ctx, n, 256, 8), 256, 0, ctx->stream>>>(keys, n, pf, buckets);
+    QG_TRY(qg_check_launch(ctx, "k_part_eval"));
+    return qg_ctx_check(ctx);
+}

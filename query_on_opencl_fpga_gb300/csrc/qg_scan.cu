@@ -95,9 +95,8 @@ qg_status qg_scan_launch(qg_ctx *ctx, const int32_t *in, int32_t *out, int64_t n
     if (n == 0) return QG_OK;
     int64_t tiles = qg_ceil_div(n, TILE);
     if (tiles > 0x7fffffff) return QG_ERR_UNSUPPORTED;
-    char *scr;
-    QG_TRY(qg_scratch(ctx, qg_lb_bytes(tiles), &scr));
-    qg_lookback lb{(unsigned long long *)scr, ctx->ctl, ctx->spin_limit, QG_SITE_SCAN};
+    qg_lookback lb;
+    QG_TRY(qg_lb_make(ctx, tiles, QG_SITE_SCAN, &lb));
     bool vec = (((uintptr_t)in | (uintptr_t)out) & 15) == 0;
     qg_pre_launch(ctx);
     if (vec)

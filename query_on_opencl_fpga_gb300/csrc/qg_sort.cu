@@ -24,6 +24,7 @@
 #include <vector>
 #include "qg_internal.cuh"
 #include "qg_sort.cuh"
+#include "qg_part.cuh"
 
 namespace {
 
@@ -65,13 +66,23 @@ struct RsSmem {
     // REC: v holds the u64 items; KV3: v holds (a, b) pairs and k the keys
     unsigned long long v[RS_TILE];
     uint32_t k[KV3 ? RS_TILE : 1];
+    uint8_t dg[RS_TILE];  // digit of each reordered item
 };
 
-template <bool KV3>
+// Digit of a key: radix form ((k - key_off) >> shift) & 255, or the bits
+// [shift, shift + 8) of the learned partition bucket of k.
+template <bool LEARNED>
+__device__ __forceinline__ uint32_t rs_digit(uint32_t k, uint32_t key_off, int shift,
+                                             const qg_cdf_model *model) {
+    if (LEARNED) return (qg_cdf_bucket(model, k) >> shift) & 255u;
+    return (uint32_t)((unsigned long long)(k - key_off) >> shift) & 255u;  // shift may exceed 31
+}
+
+template <bool KV3, bool LEARNED>
 __global__ void __launch_bounds__(RS_THREADS)
 k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
-             const uint32_t *__restrict__ dbase, uint32_t *__restrict__ status, qg_control *ctl,
-             uint32_t spin_limit) {
+             const qg_cdf_model *model, const uint32_t *__restrict__ dbase,
+             uint32_t *__restrict__ status, qg_control *ctl, uint32_t spin_limit) {
     extern __shared__ __align__(16) unsigned char rs_raw[];
     RsSmem<KV3> &S = *reinterpret_cast<RsSmem<KV3> *>(rs_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -86,6 +97,7 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
     uint32_t key[RS_ITEMS];
     unsigned long long val[RS_ITEMS];
     uint32_t rank[RS_ITEMS];
+    uint32_t dpack[RS_ITEMS / 4];  // the items' digits, four per word
     // All loads are issued before any ranking: __syncwarp orders memory, so
     // a load placed after one in program order cannot be hoisted above it,
     // and interleaving would pay one DRAM latency per item.
@@ -109,7 +121,9 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
     for (int i = 0; i < RS_ITEMS; i++) {
         long long idx = wbase + i * 32 + lane;
         bool valid = idx < n;
-        uint32_t d = ((key[i] - key_off) >> shift) & 255u;
+        uint32_t d = rs_digit<LEARNED>(key[i], key_off, shift, model);
+        if ((i & 3) == 0) dpack[i >> 2] = 0;
+        dpack[i >> 2] |= d << (8 * (i & 3));
         uint32_t peers = __ballot_sync(QG_FULL_MASK, valid);
 #pragma unroll
         for (int b = 0; b < 8; b++) {
@@ -195,9 +209,10 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
     for (int i = 0; i < RS_ITEMS; i++) {
         long long idx = wbase + i * 32 + lane;
         if (idx < n) {
-            uint32_t d = ((key[i] - key_off) >> shift) & 255u;
+            uint32_t d = (dpack[i >> 2] >> (8 * (i & 3))) & 255u;
             uint32_t pos = S.dstart[d] + S.whist[warp][d] + rank[i];
             S.v[pos] = val[i];
+            S.dg[pos] = (uint8_t)d;
             if (KV3) S.k[pos] = key[i];
         }
     }
@@ -207,7 +222,7 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
     for (int p = tid; p < cnt; p += RS_THREADS) {
         unsigned long long v = S.v[p];
         uint32_t k = KV3 ? S.k[p] : (uint32_t)(v >> 32);
-        uint32_t d = ((k - key_off) >> shift) & 255u;
+        uint32_t d = S.dg[p];
         uint32_t g = S.goff[d] + (uint32_t)p;
         if (KV3) {
             dst.k[g] = k;
@@ -268,49 +283,66 @@ int qg_sort_plan(const uint32_t *h_hist, int npos, long long n, int *passes, uin
     return np;
 }
 
-qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
-                          uint32_t key_off, const int *passes, int np, const uint32_t *h_bases,
-                          bool *result_in_b) {
+template <bool KV3, bool LEARNED>
+static qg_status rs_set_attr(qg_ctx *ctx) {
+    static bool done = false;
+    if (!done) {
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, LEARNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sizeof(RsSmem<KV3>)), "attr");
+        done = true;
+    }
+    return QG_OK;
+}
+
+qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
+                             const qg_part_fn &pf, const int *passes, int np, const uint32_t *h_bases,
+                             bool *result_in_b) {
     *result_in_b = false;
     if (np == 0 || n <= 1) return QG_OK;
     if (n >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
+    if (kv3 && pf.learned) return QG_ERR_UNSUPPORTED;
     const long long tiles = (n + RS_TILE - 1) / RS_TILE;
     size_t need = 4 * QG_RADIX * 4 + (size_t)tiles * QG_RADIX * 4;
     char *scr;
     QG_TRY(qg_scratch(ctx, need, &scr));
     uint32_t *dbase = (uint32_t *)scr;
     uint32_t *status = dbase + 4 * QG_RADIX;
-    // The bases go up through the context's pinned slots area: synchronous
-    // copy of 4 KB, issued in stream order.
+    // 4 KB of digit bases, in stream order before the passes that read them.
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(dbase, h_bases, 4 * QG_RADIX * 4, cudaMemcpyHostToDevice, ctx->stream), "bases h2d");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
-    static bool attr_done[2] = {false, false};
-    if (!attr_done[kv3]) {
-        if (kv3)
-            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RsSmem<true>)), "attr");
-        else
-            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RsSmem<false>)), "attr");
-        attr_done[kv3] = true;
-    }
+    if (kv3) QG_TRY((rs_set_attr<true, false>(ctx)));
+    else if (pf.learned) QG_TRY((rs_set_attr<false, true>(ctx)));
+    else QG_TRY((rs_set_attr<false, false>(ctx)));
     bool in_a = true;
     for (int i = 0; i < np; i++) {
         const int p = passes[i];
         QG_TRY_CUDA(ctx, cudaMemsetAsync(status, 0, (size_t)tiles * QG_RADIX * 4, ctx->stream), "memset status");
         const qg_sort_bufs &s = in_a ? a : b;
         const qg_sort_bufs &d = in_a ? b : a;
+        const int shift = pf.learned ? 8 * p : pf.shift + 8 * p;
         qg_pre_launch(ctx);
         if (kv3)
-            k_radix_pass<true><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, 8 * p, key_off, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+            k_radix_pass<true, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+        else if (pf.learned)
+            k_radix_pass<false, true><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n, shift, 0u, pf.model, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
         else
-            k_radix_pass<false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, 8 * p, key_off, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+            k_radix_pass<false, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
         in_a = !in_a;
     }
     *result_in_b = !in_a;
     return QG_OK;
+}
+
+qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
+                          uint32_t key_off, const int *passes, int np, const uint32_t *h_bases,
+                          bool *result_in_b) {
+    qg_part_fn pf{0, key_off, 0, nullptr};
+    return qg_radix_passes_pf(ctx, kv3, a, b, n, pf, passes, np, h_bases, result_in_b);
 }
 
 // Sort REC items in `data` (n u64) using `tmp` (n u64) as the ping-pong

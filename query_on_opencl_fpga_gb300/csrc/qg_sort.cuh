@@ -26,6 +26,12 @@ int qg_sort_plan(const uint32_t *h_hist, int npos, long long n, int *passes, uin
 qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
                           uint32_t key_off, const int *passes, int np, const uint32_t *h_bases,
                           bool *result_in_b);
+// Same, with the digits taken from a partition function: pass position p
+// sorts by bits [8p, 8p + 8) of the bucket (radix form: of (k - kmin) >> shift).
+struct qg_part_fn;
+qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
+                             const qg_part_fn &pf, const int *passes, int np, const uint32_t *h_bases,
+                             bool *result_in_b);
 // Sort REC items in place with `tmp` as the second buffer (synchronises once).
 qg_status qg_sort_rec_inplace(qg_ctx *ctx, unsigned long long *data, unsigned long long *tmp,
                               long long n);

@@ -78,20 +78,45 @@ def config2_join(nR: int = 1 << 24, nS: int = 1 << 28, seed: int = 0, device="cp
     return {"rkey": rkey, "rpay": rpay, "skey": skey, "spay": spay, "slo": -(2 ** 31), "shi": 299}
 
 
-def skewed_keys(n: int, seed: int, device="cpu", heavy_frac: float = 0.05) -> torch.Tensor:
-    """8 Gaussians (means uniform over int32, sigma 2^20) + Zipf(1.2) heavy hitters."""
+def skewed_keys(n: int, seed: int, device="cpu", heavy_frac: float = 0.05,
+                sample_seed: int | None = None) -> torch.Tensor:
+    """8 Gaussians (means uniform over int32, sigma 2^20) + Zipf(1.2) heavy hitters.
+
+    `seed` fixes the mixture (means, heavy keys); `sample_seed` (default
+    `seed`) the draws, so that two sides can share one mixture."""
     g = _gen(seed, device)
     means = torch.randint(-(2 ** 31) + (1 << 24), 2 ** 31 - (1 << 24), (8,), generator=g,
                           device=device, dtype=torch.int64).to(torch.float64)
-    comp = torch.randint(0, 8, (n,), generator=g, device=device)
-    x = means[comp] + torch.randn(n, generator=g, device=device, dtype=torch.float64) * float(1 << 20)
-    x = x.round().clamp(-(2 ** 31), 2 ** 31 - 1).to(torch.int64)
-    heavy = torch.rand(n, generator=g, device=device) < heavy_frac
-    hk = zipf_ranks(n, 1 << 16, 1.2, seed + 11, device)
     hkeys = torch.randint(-(2 ** 31), 2 ** 31 - 1, (1 << 16,), generator=g, device=device,
                           dtype=torch.int64)
+    gs = _gen(seed if sample_seed is None else sample_seed + 1_000_003, device)
+    comp = torch.randint(0, 8, (n,), generator=gs, device=device)
+    x = means[comp] + torch.randn(n, generator=gs, device=device, dtype=torch.float64) * float(1 << 20)
+    x = x.round().clamp(-(2 ** 31), 2 ** 31 - 1).to(torch.int64)
+    heavy = torch.rand(n, generator=gs, device=device) < heavy_frac
+    hk = zipf_ranks(n, 1 << 16, 1.2, (seed if sample_seed is None else sample_seed) + 11, device)
     x = torch.where(heavy, hkeys[hk], x)
     return x.to(torch.int32)
+
+
+def config4_skewed(nR: int = 1 << 25, nS: int = 1 << 28, seed: int = 0, device="cpu"):
+    """Skewed join: R = nR distinct keys drawn from the mixture (a unique
+    build side, as in config 2), S = nS keys drawn from the same mixture
+    (heavy hitters included), payloads uniform [0, 1000), filter S.payload < 300."""
+    want = nR
+    draw = int(nR * 1.6) + 1024
+    while True:
+        cand = torch.unique(skewed_keys(draw, seed, device, sample_seed=seed + 1))
+        if cand.numel() >= want:
+            break
+        draw *= 2
+    perm = torch.randperm(cand.numel(), generator=_gen(seed + 2, device), device=device)[:want]
+    rkey = cand[perm].to(torch.int32)
+    del cand, perm
+    rpay = uniform_i32(nR, 0, 1000, seed + 3, device)
+    skey = skewed_keys(nS, seed, device, sample_seed=seed + 4)
+    spay = uniform_i32(nS, 0, 1000, seed + 5, device)
+    return {"rkey": rkey, "rpay": rpay, "skey": skey, "spay": spay, "slo": -(2 ** 31), "shi": 299}
 
 
 def records(key: torch.Tensor, payload: torch.Tensor | None = None) -> torch.Tensor:

@@ -1,0 +1,135 @@
+"""GPU parity of the join variants (radix / learned range partitions, hash +
+sort) against the oracle, including the buckets that leave the shared-memory
+bucket kernel (single-key cross products and recursive sub-joins), skewed
+keys with heavy hitters, and the learned partition function itself."""
+import numpy as np
+import pytest
+import torch
+
+from query_on_opencl_fpga_gb300 import datagen
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def check_join(got, exp):
+    gk, ga, gb = [t.cpu().numpy() for t in got]
+    u = gk.view(np.uint32)
+    assert (u[1:] >= u[:-1]).all(), "output not sorted by key"
+    ek, ea, eb = [np.asarray(x) for x in exp]
+    assert gk.size == ek.size
+    g = np.lexsort((gb, ga, u))
+    e = np.lexsort((eb, ea, ek.view(np.uint32)))
+    assert np.array_equal(gk[g], ek[e])
+    assert np.array_equal(ga[g], ea[e])
+    assert np.array_equal(gb[g], eb[e])
+
+
+@pytest.fixture
+def knobs(ctx):
+    yield ctx.join_set_knobs
+    ctx.join_set_knobs(0, 0, 0, 0)
+
+
+CASES = [
+    # nR, nS, R keyspace, S keyspace (duplicates in R when nR > keyspace)
+    (1, 1, 1, 1),
+    (10, 1000, 20, 40),
+    (4096, 100003, 8192, 16384),
+    (1 << 16, 1 << 20, 1 << 17, 1 << 18),
+    (100, 50000, 50, 100),
+    (3000, 200000, 1 << 31, 1 << 31),  # sparse keys: wide buckets, bitonic path
+]
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("nR,nS,kr,ks", CASES)
+def test_join_variants(ctx, orc, knobs, variant, nR, nS, kr, ks):
+    knobs(variant)
+    rng = np.random.default_rng(nR * 7 + nS + variant)
+    rkey = (rng.integers(0, kr, nR) - (kr // 2 if kr > 1 << 30 else 0)).astype(np.int64).astype(np.int32)
+    rpay = rng.integers(0, 1000, nR).astype(np.int32)
+    skey = (rng.integers(0, ks, nS) - (ks // 2 if ks > 1 << 30 else 0)).astype(np.int64).astype(np.int32)
+    if ks > 1 << 30:  # make sparse keys hit R too
+        pick = rng.random(nS) < 0.5
+        skey[pick] = rkey[rng.integers(0, nR, int(pick.sum()))]
+    spay = rng.integers(0, 1000, nS).astype(np.int32)
+    got = ctx.join_filter_sort(dev(rkey), dev(rpay), dev(skey), dev(spay), -(2 ** 31), 299)
+    exp = orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 299,
+                               cap=nS * max(1, nR // max(1, min(kr, nR)) + 8), mt=True)
+    check_join(got, exp)
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_join_outside_buckets(ctx, orc, knobs, variant):
+    # Tiny bucket capacities and few buckets: most buckets leave the bucket
+    # kernel -- heavy single keys become cross products, the rest recurse.
+    knobs(variant, 4, 64, 32)
+    rng = np.random.default_rng(5)
+    base = rng.integers(0, 1 << 20, 3000)
+    rkey = np.concatenate([base, np.full(5, 777), np.full(3, -5)]).astype(np.int32)
+    rpay = rng.integers(0, 1000, rkey.size).astype(np.int32)
+    skey = np.concatenate([rng.choice(base, 40000), np.full(3000, 777), np.full(500, -5),
+                           rng.integers(0, 1 << 21, 5000)]).astype(np.int32)
+    rng.shuffle(skey)
+    spay = rng.integers(0, 1000, skey.size).astype(np.int32)
+    got = ctx.join_filter_sort(dev(rkey), dev(rpay), dev(skey), dev(spay), -(2 ** 31), 499)
+    st = ctx.join_stats()
+    assert st["outside_buckets"] > 0
+    exp = orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 499, cap=skey.size * 8, mt=True)
+    check_join(got, exp)
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_join_skewed_mixture(ctx, orc, knobs, variant):
+    knobs(variant)
+    d = datagen.config4_skewed(1 << 17, 1 << 21, seed=3)
+    args = [d[k].numpy() for k in ("rkey", "rpay", "skey", "spay")]
+    got = ctx.join_filter_sort(*[dev(a) for a in args], d["slo"], d["shi"])
+    st = ctx.join_stats()
+    assert st["path"] == {0: st["path"], 1: "radix", 2: "learned"}[variant]
+    check_join(got, orc.join_filter_sort(*args, d["slo"], d["shi"], mt=True))
+
+
+def test_learned_spreads_skew_better_than_radix(ctx, knobs):
+    # On the skewed mixture, radix partitioning leaves most rows in buckets
+    # too big for shared memory; the learned partition function does not.
+    d = datagen.config4_skewed(1 << 18, 1 << 22, seed=4, device="cuda")
+    rows = {}
+    for v in (1, 2):
+        knobs(v)
+        ctx.join_filter_sort(d["rkey"], d["rpay"], d["skey"], d["spay"], d["slo"], d["shi"])
+        rows[v] = ctx.join_stats()["outside_rows"]
+    assert rows[2] * 4 < rows[1]
+
+
+def test_part_model_monotone_and_heavy_keys_isolated(ctx):
+    keys = datagen.skewed_keys(1 << 20, 9, device="cuda")
+    nb = 4096
+    model = ctx.part_learn(keys, nb)
+    u = torch.unique(keys.to(torch.int64) & 0xFFFFFFFF)  # ascending unsigned
+    probe = torch.cat([u, u + 1, u - 1]).clamp(0, 2 ** 32 - 1)
+    probe = torch.unique(probe)
+    probe32 = (probe - (probe >= 2 ** 31).to(torch.int64) * 2 ** 32).to(torch.int32)
+    b = ctx.part_eval(probe32, model).to(torch.int64)
+    assert int(b.min()) >= 0 and int(b.max()) < nb
+    assert bool((b[1:] >= b[:-1]).all()), "bucket function not monotone in the unsigned key"
+    # the most frequent key owns its bucket
+    vals, cnt = torch.unique(keys, return_counts=True)
+    top = vals[cnt.argmax()].reshape(1)
+    tb = int(ctx.part_eval(top, model)[0])
+    same = probe32[(b == tb)]
+    assert same.numel() == 1 and int(same[0]) == int(top[0])
+    # buckets are balanced within a few times the mean on the sample itself
+    hb = torch.bincount(ctx.part_eval(keys, model).to(torch.int64), minlength=nb)
+    heavy_mass = int(cnt.max())
+    assert int(hb.max()) <= max(8 * keys.numel() // nb, heavy_mass)
+
+
+def test_part_radix_eval(ctx):
+    keys = torch.tensor([5, 6, 1029, -1], dtype=torch.int32, device="cuda")
+    b = ctx.part_eval(keys, None, kmin=5, shift=10).cpu().tolist()
+    assert b == [0, 0, 1, (2 ** 32 - 1 - 5) >> 10]
