@@ -20,15 +20,14 @@ constexpr int FT_LB_WARPS = 4;  // warps doing the look-back: 128 predecessors p
 
 // Records (uint2 {x, y}), two per 128-bit load.  ROUNDS loads per thread.
 template <int ROUNDS>
-__global__ void __launch_bounds__(FT_THREADS)
+__global__ void __launch_bounds__(FT_THREADS, 5)
 k_filter_rec(const uint4 *__restrict__ in, long long n, int32_t lo, int32_t hi,
              uint2 *__restrict__ out, long long cap, long long *__restrict__ d_count,
              qg_lookback lb) {
     constexpr int TILE = FT_THREADS * ROUNDS * 2;
     __shared__ uint32_t s_tile, s_epoch, s_excl;
     __shared__ uint32_t s_woff[ROUNDS * FT_WARPS];
-    qg_lb_begin(lb, &s_tile, &s_epoch);
-    const uint32_t tile = s_tile;
+    const uint32_t tile = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long base = (long long)tile * TILE;
     const uint32_t lt = qg_lanemask_lt();
@@ -51,6 +50,7 @@ k_filter_rec(const uint4 *__restrict__ in, long long n, int32_t lo, int32_t hi,
             v[r] = make_uint4(0, 0, 0, 0);
         }
     }
+    qg_lb_begin(lb, &s_tile, &s_epoch);  // epoch read while the loads are in flight
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         long long idx = base + (long long)(r * FT_THREADS + tid) * 2;
@@ -79,21 +79,20 @@ k_filter_rec(const uint4 *__restrict__ in, long long n, int32_t lo, int32_t hi,
             if (pos < cap) out[pos] = make_uint2(v[r].z, v[r].w);
         }
     }
-    qg_lb_end(lb);
+    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
 }
 
 // Columns: int32 key and payload, four rows per 128-bit load.  Output is the
 // int32 pair (row id, payload).
 template <int ROUNDS>
-__global__ void __launch_bounds__(FT_THREADS)
+__global__ void __launch_bounds__(FT_THREADS, 5)
 k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, long long n,
               int32_t lo, int32_t hi, int2 *__restrict__ out, long long cap,
               long long *__restrict__ d_count, qg_lookback lb) {
     constexpr int TILE = FT_THREADS * ROUNDS * 4;
     __shared__ uint32_t s_tile, s_epoch, s_excl;
     __shared__ uint32_t s_woff[ROUNDS * FT_WARPS];
-    qg_lb_begin(lb, &s_tile, &s_epoch);
-    const uint32_t tile = s_tile;
+    const uint32_t tile = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long base = (long long)tile * TILE;
     const uint32_t lt = qg_lanemask_lt();
@@ -116,6 +115,7 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
             pv[r] = make_int4(p[0], p[1], p[2], p[3]);
         }
     }
+    qg_lb_begin(lb, &s_tile, &s_epoch);  // epoch read while the loads are in flight
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         long long idx = base + (long long)(r * FT_THREADS + tid) * 4;
@@ -152,7 +152,7 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
             }
         }
     }
-    qg_lb_end(lb);
+    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
 }
 
 constexpr int REC_ROUNDS = 8;   // 4096 records per tile

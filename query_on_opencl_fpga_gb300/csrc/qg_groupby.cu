@@ -94,7 +94,7 @@ k_group_bounds(const uint4 *__restrict__ in, long long n, int32_t *__restrict__ 
         if ((fl >> (2 * r + 1)) & 1u)
             if (pos < cap) startPos[pos] = (int32_t)(idx + 1);
     }
-    qg_lb_end(lb);
+    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
 }
 
 // ---------------------------------------------------------------------------

@@ -148,10 +148,11 @@ __device__ __forceinline__ uint32_t qg_hash32(uint32_t k) {
 // Status word per tile (64 bit): [63:34] epoch, [33:32] flag, [31:0] value.
 // flag 1 = tile aggregate published, flag 2 = inclusive prefix published.
 // A word whose epoch differs from the running launch's epoch is "not yet
-// written".  Tile ids are handed out by an atomic counter in start order, so
-// every predecessor of a running tile has started and will publish.  The last
-// CTA to finish resets the counters and advances the epoch, so no memset is
-// needed between launches.
+// written".  Tile i is CTA i: the hardware starts CTAs in index order, so
+// every predecessor of a running tile has started and will publish (and a
+// wait that exceeds the poll limit reports QG_ERR_TIMEOUT instead of hanging).
+// The last CTA to finish advances the epoch, so no memset is needed between
+// launches, also when a launch is replayed from a CUDA graph.
 // ---------------------------------------------------------------------------
 struct qg_lookback {
     unsigned long long *status;
@@ -173,7 +174,7 @@ __device__ __forceinline__ unsigned long long qg_lb_word(uint32_t epoch, unsigne
 __device__ __forceinline__ void qg_lb_begin(const qg_lookback &lb, uint32_t *s_tile,
                                             uint32_t *s_epoch) {
     if (threadIdx.x == 0) {
-        *s_tile = atomicAdd(&lb.ctl->tile_ctr, 1u);
+        *s_tile = blockIdx.x;
         *s_epoch = *(volatile uint32_t *)&lb.ctl->epoch;
     }
     __syncthreads();
@@ -335,7 +336,18 @@ __device__ __forceinline__ void qg_tile_offsets_wide(uint32_t *s_woff, const qg_
     __syncthreads();
 }
 
-// Called by all threads at kernel end: the last CTA resets the counters.
+// End of a one-tile-per-CTA look-back kernel: the CTA of the last tile
+// advances the epoch.  When that CTA gets here every other tile has published
+// (its look-back waited for its predecessors, and theirs for theirs), so
+// every CTA of the launch has read the epoch already; no fence or counter.
+__device__ __forceinline__ void qg_lb_finish(const qg_lookback &lb, uint32_t tile,
+                                             uint32_t last_tile, uint32_t epoch) {
+    if (threadIdx.x == 0 && tile == last_tile) *(volatile uint32_t *)&lb.ctl->epoch = epoch + 1u;
+}
+
+// End of a persistent look-back kernel whose CTAs take tiles from
+// ctl->tile_ctr: the last CTA to finish resets the counters and advances
+// the epoch.
 __device__ __forceinline__ void qg_lb_end(const qg_lookback &lb) {
     __syncthreads();
     if (threadIdx.x == 0) {

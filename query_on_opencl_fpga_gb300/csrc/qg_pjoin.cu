@@ -80,7 +80,7 @@ constexpr int SF_WARPS = SF_THREADS / 32;
 constexpr int SF_ROUNDS = 4;  // int4 of keys + int4 of payloads per round: 4096 rows per tile
 constexpr int SF_LB_WARPS = 4;
 
-__global__ void __launch_bounds__(SF_THREADS)
+__global__ void __launch_bounds__(SF_THREADS, 5)
 k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay, long long n,
              int32_t slo, int32_t shi, uint32_t kmin, uint32_t kmax,
              unsigned long long *__restrict__ out, long long *__restrict__ d_count, qg_lookback lb) {
@@ -88,8 +88,7 @@ k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
     __shared__ uint32_t s_tile, s_epoch, s_excl;
     __shared__ uint32_t s_woff[SF_ROUNDS * SF_WARPS];
     __shared__ uint32_t s_tmp[2 * SF_LB_WARPS + 1];
-    qg_lb_begin(lb, &s_tile, &s_epoch);
-    const uint32_t tile = s_tile;
+    const uint32_t tile = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long base = (long long)tile * TILE;
     const uint32_t lt = qg_lanemask_lt();
@@ -108,6 +107,7 @@ k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
             pv[r] = make_int4(p[0], p[1], p[2], p[3]);
         }
     }
+    qg_lb_begin(lb, &s_tile, &s_epoch);  // epoch read while the loads are in flight
     uint32_t fl = 0, lpre[SF_ROUNDS];
 #pragma unroll
     for (int r = 0; r < SF_ROUNDS; r++) {
@@ -133,10 +133,10 @@ k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
     }
     qg_tile_offsets_wide<SF_ROUNDS * SF_WARPS, SF_LB_WARPS>(s_woff, lb, tile, s_epoch, &s_excl, s_tmp,
                                                            d_count, gridDim.x - 1);
-    const long long excl = s_excl;
+    const uint32_t excl = s_excl;  // n < 2^30 rows on this path
 #pragma unroll
     for (int r = 0; r < SF_ROUNDS; r++) {
-        long long pos = excl + s_woff[r * SF_WARPS + warp] + lpre[r];
+        uint32_t pos = excl + s_woff[r * SF_WARPS + warp] + lpre[r];
         const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
         const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
 #pragma unroll
@@ -147,7 +147,7 @@ k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
                 pos++;
             }
     }
-    qg_lb_end(lb);
+    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
 }
 
 // ---------------------------------------------------------------------------
@@ -575,7 +575,7 @@ k_pj_join(PbArgs a, qg_lookback lb) {
             }
         }
     }
-    qg_lb_end(lb);
+    qg_lb_finish(lb, b, gridDim.x - 1, S.epoch);
 }
 
 // ---------------------------------------------------------------------------

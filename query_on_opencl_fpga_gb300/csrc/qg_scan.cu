@@ -85,7 +85,7 @@ k_scan_excl(const int32_t *in, int32_t *out, long long n, qg_lookback lb) {
                 if (idx + j < n) out[idx + j] = (int32_t)o[j];
         }
     }
-    qg_lb_end(lb);
+    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
 }
 
 }  // namespace

@@ -86,10 +86,11 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
     extern __shared__ __align__(16) unsigned char rs_raw[];
     RsSmem<KV3> &S = *reinterpret_cast<RsSmem<KV3> *>(rs_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) S.tile = atomicAdd(&ctl->tile_ctr, 1u);
     for (int i = tid; i < RS_WARPS * QG_RADIX; i += RS_THREADS) (&S.whist[0][0])[i] = 0;
     __syncthreads();
-    const uint32_t tile = S.tile;
+    // Tile i is CTA i (started in index order); the status words are cleared
+    // before every pass, so nothing has to be reset at the end.
+    const uint32_t tile = blockIdx.x;
     const long long base = (long long)tile * RS_TILE;
     const long long wbase = base + (long long)warp * 32 * RS_ITEMS;
     const uint32_t lt = qg_lanemask_lt();
@@ -230,17 +231,6 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
             dst.b[g] = (uint32_t)(v >> 32);
         } else {
             dst.rec[g] = v;
-        }
-    }
-    __syncthreads();
-    if (tid == 0) {
-        __threadfence();
-        uint32_t done = atomicAdd(&ctl->done_ctr, 1u);
-        if (done == gridDim.x - 1) {
-            ctl->tile_ctr = 0;
-            ctl->done_ctr = 0;
-            ctl->epoch = (ctl->epoch + 1) & 0x3fffffffu;
-            __threadfence();
         }
     }
 }
