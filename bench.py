@@ -434,6 +434,13 @@ def run_only(args):
         j = datagen.config2_join(nr, n, seed=0, device="cuda")
         fn = lambda: ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"],  # noqa: E731
                                           j["shi"], cap=int(n * 0.26) + 1024)
+    elif args.only == "skew":
+        n = rows or (1 << 28)
+        nr = args.rows2 or min(1 << 25, max(n // 8, 1))
+        j = datagen.config4_skewed(nr, n, seed=0, device="cuda")
+        ctx.join_set_knobs(max(args.variant, 0))
+        fn = lambda: ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"],  # noqa: E731
+                                          j["shi"], cap=int(n * 0.3) + 1024)
     elif args.only == "sort":
         n = rows or (1 << 26)
         from query_on_opencl_fpga_gb300.datagen import records, uniform_i32
@@ -448,6 +455,8 @@ def run_only(args):
         ctx.check(ctx.lib.qg_groupby_set_knobs(args.variant, 13, 0, 0), "qg_groupby_set_knobs")
     ms, kern, launches = timed(ctx, fn, args.steps, args.warmup, 1, stream)
     extra = {"groupby_stats": ctx.groupby_stats()} if args.only in ("groupby", "fused") else {}
+    if args.only in ("join", "skew"):
+        extra = {"join_stats": ctx.join_stats()}
     print(json.dumps({"only": args.only, "rows": n, "variant": args.variant, "ms_per_op": ms,
                       "rows_per_s": n / (ms * 1e-3),
                       "kernels_ms_per_op": {k: v[1] / args.steps for k, v in kern.items()},
@@ -457,7 +466,7 @@ def run_only(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default=None, help="groupby|fused|filter|join|sort: one operator alone")
+    ap.add_argument("--only", default=None, help="groupby|fused|filter|join|skew|sort: one operator alone")
     ap.add_argument("--rows", type=int, default=0, help="row count for --only (default: the config size)")
     ap.add_argument("--variant", type=int, default=-1, help="column filter kernel variant for --only filter")
     ap.add_argument("--rows2", type=int, default=0, help="build-side rows for --only join")

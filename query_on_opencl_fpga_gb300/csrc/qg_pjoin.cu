@@ -151,29 +151,57 @@ k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
 }
 
 // ---------------------------------------------------------------------------
-// 3. bucket histogram (shared-memory privatised), CDF sample and fit
+// 3. digit histograms of the bucket id, bucket bounds, CDF sample and fit
 // ---------------------------------------------------------------------------
-constexpr int PJ_MAX_BUCKETS = 1 << 15;
+constexpr int PJ_MAX_BUCKETS = 1 << 16;  // two 8-bit partition passes
 
-__global__ void __launch_bounds__(1024)
-k_pj_hist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn pf, uint32_t nb,
-          uint32_t *__restrict__ counts, qg_control *ctl) {
-    extern __shared__ uint32_t h[];
-    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) h[i] = 0;
+// Histograms of the two 8-bit digits of each row's bucket (shared-memory
+// privatised), for the partition passes' digit bases.
+__global__ void __launch_bounds__(256)
+k_pj_dhist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn pf, uint32_t nb,
+           uint32_t *__restrict__ hist, qg_control *ctl) {
+    __shared__ uint32_t h[2][256];
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) (&h[0][0])[i] = 0;
     __syncthreads();
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t k = (uint32_t)(__ldg(rec + i) >> 32);
-        const uint32_t b = qg_part_bucket(pf, k);
+        const uint32_t b = qg_part_bucket(pf, (uint32_t)(__ldg(rec + i) >> 32));
         if (b >= nb) {  // a key outside the partition function's domain
             qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_HIST);
             continue;
         }
-        atomicAdd(&h[b], 1u);
+        atomicAdd(&h[0][b & 255u], 1u);
+        atomicAdd(&h[1][b >> 8], 1u);
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
-        if (h[i]) atomicAdd(&counts[i], h[i]);
+    for (int i = threadIdx.x; i < 512; i += blockDim.x)
+        if ((&h[0][0])[i]) atomicAdd(&hist[i], (&h[0][0])[i]);
+}
+
+// After partitioning (rows in bucket order): beg[b] = first row whose bucket
+// is >= b, for b in [0, nb]; one thread per bucket, binary search.
+__global__ void k_pj_bounds(const unsigned long long *__restrict__ rec, long long n, qg_part_fn pf,
+                            uint32_t nb, uint32_t *__restrict__ beg) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > nb) return;
+    long long lo = 0, hi = n;
+    while (lo < hi) {
+        const long long mid = (lo + hi) >> 1;
+        if (qg_part_bucket(pf, (uint32_t)(__ldg(rec + mid) >> 32)) < b) lo = mid + 1;
+        else hi = mid;
+    }
+    beg[b] = (uint32_t)lo;
+}
+
+// Bucket counts of the key sample under a partition function (global atomics;
+// the sample has at most 2^20 keys).
+__global__ void k_pj_smp_hist(const unsigned long long *__restrict__ smp, long long m, qg_part_fn pf,
+                              uint32_t nb, uint32_t *__restrict__ counts) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+         i += (long long)gridDim.x * blockDim.x) {
+        const uint32_t b = qg_part_bucket(pf, (uint32_t)(__ldg(smp + i) >> 32));
+        if (b < nb) atomicAdd(&counts[b], 1u);
+    }
 }
 
 // Sample m keys spread evenly over both inputs (proportionally to their
@@ -667,64 +695,95 @@ qg_status qg_join_hash_sort(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpa
 
 namespace {
 
-int g_pj_variant = 0;  // 0 auto (radix, learned when radix leaves big buckets), 1 radix, 2 learned, 3 hash join + sort
-int g_pj_blog2 = 0;    // 0: bucket count from the input size
+int g_pj_variant = 0;  // 0 auto (radix; learned when a key sample shows that it spreads the rows better), 1 radix, 2 learned, 3 hash join + sort
+int g_pj_blog2 = 0;    // 0: fine bucket count from the input size
 uint32_t g_pj_smax = PB_SMAX, g_pj_rmax = PB_RMAX;
-constexpr long long PB_TARGET = 2560;     // R + S' rows per bucket aimed at
-constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit the learned model
+constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit (and judge) the learned model
+constexpr int PJ_MAX_DEPTH = 6;
 
 struct PjLevel {
     PjRange *range;
-    uint32_t *cnt;  // [2 * nb]: R counts, then S' counts
-    uint32_t *rbeg, *sbeg, *big, *mm;
-    unsigned long long *bigcnt, *off, *total, *smp, *smp2;
-    qg_cdf_model *model;
+    uint32_t *dh;          // [side R, S'][digit 0, 1][256]
+    uint32_t *rbk, *sbk;   // [nb + 1] first row of each fine bucket
+    uint32_t *gr, *gs;     // [nb + 1] first row of each join group
+    uint32_t *big, *mm;    // [nb] group handled outside the bucket kernel; [2 nb] key ranges
+    uint32_t *scnt;        // [2 nb] sample counts under radix, learned
+    unsigned long long *bigcnt, *off, *total;
     PjCross *cross;
     PjPlace *place;
+    qg_cdf_model *model;             // learned model (top level only)
+    unsigned long long *smp, *smp2;  // key sample (top level only)
 };
 
-size_t pj_level_bytes(uint32_t nb) {
+size_t pj_level_bytes(uint32_t nb, bool learned) {
     size_t b = 0;
     auto add = [&](size_t x) { b += qg_align_up(x, 256); };
     add(sizeof(PjRange));
-    add((size_t)2 * nb * 4);
-    add((size_t)(nb + 1) * 4);
-    add((size_t)(nb + 1) * 4);
+    add(4 * 256 * 4);
+    for (int i = 0; i < 4; i++) add((size_t)(nb + 1) * 4);
     add((size_t)nb * 4);
+    add((size_t)2 * nb * 4);
     add((size_t)2 * nb * 4);
     add((size_t)nb * 8);
     add((size_t)nb * 8);
     add(8);
-    add((size_t)CDF_SAMPLE * 8);
-    add((size_t)CDF_SAMPLE * 8);
-    add(sizeof(qg_cdf_model));
     add((size_t)nb * sizeof(PjCross));
     add((size_t)nb * sizeof(PjPlace));
+    if (learned) {
+        add(sizeof(qg_cdf_model));
+        add((size_t)CDF_SAMPLE * 8);
+        add((size_t)CDF_SAMPLE * 8);
+    }
     return b;
 }
 
-void pj_level_carve(char *p, uint32_t nb, PjLevel *L) {
+void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     auto take = [&](size_t x) { char *q = p; p += qg_align_up(x, 256); return q; };
     L->range = (PjRange *)take(sizeof(PjRange));
-    L->cnt = (uint32_t *)take((size_t)2 * nb * 4);
-    L->rbeg = (uint32_t *)take((size_t)(nb + 1) * 4);
-    L->sbeg = (uint32_t *)take((size_t)(nb + 1) * 4);
+    L->dh = (uint32_t *)take(4 * 256 * 4);
+    L->rbk = (uint32_t *)take((size_t)(nb + 1) * 4);
+    L->sbk = (uint32_t *)take((size_t)(nb + 1) * 4);
+    L->gr = (uint32_t *)take((size_t)(nb + 1) * 4);
+    L->gs = (uint32_t *)take((size_t)(nb + 1) * 4);
     L->big = (uint32_t *)take((size_t)nb * 4);
     L->mm = (uint32_t *)take((size_t)2 * nb * 4);
+    L->scnt = (uint32_t *)take((size_t)2 * nb * 4);
     L->bigcnt = (unsigned long long *)take((size_t)nb * 8);
     L->off = (unsigned long long *)take((size_t)nb * 8);
     L->total = (unsigned long long *)take(8);
-    L->smp = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
-    L->smp2 = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
-    L->model = (qg_cdf_model *)take(sizeof(qg_cdf_model));
     L->cross = (PjCross *)take((size_t)nb * sizeof(PjCross));
     L->place = (PjPlace *)take((size_t)nb * sizeof(PjPlace));
+    L->model = nullptr;
+    L->smp = L->smp2 = nullptr;
+    if (learned) {
+        L->model = (qg_cdf_model *)take(sizeof(qg_cdf_model));
+        L->smp = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
+        L->smp2 = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
+    }
+}
+
+// Grow-only per-depth device buffers of the context.
+qg_status pj_pool_get(qg_ctx *ctx, char **slot, size_t *slot_bytes, size_t bytes, char **out) {
+    bytes = qg_align_up(bytes ? bytes : 256, 256);
+    if (bytes > *slot_bytes) {
+        QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+        if (*slot) cudaFree(*slot);
+        *slot = nullptr;
+        *slot_bytes = 0;
+        if (cudaMalloc((void **)slot, bytes + bytes / 4) != cudaSuccess) {
+            cudaGetLastError();
+            *slot = nullptr;
+            return QG_ERR_OOM;
+        }
+        *slot_bytes = bytes + bytes / 4;
+    }
+    *out = *slot;
+    return QG_OK;
 }
 
 qg_status pj_attrs(qg_ctx *ctx) {
     static bool done = false;
     if (!done) {
-        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, PJ_MAX_BUCKETS * 4), "attr hist");
         QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PbSmem)), "attr join");
         done = true;
     }
@@ -739,42 +798,26 @@ int pj_grid(qg_ctx *ctx, long long work, int per_block, int per_sm) {
     return (int)b;
 }
 
-// Bucket counts of both sides into h[0 .. 2 nb) (R then S'); synchronises.
-qg_status pj_hist(qg_ctx *ctx, const qg_part_fn &pf, uint32_t nb, const unsigned long long *r,
-                  long long nR, const unsigned long long *s, long long nS, uint32_t *d_cnt,
-                  std::vector<uint32_t> &h) {
-    QG_TRY_CUDA(ctx, cudaMemsetAsync(d_cnt, 0, (size_t)2 * nb * 4, ctx->stream), "memset counts");
-    const size_t smem = (size_t)nb * 4;
+// Digit histograms of both sides' bucket ids into h[0 .. 1024) (synchronises).
+qg_status pj_dhist(qg_ctx *ctx, const PjLevel &L, const qg_part_fn &pf, uint32_t nb,
+                   const unsigned long long *r, long long nR, const unsigned long long *s, long long nS,
+                   uint32_t *h) {
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 4 * 256 * 4, ctx->stream), "memset dhist");
     qg_pre_launch(ctx);
-    k_pj_hist<<<pj_grid(ctx, nR, 1024, 1), 1024, smem, ctx->stream>>>(r, nR, pf, nb, d_cnt, ctx->ctl);
-    QG_TRY(qg_check_launch(ctx, "k_pj_hist"));
+    k_pj_dhist<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, pf, nb, L.dh, ctx->ctl);
+    QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     qg_pre_launch(ctx);
-    k_pj_hist<<<pj_grid(ctx, nS, 1024, 1), 1024, smem, ctx->stream>>>(s, nS, pf, nb, d_cnt + nb, ctx->ctl);
-    QG_TRY(qg_check_launch(ctx, "k_pj_hist"));
-    h.resize((size_t)2 * nb);
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), d_cnt, (size_t)2 * nb * 4, cudaMemcpyDeviceToHost, ctx->stream), "counts d2h");
+    k_pj_dhist<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl);
+    QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     return qg_collect_error(ctx);
 }
 
-// Rows in buckets that do not fit the bucket kernel.
-long long pj_oversize_rows(const std::vector<uint32_t> &h, uint32_t nb, uint32_t *nbig) {
-    long long rows = 0;
-    uint32_t c = 0;
-    for (uint32_t b = 0; b < nb; b++) {
-        const uint32_t rc = h[b], sc = h[nb + b];
-        if (rc && sc && (rc > g_pj_rmax || sc > g_pj_smax)) {
-            rows += (long long)rc + sc;
-            c++;
-        }
-    }
-    if (nbig) *nbig = c;
-    return rows;
-}
-
-// Fit the learned model on a sample of both sides' keys (records).
+// Fit the learned model on a sample of both sides' keys (records); the
+// sorted sample stays in L.smp (m keys).
 qg_status pj_train(qg_ctx *ctx, const PjLevel &L, uint32_t nb, const unsigned long long *r, long long nR,
-                   const unsigned long long *s, long long nS) {
+                   const unsigned long long *s, long long nS, long long *m_out) {
     const long long n = nR + nS;
     const long long m = n < CDF_SAMPLE ? n : CDF_SAMPLE;
     long long mR = nR ? (m * nR) / n : 0;
@@ -788,52 +831,43 @@ qg_status pj_train(qg_ctx *ctx, const PjLevel &L, uint32_t nb, const unsigned lo
     if (hthr < 2) hthr = 2;
     qg_pre_launch(ctx);
     k_cdf_fit<<<1, FIT_THREADS, 0, ctx->stream>>>(L.smp, m, nb, hthr, L.model);
-    return qg_check_launch(ctx, "k_cdf_fit");
+    QG_TRY(qg_check_launch(ctx, "k_cdf_fit"));
+    *m_out = m;
+    return QG_OK;
 }
 
-struct PjTemp {
-    uint32_t *k = nullptr, *a = nullptr, *c = nullptr;
-    void release() {
-        if (k) cudaFree(k);
-        if (a) cudaFree(a);
-        if (c) cudaFree(c);
-        k = a = c = nullptr;
-    }
-};
-
-qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
-                  unsigned long long *s, unsigned long long *ssp, long long nS, uint32_t kmin,
-                  uint32_t kmax, int variant, uint32_t *ok, uint32_t *oa, uint32_t *ob, long long cap,
-                  long long *M_out, int depth, char *lvl_mem);
-
-// Join one oversize multi-key bucket into freshly allocated columns.
-qg_status pj_sub(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
-                 unsigned long long *s, unsigned long long *ssp, long long nS, uint32_t kmin,
-                 uint32_t kmax, int variant, int depth, PjTemp *t, long long *M) {
-    long long capt = nS + nR + 1024;
-    for (int attempt = 0; attempt < 2; attempt++) {
-        t->release();
-        if (cudaMalloc((void **)&t->k, (size_t)capt * 4) != cudaSuccess ||
-            cudaMalloc((void **)&t->a, (size_t)capt * 4) != cudaSuccess ||
-            cudaMalloc((void **)&t->c, (size_t)capt * 4) != cudaSuccess) {
-            cudaGetLastError();
-            t->release();
-            return QG_ERR_OOM;
+// Rows (estimated from the sample) that would land in buckets larger than the
+// bucket kernel takes, for each function: the judge between radix and learned.
+qg_status pj_judge(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot, const qg_part_fn &radix,
+                   uint32_t nb_radix, const qg_part_fn &learned, uint32_t nb, double *over_radix,
+                   double *over_learned) {
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(L.scnt, 0, (size_t)2 * nb * 4, ctx->stream), "memset scnt");
+    qg_pre_launch(ctx);
+    k_pj_smp_hist<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(L.smp, m, radix, nb_radix, L.scnt);
+    QG_TRY(qg_check_launch(ctx, "k_pj_smp_hist"));
+    qg_pre_launch(ctx);
+    k_pj_smp_hist<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(L.smp, m, learned, nb, L.scnt + nb);
+    QG_TRY(qg_check_launch(ctx, "k_pj_smp_hist"));
+    std::vector<uint32_t> c((size_t)2 * nb);
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(c.data(), L.scnt, c.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "scnt d2h");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    const double scale = (double)ntot / (double)m;
+    const double lim = 0.8 * (double)(g_pj_smax + g_pj_rmax);
+    double o[2] = {0, 0};
+    for (int f = 0; f < 2; f++)
+        for (uint32_t b = 0; b < (f ? nb : nb_radix); b++) {
+            const double est = c[(size_t)f * nb + b] * scale;
+            if (est > lim) o[f] += est;
         }
-        QG_TRY(pj_core(ctx, r, rsp, nR, s, ssp, nS, kmin, kmax, variant, t->k, t->a, t->c, capt, M,
-                       depth, nullptr));
-        if (*M <= capt) return QG_OK;
-        capt = *M;
-    }
-    return QG_ERR_CAPACITY;
+    *over_radix = o[0];
+    *over_learned = o[1];
+    return QG_OK;
 }
 
-struct PjLevelMem {
-    char *p = nullptr;
-    bool own = false;
-    ~PjLevelMem() {
-        if (own && p) cudaFree(p);
-    }
+struct PjTempOut {
+    uint32_t *k, *a, *c;
+    long long cap;
+    bool own;  // allocated for this group alone (its output outgrew the slice)
 };
 
 qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
@@ -842,119 +876,133 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
                   long long *M_out, int depth, char *lvl_mem) {
     *M_out = 0;
     if (nR == 0 || nS == 0) return QG_OK;
-    if (depth > 6) return QG_ERR_UNSUPPORTED;
+    if (depth > PJ_MAX_DEPTH) return QG_ERR_UNSUPPORTED;
     QG_TRY(pj_attrs(ctx));
     const long long ntot = nR + nS;
-    // Buckets: about PB_TARGET rows each, and room for twice the rows of each
-    // side at the bucket kernel's capacity.  A nested level splits its key
-    // range at least 256 ways, so that every level narrows it and the
-    // recursion ends in single-key buckets.
+    // Fine buckets of about a quarter of the bucket kernel's capacity (join
+    // groups pack several of them); a nested level splits its key range at
+    // least 256 ways, so every level narrows it and the recursion ends in
+    // single-key buckets.
     uint32_t nb = depth > 0 ? 256u : 1u;
-    if (g_pj_blog2 > 0 && depth == 0) nb = 1u << g_pj_blog2;
-    else
+    if (g_pj_blog2 > 0 && depth == 0) {
+        nb = 1u << g_pj_blog2;
+    } else {
         while (nb < (uint32_t)PJ_MAX_BUCKETS &&
-               ((long long)nb * PB_TARGET < ntot || (long long)nb * g_pj_smax < 2 * nS ||
-                (long long)nb * g_pj_rmax < 2 * nR))
+               ((long long)nb * 1024 < ntot || (long long)nb * (g_pj_smax / 4) < nS ||
+                (long long)nb * (g_pj_rmax / 4) < nR))
             nb <<= 1;
+    }
     int lb2 = 0;
     while ((1u << lb2) < nb) lb2++;
     const uint32_t range = kmax - kmin;
     const int bits = range ? 32 - __builtin_clz(range) : 0;
     const int shift = bits > lb2 ? bits - lb2 : 0;
     const uint32_t nb_radix = (uint32_t)(((unsigned long long)range >> shift) + 1);
+    const bool may_learn = depth == 0 && variant != 1;
 
-    PjLevelMem lm;
-    lm.p = lvl_mem;
-    if (!lm.p) {
-        if (cudaMalloc((void **)&lm.p, pj_level_bytes(nb)) != cudaSuccess) {
-            cudaGetLastError();
-            return QG_ERR_OOM;
-        }
-        lm.own = true;
-    }
+    char *mem = lvl_mem;
+    if (!mem) QG_TRY(pj_pool_get(ctx, &ctx->pj_pool[depth], &ctx->pj_pool_bytes[depth],
+                                 pj_level_bytes(nb, may_learn), &mem));
     PjLevel L;
-    pj_level_carve(lm.p, nb, &L);
+    pj_level_carve(mem, nb, may_learn, &L);
     const qg_part_fn radix{0, kmin, shift, nullptr};
     const qg_part_fn learned{1, 0u, 0, L.model};
 
-    std::vector<uint32_t> h;
-    QG_TRY(pj_hist(ctx, radix, nb_radix, r, nR, s, nS, L.cnt, h));
-    uint32_t nbig = 0;
-    const long long over_radix = pj_oversize_rows(h, nb_radix, &nbig);
-    bool use_learned = variant == 2;
+    // radix digit histograms; a lopsided high digit means skew, and then a
+    // key sample judges whether the learned function spreads the rows better
+    uint32_t h[1024];
+    QG_TRY(pj_dhist(ctx, L, radix, nb_radix, r, nR, s, nS, h));
+    bool use_learned = may_learn && variant == 2;
     bool judged = false;
-    if (variant == 0 && depth == 0 && over_radix * 50 > ntot) use_learned = judged = true;
-    uint32_t nbu = nb_radix;
-    if (use_learned) {
-        QG_TRY(pj_train(ctx, L, nb, r, nR, s, nS));
-        std::vector<uint32_t> h2;
-        QG_TRY(pj_hist(ctx, learned, nb, r, nR, s, nS, L.cnt, h2));
-        uint32_t nbig2 = 0;
-        const long long over_learned = pj_oversize_rows(h2, nb, &nbig2);
-        // Radix partitioning judges the learned model: keep radix when the
-        // model does not leave fewer rows in oversize buckets.
-        if (judged && over_learned >= over_radix) {
-            use_learned = false;
-        } else {
-            h.swap(h2);
-            nbu = nb;
-            nbig = nbig2;
-        }
+    if (may_learn && variant == 0 && ntot >= (1 << 16)) {
+        const uint32_t *hs = h + 512 + (nb_radix > 256 ? 256 : 0);
+        const uint32_t nbin = nb_radix > 256 ? ((nb_radix - 1) >> 8) + 1 : nb_radix;
+        uint32_t mx = 0;
+        for (uint32_t i = 0; i < nbin; i++) mx = hs[i] > mx ? hs[i] : mx;
+        if ((double)mx > 4.0 * (double)nS / (double)nbin) judged = true;
     }
+    long long m = 0;
+    if (use_learned || judged) QG_TRY(pj_train(ctx, L, nb, r, nR, s, nS, &m));
+    if (judged) {
+        double orad = 0, olrn = 0;
+        QG_TRY(pj_judge(ctx, L, m, ntot, radix, nb_radix, learned, nb, &orad, &olrn));
+        use_learned = olrn < 0.5 * orad;
+    }
+    if (use_learned) QG_TRY(pj_dhist(ctx, L, learned, nb, r, nR, s, nS, h));
     const qg_part_fn &pf = use_learned ? learned : radix;
+    const uint32_t nbu = use_learned ? nb : nb_radix;
 
-    // bucket offsets and digit bases of the partition passes
-    std::vector<uint32_t> rbeg(nbu + 1), sbeg(nbu + 1);
-    uint32_t hr[4 * QG_RADIX] = {0}, hs[4 * QG_RADIX] = {0};
-    int bb = 0;
-    while ((1u << bb) < nbu) bb++;
-    const int npos = (bb + 7) / 8;
-    {
-        uint32_t rr = 0, ss = 0;
-        for (uint32_t b = 0; b < nbu; b++) {
-            rbeg[b] = rr;
-            sbeg[b] = ss;
-            rr += h[b];
-            ss += h[nbu + b];
-            for (int p = 0; p < npos; p++) {
-                hr[p * QG_RADIX + ((b >> (8 * p)) & 255u)] += h[b];
-                hs[p * QG_RADIX + ((b >> (8 * p)) & 255u)] += h[nbu + b];
-            }
-        }
-        rbeg[nbu] = rr;
-        sbeg[nbu] = ss;
-    }
-    // partition both sides by bucket
+    // partition both sides by bucket (one or two stable 8-bit passes)
+    const int npos = nbu > 256 ? 2 : (nbu > 1 ? 1 : 0);
     if (npos > 0) {
+        uint32_t hist[4 * QG_RADIX] = {0}, bases[4 * QG_RADIX];
         int passes[4], np;
-        uint32_t bases[4 * QG_RADIX];
         bool in_b = false;
-        np = qg_sort_plan(hr, npos, nR, passes, bases);
+        memcpy(hist, h, 512 * 4);
+        np = qg_sort_plan(hist, npos, nR, passes, bases);
         QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{r, nullptr, nullptr, nullptr},
-                                  qg_sort_bufs{rsp, nullptr, nullptr, nullptr}, nR, pf, passes, np, bases,
-                                  &in_b));
+                                  qg_sort_bufs{rsp, nullptr, nullptr, nullptr}, nR, pf, passes, np, bases, &in_b));
         if (in_b) std::swap(r, rsp);
-        np = qg_sort_plan(hs, npos, nS, passes, bases);
+        memcpy(hist, h + 512, 512 * 4);
+        np = qg_sort_plan(hist, npos, nS, passes, bases);
         QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{s, nullptr, nullptr, nullptr},
-                                  qg_sort_bufs{ssp, nullptr, nullptr, nullptr}, nS, pf, passes, np, bases,
-                                  &in_b));
+                                  qg_sort_bufs{ssp, nullptr, nullptr, nullptr}, nS, pf, passes, np, bases, &in_b));
         if (in_b) std::swap(s, ssp);
     }
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.rbeg, rbeg.data(), (size_t)(nbu + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "rbeg h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.sbeg, sbeg.data(), (size_t)(nbu + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "sbeg h2d");
+    // fine bucket bounds
+    qg_pre_launch(ctx);
+    k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(r, nR, pf, nbu, L.rbk);
+    QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
+    qg_pre_launch(ctx);
+    k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(s, nS, pf, nbu, L.sbk);
+    QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
+    std::vector<uint32_t> rbk(nbu + 1), sbk(nbu + 1);
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(rbk.data(), L.rbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "rbk d2h");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(sbk.data(), L.sbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "sbk d2h");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
 
-    // buckets handled outside the bucket kernel
-    std::vector<uint32_t> big(nbu, 0);
-    std::vector<unsigned long long> bigcnt(nbu, 0);
-    std::vector<PjCross> over, cross;
-    std::vector<PjPlace> place;
-    std::vector<PjTemp> temps;
-    int depth_max = depth;
-    for (uint32_t b = 0; b < nbu; b++) {
-        const uint32_t rc = h[b], sc = h[nbu + b];
-        if (rc && sc && (rc > g_pj_rmax || sc > g_pj_smax)) over.push_back(PjCross{b, rbeg[b], rc, sbeg[b], sc});
+    // Pack consecutive fine buckets into join groups up to the bucket
+    // kernel's capacity.  A bucket above it is a group of its own, handled
+    // outside the kernel when both sides have rows (flag 1) and skipped when
+    // one side is empty (flag 2).
+    std::vector<uint32_t> gr{0}, gs{0}, big;
+    std::vector<PjCross> over;
+    {
+        uint32_t cr = 0, cs = 0;
+        bool open = false;
+        auto close = [&](uint32_t b) {
+            if (open) { gr.push_back(rbk[b]); gs.push_back(sbk[b]); big.push_back(0); }
+            open = false;
+            cr = cs = 0;
+        };
+        for (uint32_t b = 0; b < nbu; b++) {
+            const uint32_t rc = rbk[b + 1] - rbk[b], sc = sbk[b + 1] - sbk[b];
+            if (rc > g_pj_rmax || sc > g_pj_smax) {
+                close(b);
+                gr.push_back(rbk[b + 1]);
+                gs.push_back(sbk[b + 1]);
+                const bool joinable = rc && sc;
+                big.push_back(joinable ? 1u : 2u);
+                if (joinable) over.push_back(PjCross{(uint32_t)(big.size() - 1), rbk[b], rc, sbk[b], sc});
+                continue;
+            }
+            if (cr + rc > g_pj_rmax || cs + sc > g_pj_smax) close(b);
+            cr += rc;
+            cs += sc;
+            open = true;
+        }
+        close(nbu);
     }
-    qg_status st = QG_OK;
+    const uint32_t G = (uint32_t)big.size();
+    std::vector<unsigned long long> bigcnt(G, 0);
+    std::vector<uint32_t> bigflag(G, 0);
+    for (uint32_t g = 0; g < G; g++) bigflag[g] = big[g] ? 1u : 0u;
+
+    // outside groups: single-key cross products, the rest recursively
+    std::vector<PjCross> cross;
+    std::vector<PjPlace> place;
+    std::vector<PjTempOut> temps;
+    int depth_max = depth;
     if (!over.empty()) {
         std::vector<uint32_t> mm(2 * over.size());
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, over.data(), over.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "list h2d");
@@ -963,40 +1011,65 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
         QG_TRY(qg_check_launch(ctx, "k_pj_minmax"));
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(mm.data(), L.mm, mm.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "mm d2h");
         QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-        temps.reserve(over.size());
+        // one slice of the per-depth output pool for each recursive group
+        size_t slice_rows = 0;
+        for (size_t i = 0; i < over.size(); i++)
+            if (mm[2 * i] != mm[2 * i + 1]) slice_rows += (size_t)over[i].sn + over[i].rn + 1024;
+        char *tmp = nullptr;
+        if (slice_rows)
+            QG_TRY(pj_pool_get(ctx, &ctx->pj_tmp[depth], &ctx->pj_tmp_bytes[depth], slice_rows * 12, &tmp));
+        size_t used = 0;
+        qg_status st = QG_OK;
         for (size_t i = 0; i < over.size() && st == QG_OK; i++) {
             const PjCross &e = over[i];
-            big[e.b] = 1;
             if (mm[2 * i] == mm[2 * i + 1]) {
                 bigcnt[e.b] = (unsigned long long)e.rn * e.sn;
                 cross.push_back(e);
-            } else {
-                temps.emplace_back();
-                long long Mb = 0;
-                const int sub_variant = variant == 2 ? 2 : 1;
-                st = pj_sub(ctx, r + e.rb, rsp + e.rb, e.rn, s + e.sb, ssp + e.sb, e.sn, mm[2 * i],
-                            mm[2 * i + 1], sub_variant, depth + 1, &temps.back(), &Mb);
-                bigcnt[e.b] = (unsigned long long)Mb;
-                place.push_back(PjPlace{e.b, temps.back().k, temps.back().a, temps.back().c,
-                                        (unsigned long long)Mb});
-                if (ctx->pj_stats[4] > (uint32_t)depth_max) depth_max = (int)ctx->pj_stats[4];
+                continue;
             }
+            const long long capt = (long long)e.sn + e.rn + 1024;
+            PjTempOut t{(uint32_t *)(tmp + used * 4), (uint32_t *)(tmp + (slice_rows + used) * 4),
+                        (uint32_t *)(tmp + (2 * slice_rows + used) * 4), capt, false};
+            used += (size_t)capt;
+            long long Mb = 0;
+            st = pj_core(ctx, r + e.rb, rsp + e.rb, e.rn, s + e.sb, ssp + e.sb, e.sn, mm[2 * i], mm[2 * i + 1], 1,
+                         t.k, t.a, t.c, t.cap, &Mb, depth + 1, nullptr);
+            if (st == QG_OK && Mb > t.cap) {  // more matches than rows: buffers of its own
+                PjTempOut u{nullptr, nullptr, nullptr, Mb, true};
+                if (cudaMalloc((void **)&u.k, (size_t)Mb * 4) != cudaSuccess ||
+                    cudaMalloc((void **)&u.a, (size_t)Mb * 4) != cudaSuccess ||
+                    cudaMalloc((void **)&u.c, (size_t)Mb * 4) != cudaSuccess) {
+                    cudaGetLastError();
+                    if (u.k) cudaFree(u.k);
+                    if (u.a) cudaFree(u.a);
+                    st = QG_ERR_OOM;
+                    break;
+                }
+                temps.push_back(u);
+                t = u;
+                st = pj_core(ctx, r + e.rb, rsp + e.rb, e.rn, s + e.sb, ssp + e.sb, e.sn, mm[2 * i], mm[2 * i + 1],
+                             1, t.k, t.a, t.c, t.cap, &Mb, depth + 1, nullptr);
+            }
+            if ((int)ctx->pj_stats[4] > depth_max) depth_max = (int)ctx->pj_stats[4];
+            bigcnt[e.b] = (unsigned long long)Mb;
+            place.push_back(PjPlace{e.b, t.k, t.a, t.c, (unsigned long long)Mb});
+        }
+        if (st != QG_OK) {
+            for (auto &t : temps) { cudaFree(t.k); cudaFree(t.a); cudaFree(t.c); }
+            return st;
         }
     }
-    if (st != QG_OK) {
-        for (auto &t : temps) t.release();
-        return st;
-    }
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.big, big.data(), (size_t)nbu * 4, cudaMemcpyHostToDevice, ctx->stream), "big h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.bigcnt, bigcnt.data(), (size_t)nbu * 8, cudaMemcpyHostToDevice, ctx->stream), "bigcnt h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gr, gr.data(), (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gr h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gs, gs.data(), (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gs h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.big, bigflag.data(), (size_t)G * 4, cudaMemcpyHostToDevice, ctx->stream), "big h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.bigcnt, bigcnt.data(), (size_t)G * 8, cudaMemcpyHostToDevice, ctx->stream), "bigcnt h2d");
 
-    // the bucket kernel (look-back status from the scratch arena, taken after
-    // the nested calls, which use the arena themselves)
+    // the bucket kernel over the join groups
     qg_lookback lb;
-    QG_TRY(qg_lb_make(ctx, nbu, QG_SITE_JOIN_PROBE, &lb));
-    PbArgs args{r, s, L.rbeg, L.sbeg, L.big, L.bigcnt, L.off, L.total, ok, oa, ob, cap};
+    QG_TRY(qg_lb_make(ctx, G, QG_SITE_JOIN_PROBE, &lb));
+    PbArgs args{r, s, L.gr, L.gs, L.big, L.bigcnt, L.off, L.total, ok, oa, ob, cap};
     qg_pre_launch(ctx);
-    k_pj_join<<<nbu, PB_THREADS, sizeof(PbSmem), ctx->stream>>>(args, lb);
+    k_pj_join<<<G, PB_THREADS, sizeof(PbSmem), ctx->stream>>>(args, lb);
     QG_TRY(qg_check_launch(ctx, "k_pj_join"));
     if (!cross.empty()) {
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, cross.data(), cross.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "cross h2d");
@@ -1012,18 +1085,17 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
             L.place, L.off, ok, oa, ob, cap);
         QG_TRY(qg_check_launch(ctx, "k_pj_place"));
     }
-    unsigned long long total = 0;
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-    total = (unsigned long long)ctx->pinned[0];
-    for (auto &t : temps) t.release();
-    // The look-back sums are 32-bit: recompute the total in 64 bits from the
-    // outside buckets when they alone could wrap it.
+    const unsigned long long total = (unsigned long long)ctx->pinned[0];
+    for (auto &t : temps) { cudaFree(t.k); cudaFree(t.a); cudaFree(t.c); }
+    // The look-back sums are 32-bit: report the outside groups' 64-bit sum
+    // when they alone could wrap it (a capacity error follows).
     *M_out = (long long)total;
     {
         unsigned long long outside = 0;
-        for (uint32_t b = 0; b < nbu; b++) outside += bigcnt[b];
-        if (outside >= (1ull << 32)) *M_out = (long long)outside;  // capacity error follows
+        for (uint32_t g = 0; g < G; g++) outside += bigcnt[g];
+        if (outside >= (1ull << 32)) *M_out = (long long)outside;
     }
     if (depth == 0) {
         ctx->pj_stats[0] = use_learned ? 2 : 1;
@@ -1040,7 +1112,7 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
             ctx->pj_stats[5] = hk[0];
             ctx->pj_stats[6] = hk[3];
         }
-        ctx->pj_stats[7] = judged ? 1 : 0;
+        ctx->pj_stats[7] = (judged && use_learned) ? 1 : 0;
     }
     ctx->pj_stats[4] = (uint32_t)depth_max;
     return QG_OK;
@@ -1050,7 +1122,7 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
 
 extern "C" QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucket_s_max,
                                               uint32_t bucket_r_max) {
-    if (variant < 0 || variant > 3 || buckets_log2 < 0 || buckets_log2 > 15) return QG_ERR_INVALID;
+    if (variant < 0 || variant > 3 || buckets_log2 < 0 || buckets_log2 > 16) return QG_ERR_INVALID;
     if (bucket_s_max > (uint32_t)PB_SMAX || bucket_r_max > (uint32_t)PB_RMAX) return QG_ERR_INVALID;
     g_pj_variant = variant;
     g_pj_blog2 = buckets_log2;
@@ -1085,7 +1157,7 @@ extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey
     // aux: R records + spare, S' records + spare, level-0 arrays
     const size_t rb = qg_align_up((size_t)nR * 8, 256), sb = qg_align_up((size_t)nS * 8, 256);
     char *aux;
-    QG_TRY(qg_aux(ctx, 2 * rb + 2 * sb + pj_level_bytes(PJ_MAX_BUCKETS), &aux));
+    QG_TRY(qg_aux(ctx, 2 * rb + 2 * sb + pj_level_bytes(PJ_MAX_BUCKETS, true), &aux));
     unsigned long long *R = (unsigned long long *)aux, *Rsp = (unsigned long long *)(aux + rb);
     unsigned long long *S = (unsigned long long *)(aux + 2 * rb), *Ssp = (unsigned long long *)(aux + 2 * rb + sb);
     char *lvl = aux + 2 * rb + 2 * sb;
