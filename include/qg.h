@@ -71,6 +71,10 @@ QG_API uint64_t qg_ctx_launch_count(qg_ctx *ctx);
  * (host/host/testFilter.cpp:110-141); this measures device time. */
 QG_API qg_status qg_ctx_enable_timing(qg_ctx *ctx, int on);
 QG_API int qg_ctx_timing_report(qg_ctx *ctx, char *buf, size_t len);
+/* Milliseconds from the start of the first to the end of the last launch
+ * logged since timing was enabled or last reported (an operator's device
+ * span, gaps between its kernels included); -1 when nothing was logged. */
+QG_API double qg_ctx_timing_span(qg_ctx *ctx);
 
 /* Device buffers handed out by callee-allocates entry points. */
 QG_API qg_status qg_malloc(qg_ctx *ctx, void **ptr, size_t bytes);
@@ -216,6 +220,26 @@ QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucke
  * out[6] heavy keys among them, out[7] 1 when the automatic choice moved
  * from radix to the learned function. */
 QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8);
+
+/* ---- learned cost model (no reference counterpart; it stands beside the
+ * static unit-cost table of host/dynamic_programming.cpp:152-167) ----
+ * A 16 -> 64 (ReLU) -> 1 fp32 MLP over plan features, trained on timings the
+ * engine records, predicting an operator variant's log run time.  params is
+ * a device array of qg_mlp_param_count() floats: W1[64][16], b1[64], W2[64],
+ * b2.  X is n x 16 row-major, y and out n floats, all on the device. */
+QG_API int64_t qg_mlp_param_count(void);
+/* Deterministic initialisation from a seed (uniform +-1/sqrt(fan_in), zero biases). */
+QG_API qg_status qg_mlp_init(qg_ctx *ctx, float *params, uint32_t seed);
+QG_API qg_status qg_mlp_predict(qg_ctx *ctx, const float *params, const float *X, int64_t n,
+                                float *out);
+/* Gradient of mean((f(X) - y)^2) into grad (param_count floats); loss (device
+ * float, may be NULL) receives the loss.  Deterministic (no atomics). */
+QG_API qg_status qg_mlp_grad(qg_ctx *ctx, const float *params, const float *X, const float *y,
+                             int64_t n, float *grad, float *loss);
+/* `steps` full-batch Adam steps.  opt: 3 * param_count device floats, zeroed
+ * before the first call of a training run; *t counts the steps taken. */
+QG_API qg_status qg_mlp_train(qg_ctx *ctx, float *params, const float *X, const float *y, int64_t n,
+                              int steps, float lr, float *opt, int *t, float *loss);
 
 /* ---- learned partition function (no reference counterpart) ----
  * A piecewise-linear model of a key CDF (1024 fp32 segments plus heavy-key

@@ -52,6 +52,8 @@ def lib() -> ctypes.CDLL:
                                                   c_int64, c_int32, c_int32, c_int64, c_void_p,
                                                   c_void_p, c_void_p]),
             "orc_hash_join_ref": (c_int64, [c_void_p, c_int64, c_void_p, c_int64, c_int64, c_void_p]),
+            "orc_mlp_forward": (None, [c_void_p, c_void_p, c_int64, c_void_p]),
+            "orc_mlp_grad": (ctypes.c_double, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -177,3 +179,21 @@ def ref_tool(*args: str) -> str:
     from the reference sources into oracle/_ref)."""
     res = subprocess.run([str(REF_TOOL), *map(str, args)], capture_output=True, text=True)
     return res.stdout + res.stderr
+
+
+def mlp_forward(params: np.ndarray, X: np.ndarray) -> np.ndarray:
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(X, np.float32)
+    out = np.empty(x.shape[0], np.float64)
+    lib().orc_mlp_forward(_p(p), _p(x), x.shape[0], _p(out))
+    return out
+
+
+def mlp_grad(params: np.ndarray, X: np.ndarray, y: np.ndarray):
+    """(loss, gradient) of mean((f(X) - y)^2) in double precision."""
+    p = np.ascontiguousarray(params, np.float32)
+    x = np.ascontiguousarray(X, np.float32)
+    t = np.ascontiguousarray(y, np.float32)
+    g = np.empty(p.size, np.float64)
+    loss = lib().orc_mlp_grad(_p(p), _p(x), _p(t), x.shape[0], _p(g))
+    return loss, g

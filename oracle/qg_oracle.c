@@ -529,3 +529,52 @@ ORC_EXPORT int64_t orc_hash_join_ref(const uint32_t *r, int64_t nR, const uint32
     free(rk);
     return m > cap ? -m - 1 : m;
 }
+
+/* ---- learned cost model (no reference counterpart: the reference's cost
+ * model is the static table of host/dynamic_programming.cpp:152-167) ----
+ * Restatement of the 16 -> 64 (ReLU) -> 1 MLP of csrc/qg_mlp.cu in double
+ * precision, the checker of the GPU forward pass and gradients.
+ * Parameters: W1[64][16], b1[64], W2[64], b2. */
+#define ORC_MI 16
+#define ORC_MH 64
+ORC_EXPORT void orc_mlp_forward(const float *p, const float *X, int64_t n, double *out) {
+    const float *W1 = p, *b1 = p + ORC_MI * ORC_MH, *W2 = b1 + ORC_MH, *b2 = W2 + ORC_MH;
+    for (int64_t s = 0; s < n; s++) {
+        double o = b2[0];
+        for (int j = 0; j < ORC_MH; j++) {
+            double a = b1[j];
+            for (int k = 0; k < ORC_MI; k++) a += (double)W1[j * ORC_MI + k] * X[s * ORC_MI + k];
+            if (a > 0) o += a * W2[j];
+        }
+        out[s] = o;
+    }
+}
+
+/* Gradient of mean((f(x) - y)^2); returns the loss. */
+ORC_EXPORT double orc_mlp_grad(const float *p, const float *X, const float *y, int64_t n, double *grad) {
+    const float *W1 = p, *b1 = p + ORC_MI * ORC_MH, *W2 = b1 + ORC_MH, *b2 = W2 + ORC_MH;
+    const int P = ORC_MI * ORC_MH + 2 * ORC_MH + 1;
+    for (int q = 0; q < P; q++) grad[q] = 0;
+    double loss = 0, z[ORC_MH];
+    for (int64_t s = 0; s < n; s++) {
+        double o = b2[0];
+        for (int j = 0; j < ORC_MH; j++) {
+            double a = b1[j];
+            for (int k = 0; k < ORC_MI; k++) a += (double)W1[j * ORC_MI + k] * X[s * ORC_MI + k];
+            z[j] = a;
+            if (a > 0) o += a * W2[j];
+        }
+        const double d = o - y[s];
+        loss += d * d;
+        const double go = 2.0 * d / (double)n;
+        grad[P - 1] += go;
+        for (int j = 0; j < ORC_MH; j++) {
+            if (z[j] <= 0) continue;
+            grad[ORC_MI * ORC_MH + ORC_MH + j] += go * z[j];
+            const double gz = go * W2[j];
+            grad[ORC_MI * ORC_MH + j] += gz;
+            for (int k = 0; k < ORC_MI; k++) grad[j * ORC_MI + k] += gz * X[s * ORC_MI + k];
+        }
+    }
+    return loss / (double)n;
+}

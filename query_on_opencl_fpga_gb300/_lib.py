@@ -38,6 +38,7 @@ SIGNATURES: dict[str, tuple] = {
     "qg_ctx_launch_count": (c_uint64, [c_void_p]),
     "qg_ctx_enable_timing": (c_int, [c_void_p, c_int]),
     "qg_ctx_timing_report": (c_int, [c_void_p, c_char_p, c_size_t]),
+    "qg_ctx_timing_span": (ctypes.c_double, [c_void_p]),
     "qg_malloc": (c_int, [c_void_p, POINTER(c_void_p), c_size_t]),
     "qg_free": (c_int, [c_void_p, c_void_p]),
     "qg_filter_range_rec": (c_int, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int64,
@@ -74,6 +75,12 @@ SIGNATURES: dict[str, tuple] = {
     "qg_join_set_knobs": (c_int, [c_int, c_int, c_uint32, c_uint32]),
     "qg_join_stats": (c_int, [c_void_p, c_void_p]),
     "qg_part_model_bytes": (c_int64, []),
+    "qg_mlp_param_count": (c_int64, []),
+    "qg_mlp_init": (c_int, [c_void_p, c_void_p, c_uint32]),
+    "qg_mlp_predict": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
+    "qg_mlp_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "qg_mlp_train": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int, ctypes.c_float,
+                             c_void_p, POINTER(c_int), c_void_p]),
     "qg_part_learn": (c_int, [c_void_p, c_void_p, c_int64, c_uint32, c_void_p]),
     "qg_part_eval": (c_int, [c_void_p, c_void_p, c_uint32, c_int, c_void_p, c_int64, c_void_p]),
 }

@@ -82,6 +82,46 @@ class Context:
             out[name] = (int(cnt), float(ms))
         return out
 
+    def timing_span(self) -> float:
+        """Device ms from the first logged launch's start to the last one's end (-1: none)."""
+        return float(self.lib.qg_ctx_timing_span(self.handle))
+
+    # ---- learned cost model (qg_mlp.cu) ----------------------------------
+    def mlp_init(self, seed: int = 0) -> torch.Tensor:
+        p = torch.empty(int(self.lib.qg_mlp_param_count()), dtype=torch.float32, device="cuda")
+        self.check(self.lib.qg_mlp_init(self.handle, _ptr(p), seed & 0xFFFFFFFF), "qg_mlp_init")
+        return p
+
+    def mlp_predict(self, params: torch.Tensor, X: torch.Tensor) -> torch.Tensor:
+        _check_dev(params, X)
+        out = torch.empty(X.shape[0], dtype=torch.float32, device=X.device)
+        self.check(self.lib.qg_mlp_predict(self.handle, _ptr(params), _ptr(X), X.shape[0], _ptr(out)),
+                   "qg_mlp_predict")
+        return out
+
+    def mlp_grad(self, params: torch.Tensor, X: torch.Tensor, y: torch.Tensor):
+        """(loss, gradient) of mean((f(X) - y)^2), computed by the GPU kernels."""
+        _check_dev(params, X, y)
+        g = torch.empty_like(params)
+        loss = torch.empty(1, dtype=torch.float32, device=X.device)
+        self.check(self.lib.qg_mlp_grad(self.handle, _ptr(params), _ptr(X), _ptr(y), X.shape[0], _ptr(g),
+                                        _ptr(loss)), "qg_mlp_grad")
+        return float(loss.item()), g
+
+    def mlp_train(self, params: torch.Tensor, X: torch.Tensor, y: torch.Tensor, steps: int, lr: float,
+                  opt: torch.Tensor | None = None, t: list | None = None) -> float:
+        """Full-batch Adam steps on the GPU; returns the last step's loss."""
+        _check_dev(params, X, y)
+        if opt is None:
+            opt = torch.zeros(3 * params.numel(), dtype=torch.float32, device=params.device)
+        tt = ctypes.c_int(t[0] if t else 0)
+        loss = torch.empty(1, dtype=torch.float32, device=X.device)
+        self.check(self.lib.qg_mlp_train(self.handle, _ptr(params), _ptr(X), _ptr(y), X.shape[0], steps, lr,
+                                         _ptr(opt), byref(tt), _ptr(loss)), "qg_mlp_train")
+        if t is not None:
+            t[0] = tt.value
+        return float(loss.item())
+
     def set_spin_limit(self, polls: int) -> None:
         self.check(self.lib.qg_ctx_set_spin_limit(self.handle, polls), "qg_ctx_set_spin_limit")
 

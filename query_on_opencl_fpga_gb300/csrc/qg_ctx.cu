@@ -164,6 +164,18 @@ QG_API qg_status qg_ctx_enable_timing(qg_ctx *ctx, int on) {
     return QG_OK;
 }
 
+// After synchronising: milliseconds from the start of the first launch to
+// the end of the last launch logged since timing was enabled (or the last
+// report) -- an operator's device span including the gaps between its
+// kernels.  -1 when nothing was logged.
+QG_API double qg_ctx_timing_span(qg_ctx *ctx) {
+    if (!ctx || !ctx->timing || ctx->ev_used == 0) return -1.0;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1.0;
+    float ms = -1.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[2 * (ctx->ev_used - 1) + 1]) != cudaSuccess) return -1.0;
+    return ms;
+}
+
 // After synchronising: one "name launches total_ms" line per kernel name for
 // the launches since the last report (or enable), then resets the log.
 QG_API int qg_ctx_timing_report(qg_ctx *ctx, char *buf, size_t len) {
