@@ -39,6 +39,7 @@ struct JoinCtl {
     uint32_t kmin, kmax;
     unsigned long long n_special;  // build rows equal to EMPTY_SLOT (key -1, payload -1)
     unsigned long long cursor;     // output rows produced
+    unsigned long long sortn;      // rows the device-planned sort orders (0 when over capacity)
     uint32_t hist[4][QG_RADIX];
 };
 
@@ -49,6 +50,7 @@ __global__ void k_join_ctl_init(JoinCtl *jc) {
         jc->kmax = 0;
         jc->n_special = 0;
         jc->cursor = 0;
+        jc->sortn = 0;
     }
     for (int i = t; i < 4 * QG_RADIX; i += blockDim.x) (&jc->hist[0][0])[i] = 0;
 }
@@ -381,11 +383,30 @@ static int grid_cap(qg_ctx *ctx, long long work, int per_block, int per_sm) {
     return (int)b;
 }
 
+static int g_join_table_factor = 2;  // table slots >= factor * build rows (a power of two)
+
 static uint32_t table_slots(long long nR) {
     uint64_t c = 1024;
-    while (c < (uint64_t)nR * 2) c <<= 1;
+    while (c < (uint64_t)nR * g_join_table_factor) c <<= 1;
     return (uint32_t)c;
 }
+
+void qg_join_set_table_factor(int factor) { g_join_table_factor = factor < 2 ? 2 : (factor > 8 ? 8 : factor); }
+
+namespace {
+// After the probe of the device-planned join: publish the count, and let the
+// sort run only when the output fits.
+__global__ void k_join_finish_async(JoinCtl *jc, long long cap, unsigned long long *d_count, qg_control *ctl) {
+    const unsigned long long m = jc->cursor;
+    *d_count = m;
+    if (m > (unsigned long long)cap) {
+        jc->sortn = 0;
+        qg_record_error(ctl, QG_ERR_CAPACITY, QG_SITE_JOIN_PROBE);
+    } else {
+        jc->sortn = m;
+    }
+}
+}  // namespace
 
 // Build the table in aux; returns the control block (in scratch) and mask.
 static qg_status join_build(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay, long long stride,
@@ -487,6 +508,56 @@ qg_status qg_join_hash_sort(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpa
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(out_spay, A.b, (size_t)m * 4, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
     }
     return qg_ctx_check(ctx);
+}
+
+// The hash join + filter + sort with no host round trip (for CUDA graph
+// capture, e.g. by qg_batch): the sort always takes all four key digits and
+// is planned on the device from the probe's digit counts.  d_count (device
+// int64) receives the match count; more matches than cap records
+// QG_ERR_CAPACITY in the context's error word and leaves the output unsorted.
+qg_status qg_join_hash_sort_async(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay, int64_t nR,
+                                  const int32_t *skey, const int32_t *spay, int64_t nS, int32_t slo,
+                                  int32_t shi, int32_t *out_key, int32_t *out_rpay, int32_t *out_spay,
+                                  int64_t cap, int64_t *d_count) {
+    if (!ctx || nR < 0 || nS < 0 || cap < 0 || !d_count) return QG_ERR_INVALID;
+    if ((nR > 0 && (!rkey || !rpay)) || (nS > 0 && (!skey || !spay)) ||
+        (cap > 0 && (!out_key || !out_rpay || !out_spay)))
+        return QG_ERR_INVALID;
+    if ((((uintptr_t)skey) | ((uintptr_t)spay)) & 15) return QG_ERR_INVALID;
+    if (cap >= (1LL << 30) || nS >= (1LL << 40)) return QG_ERR_UNSUPPORTED;
+    if (nR == 0 || nS == 0 || cap == 0) {
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(d_count, 0, 8, ctx->stream), "memset count");
+        return QG_OK;
+    }
+    const size_t colbytes = qg_align_up((size_t)cap * 4, 256);
+    const size_t work = qg_align_up(qg_radix_dev_work_bytes(cap), 256);
+    unsigned long long *tab;
+    uint32_t mask;
+    JoinCtl *jc;
+    char *tail;
+    QG_TRY(join_build(ctx, rkey, rpay, 1, nR, 3 * colbytes + work, &tab, &mask, &jc, &tail));
+    qg_sort_bufs A{nullptr, (uint32_t *)out_key, (uint32_t *)out_rpay, (uint32_t *)out_spay};
+    qg_sort_bufs B{nullptr, (uint32_t *)tail, (uint32_t *)(tail + colbytes), (uint32_t *)(tail + 2 * colbytes)};
+    ProbeOut po{A.k, A.a, A.b};
+    const size_t smem = sizeof(PjSmem);
+    static bool attr = false;
+    if (!attr) {
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_join_probe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "attr");
+        attr = true;
+    }
+    const long long ntiles = (nS + PJ_TILE - 1) / PJ_TILE;
+    int blocks = (int)(ntiles < (long long)ctx->sm_count * 3 ? ntiles : (long long)ctx->sm_count * 3);
+    qg_pre_launch(ctx);
+    k_join_probe<<<blocks, PJ_THREADS, smem, ctx->stream>>>(skey, spay, nS, slo, shi, tab, mask, jc, po, cap,
+                                                             0u, 4, ctx->ctl, ctx->spin_limit);
+    QG_TRY(qg_check_launch(ctx, "k_join_probe"));
+    qg_pre_launch(ctx);
+    k_join_finish_async<<<1, 1, 0, ctx->stream>>>(jc, cap, (unsigned long long *)d_count, ctx->ctl);
+    QG_TRY(qg_check_launch(ctx, "k_join_finish_async"));
+    bool in_b = false;
+    QG_TRY(qg_radix_passes_dev(ctx, true, A, B, cap, &jc->sortn, &jc->hist[0][0], 4, 0u,
+                               tail + 3 * colbytes, &in_b));
+    return in_b ? QG_ERR_INVALID : QG_OK;  // four passes end where they began
 }
 
 extern "C" QG_API qg_status qg_hash_join_ref(qg_ctx *ctx, const uint32_t *r, int64_t nR,

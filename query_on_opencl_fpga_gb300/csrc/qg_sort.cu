@@ -82,10 +82,16 @@ template <bool KV3, bool LEARNED>
 __global__ void __launch_bounds__(RS_THREADS)
 k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
              const qg_cdf_model *model, const uint32_t *__restrict__ dbase,
-             uint32_t *__restrict__ status, qg_control *ctl, uint32_t spin_limit) {
+             uint32_t *__restrict__ status, qg_control *ctl, uint32_t spin_limit,
+             const unsigned long long *__restrict__ d_n) {
     extern __shared__ __align__(16) unsigned char rs_raw[];
     RsSmem<KV3> &S = *reinterpret_cast<RsSmem<KV3> *>(rs_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // Item count known only on the device (graph-captured sorts): the grid
+    // covers the bound n, and CTAs past the real count leave at once (no
+    // tile before them waits on them).
+    if (d_n && *d_n < (unsigned long long)n) n = (long long)*d_n;
+    if ((long long)blockIdx.x * RS_TILE >= n) return;
     for (int i = tid; i < RS_WARPS * QG_RADIX; i += RS_THREADS) (&S.whist[0][0])[i] = 0;
     __syncthreads();
     // Tile i is CTA i (started in index order); the status words are cleared
@@ -314,18 +320,77 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
         qg_pre_launch(ctx);
         if (kv3)
             k_radix_pass<true, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr);
         else if (pf.learned)
             k_radix_pass<false, true><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, 0u, pf.model, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+                s, d, n, shift, 0u, pf.model, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr);
         else
             k_radix_pass<false, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit);
+                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
         in_a = !in_a;
     }
     *result_in_b = !in_a;
     return QG_OK;
+}
+
+// Exclusive digit bases of every position from a device histogram [npos][256].
+__global__ void k_radix_bases(const uint32_t *__restrict__ hist, int npos, uint32_t *__restrict__ bases) {
+    __shared__ uint32_t ws[QG_RADIX / 32];
+    const int d = threadIdx.x, lane = d & 31, w = d >> 5;
+    for (int p = 0; p < npos; p++) {
+        const uint32_t c = hist[p * QG_RADIX + d];
+        uint32_t inc = c;
+#pragma unroll
+        for (int k = 1; k < 32; k <<= 1) {
+            const uint32_t x = __shfl_up_sync(QG_FULL_MASK, inc, k);
+            if (lane >= k) inc += x;
+        }
+        if (lane == 31) ws[w] = inc;
+        __syncthreads();
+        uint32_t off = 0;
+        for (int i = 0; i < w; i++) off += ws[i];
+        bases[p * QG_RADIX + d] = off + inc - c;
+        __syncthreads();
+    }
+}
+
+qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n_bound,
+                              const unsigned long long *d_n, const uint32_t *d_hist, int npos, uint32_t key_off,
+                              char *work, bool *result_in_b) {
+    *result_in_b = false;
+    if (n_bound <= 1 || npos <= 0) return QG_OK;
+    if (n_bound >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
+    const long long tiles = (n_bound + RS_TILE - 1) / RS_TILE;
+    uint32_t *dbase = (uint32_t *)work;
+    uint32_t *status = dbase + 4 * QG_RADIX;
+    const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
+    if (kv3) QG_TRY((rs_set_attr<true, false>(ctx)));
+    else QG_TRY((rs_set_attr<false, false>(ctx)));
+    qg_pre_launch(ctx);
+    k_radix_bases<<<1, QG_RADIX, 0, ctx->stream>>>(d_hist, npos, dbase);
+    QG_TRY(qg_check_launch(ctx, "k_radix_bases"));
+    bool in_a = true;
+    for (int p = 0; p < npos; p++) {
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(status, 0, (size_t)tiles * QG_RADIX * 4, ctx->stream), "memset status");
+        const qg_sort_bufs &s = in_a ? a : b;
+        const qg_sort_bufs &d = in_a ? b : a;
+        qg_pre_launch(ctx);
+        if (kv3)
+            k_radix_pass<true, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n);
+        else
+            k_radix_pass<false, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n);
+        QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
+        in_a = !in_a;
+    }
+    *result_in_b = !in_a;
+    return QG_OK;
+}
+
+size_t qg_radix_dev_work_bytes(long long n_bound) {
+    return 4 * QG_RADIX * 4 + (size_t)((n_bound + RS_TILE - 1) / RS_TILE) * QG_RADIX * 4;
 }
 
 qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,

@@ -32,6 +32,14 @@ struct qg_part_fn;
 qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
                              const qg_part_fn &pf, const int *passes, int np, const uint32_t *h_bases,
                              bool *result_in_b);
+// Passes planned on the device, for sequences without host round trips
+// (CUDA graph capture): all `npos` positions from the device histogram d_hist
+// [npos][256] of (key - key_off) digits, over at most n_bound items whose real
+// count is *d_n.  work: qg_radix_dev_work_bytes(n_bound) bytes of device memory.
+qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n_bound,
+                              const unsigned long long *d_n, const uint32_t *d_hist, int npos, uint32_t key_off,
+                              char *work, bool *result_in_b);
+size_t qg_radix_dev_work_bytes(long long n_bound);
 // Sort REC items in place with `tmp` as the second buffer (synchronises once).
 qg_status qg_sort_rec_inplace(qg_ctx *ctx, unsigned long long *data, unsigned long long *tmp,
                               long long n);
