@@ -221,6 +221,42 @@ QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucke
  * from radix to the learned function. */
 QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8);
 
+/* ---- batched queries (no reference counterpart: the reference runs one
+ * operator per call, each followed by clFinish and host reads) ----
+ * A batch of filter / group-by / fused filter+group-by / join+sort queries is
+ * run once eagerly, captured into a CUDA graph of the operators' sync-free
+ * forms (one graph per autotuner candidate: group-by shared table of 2^12 or
+ * 2^13 slots x join hash table at 2x or 4x the build rows), timed, and the
+ * fastest graph kept; qg_batch_run replays it with one graph launch.  The
+ * batch owns a private context whose work arenas the graph addresses.
+ * Inputs and outputs stay the caller's and must stay valid while the batch
+ * exists.  Joins in a batch use the global hash table + device-planned sort;
+ * group-by outputs are unordered (QG_ORDER_NONE).  Errors of a replay (a
+ * join over cap: QG_ERR_CAPACITY; a group-by spill overflow:
+ * QG_ERR_TABLE_FULL) are reported by qg_batch_check. */
+typedef enum { QG_OP_FILTER = 0, QG_OP_GROUPBY = 1, QG_OP_FUSED = 2, QG_OP_JOIN = 3 } qg_op;
+typedef struct {
+    int op;                /* qg_op */
+    int variant;           /* -1 default; filter 0 or 1; group-by 0 two-pass, 1 global table, 2 two-pass 64-bit adds */
+    int64_t n;             /* rows (join: S rows) */
+    int64_t n2;            /* join: R rows */
+    const int32_t *in[4];  /* filter: key, payload; group-by: key, value, value2 (fused); join: rkey, rpay, skey, spay */
+    int32_t lo, hi;        /* filter: key range; fused: value2 range; join: S.payload range */
+    void *out[3];          /* filter: (row id, payload) int32 pairs; group-by: key int32, sum int64, count int64;
+                              join: key, R.payload, S.payload int32 */
+    int64_t cap;           /* output rows room (group-by: groups) */
+    int64_t *d_count;      /* device int64: rows produced */
+} qg_query;
+typedef struct qg_batch qg_batch;
+QG_API qg_status qg_batch_create(const qg_query *queries, int nq, int autotune, qg_batch **out);
+/* Enqueue the batch on `stream` (a cudaStream_t; NULL = the default stream). */
+QG_API qg_status qg_batch_run(qg_batch *b, void *stream);
+/* Synchronise `stream` and report the first device error of the batch's kernels. */
+QG_API qg_status qg_batch_check(qg_batch *b, void *stream);
+/* out4: group-by table slots log2, join table factor, best replay in us, graph nodes. */
+QG_API qg_status qg_batch_info(const qg_batch *b, int32_t *out4);
+QG_API qg_status qg_batch_destroy(qg_batch *b);
+
 /* ---- learned cost model (no reference counterpart; it stands beside the
  * static unit-cost table of host/dynamic_programming.cpp:152-167) ----
  * A 16 -> 64 (ReLU) -> 1 fp32 MLP over plan features, trained on timings the

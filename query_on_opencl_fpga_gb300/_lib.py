@@ -123,6 +123,21 @@ SIGNATURES.update({
     "scatterImpl": (None, [QgBuf, _c, QgBuf, QgBuf, _c, _c, c_void_p]),
 })
 
+class Query(ctypes.Structure):
+    """qg_query (include/qg.h)."""
+    _fields_ = [("op", c_int), ("variant", c_int), ("n", c_int64), ("n2", c_int64),
+                ("inp", c_void_p * 4), ("lo", c_int32), ("hi", c_int32), ("out", c_void_p * 3),
+                ("cap", c_int64), ("d_count", c_void_p)]
+
+
+SIGNATURES.update({
+    "qg_batch_create": (c_int, [POINTER(Query), c_int, c_int, POINTER(c_void_p)]),
+    "qg_batch_run": (c_int, [c_void_p, c_void_p]),
+    "qg_batch_check": (c_int, [c_void_p, c_void_p]),
+    "qg_batch_info": (c_int, [c_void_p, c_void_p]),
+    "qg_batch_destroy": (c_int, [c_void_p]),
+})
+
 PLAN_MAX_OPS = 16
 PLAN_MAX_IMAGES = 16
 

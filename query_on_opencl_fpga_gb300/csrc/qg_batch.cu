@@ -1,0 +1,207 @@
+// qg_batch.cu -- many queries of uneven sizes as one CUDA graph.
+//
+// The reference runs one operator per call, each call followed by clFinish
+// and host reads (host/host/common.cpp:31, testFilter.cpp:128-133).  A batch
+// here is a list of filter / group-by / fused filter+group-by / join+sort
+// queries that is
+//   1. run once eagerly per candidate configuration, so that every work arena
+//      reaches its final size (a graph may not allocate, and later growth
+//      would move memory the graph's kernels address),
+//   2. captured, for every candidate configuration of the autotuner (the
+//      group-by's shared-memory table size and the join's hash-table load),
+//      into a CUDA graph of the sync-free forms of the operators
+//      (qg_filter_cols_async, qg_groupby_cols_async, qg_join_hash_sort_async),
+//   3. timed by replays, keeping the fastest graph.
+// qg_batch_run then replays that graph on the caller's stream: the whole
+// batch costs one graph launch and no host round trip.  Each query's kernel
+// variant comes from the query (chosen by the caller, e.g. by the learned
+// cost model) or is the default.  The batch owns a private context, so its
+// arenas are never moved by other calls.
+#include <vector>
+#include "qg_internal.cuh"
+
+qg_status qg_join_hash_sort_async(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay, int64_t nR,
+                                  const int32_t *skey, const int32_t *spay, int64_t nS, int32_t slo,
+                                  int32_t shi, int32_t *out_key, int32_t *out_rpay, int32_t *out_spay,
+                                  int64_t cap, int64_t *d_count);
+void qg_join_set_table_factor(int factor);
+
+struct qg_batch {
+    qg_ctx *own = nullptr;
+    cudaStream_t stream = nullptr;  // capture stream of the private context
+    std::vector<qg_query> q;
+    cudaGraphExec_t exec = nullptr;
+    int32_t info[4] = {0, 0, 0, 0};  // hot slots log2, table factor, best replay us, graph nodes
+};
+
+namespace {
+
+struct BatchCfg {
+    int hot_log2;
+    int table_factor;
+};
+
+qg_status enqueue(qg_batch *b, const BatchCfg &c) {
+    qg_ctx *ctx = b->own;
+    qg_status st = QG_OK;
+    for (const qg_query &q : b->q) {
+        const int v = q.variant < 0 ? 0 : q.variant;
+        switch (q.op) {
+        case QG_OP_FILTER:
+            st = qg_filter_set_variant(v);
+            if (st == QG_OK)
+                st = qg_filter_cols_async(ctx, q.in[0], q.in[1], q.n, q.lo, q.hi, (int32_t *)q.out[0], q.cap,
+                                          q.d_count);
+            break;
+        case QG_OP_GROUPBY:
+        case QG_OP_FUSED:
+            st = qg_groupby_set_knobs(v, c.hot_log2, 0, 0);
+            if (st == QG_OK)
+                st = qg_groupby_cols_async(ctx, q.in[0], q.in[1], q.op == QG_OP_FUSED ? q.in[2] : nullptr, q.lo,
+                                           q.hi, q.n, (int32_t *)q.out[0], (int64_t *)q.out[1],
+                                           (int64_t *)q.out[2], q.cap, QG_ORDER_NONE, q.d_count);
+            break;
+        case QG_OP_JOIN:
+            qg_join_set_table_factor(c.table_factor);
+            st = qg_join_hash_sort_async(ctx, q.in[0], q.in[1], q.n2, q.in[2], q.in[3], q.n, q.lo, q.hi,
+                                         (int32_t *)q.out[0], (int32_t *)q.out[1], (int32_t *)q.out[2], q.cap,
+                                         q.d_count);
+            break;
+        default:
+            st = QG_ERR_INVALID;
+        }
+        if (st != QG_OK) break;
+    }
+    qg_filter_set_variant(0);
+    qg_groupby_set_knobs(0, 13, 0, 0);
+    qg_join_set_table_factor(2);
+    return st;
+}
+
+qg_status capture(qg_batch *b, const BatchCfg &c, cudaGraphExec_t *exec, size_t *nodes) {
+    cudaGraph_t g = nullptr;
+    QG_TRY_CUDA(b->own, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    const qg_status st = enqueue(b, c);
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (st != QG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    QG_TRY_CUDA(b->own, e, "end capture");
+    cudaError_t ei = cudaGraphGetNodes(g, nullptr, nodes);
+    if (ei == cudaSuccess) ei = cudaGraphInstantiate(exec, g, 0);
+    cudaGraphDestroy(g);
+    QG_TRY_CUDA(b->own, ei, "instantiate graph");
+    return QG_OK;
+}
+
+float replay_ms(qg_batch *b, cudaGraphExec_t exec, int reps) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaGraphLaunch(exec, b->stream);
+    cudaEventRecord(e0, b->stream);
+    for (int i = 0; i < reps; i++) cudaGraphLaunch(exec, b->stream);
+    cudaEventRecord(e1, b->stream);
+    float ms = -1.f;
+    if (cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / reps;
+}
+
+}  // namespace
+
+extern "C" {
+
+QG_API qg_status qg_batch_create(const qg_query *queries, int nq, int autotune, qg_batch **out) {
+    if (!queries || nq <= 0 || !out) return QG_ERR_INVALID;
+    *out = nullptr;
+    qg_batch *b = new qg_batch();
+    b->q.assign(queries, queries + nq);
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return QG_ERR_CUDA;
+    }
+    qg_status st = qg_ctx_create(&b->own, b->stream);
+    std::vector<BatchCfg> cands;
+    if (autotune) {
+        for (int h : {12, 13})
+            for (int t : {2, 4}) cands.push_back(BatchCfg{h, t});
+    } else {
+        cands.push_back(BatchCfg{13, 2});
+    }
+    // 1. eager runs of every candidate: the arenas reach their final sizes
+    for (size_t i = 0; i < cands.size() && st == QG_OK; i++) {
+        st = enqueue(b, cands[i]);
+        if (st == QG_OK) st = qg_ctx_check(b->own);
+    }
+    // 2. capture and time every candidate, keep the fastest
+    float best = 0.f;
+    for (size_t i = 0; i < cands.size() && st == QG_OK; i++) {
+        cudaGraphExec_t ex = nullptr;
+        size_t nodes = 0;
+        st = capture(b, cands[i], &ex, &nodes);
+        if (st != QG_OK) break;
+        const float ms = replay_ms(b, ex, 3);
+        st = qg_ctx_check(b->own);
+        if (st != QG_OK || ms < 0.f) {
+            cudaGraphExecDestroy(ex);
+            if (st == QG_OK) st = QG_ERR_CUDA;
+            break;
+        }
+        if (!b->exec || ms < best) {
+            if (b->exec) cudaGraphExecDestroy(b->exec);
+            b->exec = ex;
+            best = ms;
+            b->info[0] = cands[i].hot_log2;
+            b->info[1] = cands[i].table_factor;
+            b->info[2] = (int32_t)(ms * 1000.f);
+            b->info[3] = (int32_t)nodes;
+        } else {
+            cudaGraphExecDestroy(ex);
+        }
+    }
+    if (st != QG_OK) {
+        qg_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return QG_OK;
+}
+
+QG_API qg_status qg_batch_run(qg_batch *b, void *stream) {
+    if (!b || !b->exec) return QG_ERR_INVALID;
+    if (cudaGraphLaunch(b->exec, (cudaStream_t)stream) != cudaSuccess) {
+        cudaGetLastError();
+        return QG_ERR_CUDA;
+    }
+    return QG_OK;
+}
+
+QG_API qg_status qg_batch_check(qg_batch *b, void *stream) {
+    if (!b) return QG_ERR_INVALID;
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) {
+        cudaGetLastError();
+        return QG_ERR_CUDA;
+    }
+    return qg_ctx_check(b->own);
+}
+
+QG_API qg_status qg_batch_info(const qg_batch *b, int32_t *out4) {
+    if (!b || !out4) return QG_ERR_INVALID;
+    for (int i = 0; i < 4; i++) out4[i] = b->info[i];
+    return QG_OK;
+}
+
+QG_API qg_status qg_batch_destroy(qg_batch *b) {
+    if (!b) return QG_ERR_INVALID;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->own) qg_ctx_destroy(b->own);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return QG_OK;
+}
+
+}  // extern "C"
