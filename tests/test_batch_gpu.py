@@ -1,0 +1,76 @@
+"""GPU parity of the batched executor (one captured CUDA graph for many
+queries) against the plain per-query calls of the same operators."""
+import numpy as np
+import pytest
+
+from query_on_opencl_fpga_gb300 import batch as qb
+
+pytestmark = pytest.mark.gpu
+
+
+def _rows(t):
+    a = [x.cpu().numpy() for x in (t if isinstance(t, tuple) else (t,))]
+    if len(a) == 1:
+        return a[0].reshape(-1, 2).astype(np.int64)
+    return np.stack([x.astype(np.int64) for x in a], 1)
+
+
+def _same(op, got, exp):
+    g, e = _rows(got), _rows(exp)
+    assert g.shape == e.shape
+    if op == qb.OP_FILTER:  # stable: input order on both paths
+        assert np.array_equal(g, e)
+        return
+    if op == qb.OP_JOIN:  # sorted by unsigned key on both paths; equal keys in any order
+        k = (g[:, 0] & 0xFFFFFFFF)
+        assert (k[1:] >= k[:-1]).all()
+    gs = g[np.lexsort(g.T[::-1])]
+    es = e[np.lexsort(e.T[::-1])]
+    assert np.array_equal(gs, es)
+
+
+@pytest.mark.parametrize("autotune", [False, True])
+def test_batch_matches_plain_calls(ctx, autotune):
+    qs = qb.mixed_queries(24, seed=7, lo=4096, hi=1 << 18)
+    plain = qb.run_plain(ctx, qs)
+    b = qb.Batch(qs, autotune=autotune)
+    try:
+        for _ in range(2):  # replays give the same results
+            for q in qs:
+                q["count"].fill_(-1)
+            b.run()
+            b.check()
+            for q, got, exp in zip(qs, qb.batch_results(qs), plain):
+                _same(q["op"], got, exp)
+        info = b.info()
+        assert info["graph_nodes"] > len(qs) and info["replay_us"] > 0
+        assert info["hot_slots_log2"] in (12, 13) and info["join_table_factor"] in (2, 4)
+    finally:
+        b.close()
+
+
+def test_batch_variants_are_bit_identical(ctx):
+    qs = qb.mixed_queries(12, seed=11, lo=4096, hi=1 << 17, ops=(qb.OP_FILTER, qb.OP_GROUPBY, qb.OP_FUSED))
+    plain = qb.run_plain(ctx, qs)
+    for q in qs:
+        q["variant"] = 1  # filter: bulk-copy ring; group-by: global table
+    b = qb.Batch(qs, autotune=False)
+    try:
+        b.run()
+        b.check()
+        for q, got, exp in zip(qs, qb.batch_results(qs), plain):
+            _same(q["op"], got, exp)
+    finally:
+        b.close()
+
+
+def test_batch_join_over_capacity_reports_error(ctx):
+    from query_on_opencl_fpga_gb300.api import QGError
+
+    qs = qb.mixed_queries(1, seed=3, lo=8192, hi=8193, ops=(qb.OP_JOIN,))
+    qs[0]["cap"] = 10  # far fewer than the matches
+    with pytest.raises(QGError) as e:
+        qb.Batch(qs, autotune=False)
+    assert e.value.status == 3  # QG_ERR_CAPACITY, seen by the eager run
+    # the context of ordinary calls is unaffected
+    ctx.check(ctx.lib.qg_ctx_check(ctx.handle), "qg_ctx_check")
