@@ -398,13 +398,91 @@ def operator_lines(ctx, args, peak, stream):
     m = res["o"][0].numel()
     nR, nS = 1 << 24, 1 << 28
     alg = nR * 8 + nS * 8 + m * 12 + 2 * m * 12
+    sp = int((j["spay"] <= 299).logical_and(j["skey"] < nR).sum())  # S' rows the S filter keeps
     out["join_config2"] = {"rows_per_s": nS / (ms * 1e-3), "ms_per_op": ms, "out_rows": m,
                            "op_frac_of_peak": alg / (ms * 1e-3) / 1e9 / peak,
                            "kernels_ms": {k: v[1] / steps for k, v in kern.items()},
-                           "roofline_probe": roofline(kern, "k_join_probe", nS * 8 + m * 12, peak)}
+                           "path": ctx.join_stats()["path"],
+                           "roofline_sfilter": roofline(kern, "k_pj_sfilter", nS * 8 + sp * 8, peak)}
     del j, res
     torch.cuda.empty_cache()
+    if not args.no_learned:
+        out["skew_join_config4"] = skew_line(ctx, stream)
+        torch.cuda.empty_cache()
+        out["batched_config3"] = batched_line(ctx, stream)
+        torch.cuda.empty_cache()
     return out
+
+
+def skew_line(ctx, stream):
+    """Config 4: skewed join, plain radix partitioning vs the learned partition function."""
+    import torch
+
+    from query_on_opencl_fpga_gb300 import datagen
+
+    nR, nS = 1 << 25, 1 << 28
+    j = datagen.config4_skewed(nR, nS, seed=0, device="cuda")
+    res = {}
+    for name, v in (("radix", 1), ("learned", 2)):
+        ctx.join_set_knobs(v)
+
+        def step():
+            ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"], j["shi"],
+                                 cap=int(nS * 0.3) + 1024)
+
+        step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(2):
+            step()
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / 2 * 1e3
+        res[name] = {"ms_per_op": ms, "rows_per_s": (nR + nS) / (ms * 1e-3), **ctx.join_stats()}
+    ctx.join_set_knobs(0)
+    res["learned_over_radix"] = res["radix"]["ms_per_op"] / res["learned"]["ms_per_op"]
+    res["workload"] = ("config4: R 32M distinct keys and S 256M keys from 8 Gaussians (sigma 2^20) + 5% "
+                       "Zipf(1.2) heavy hitters, S.payload < 300, output sorted by key")
+    return res
+
+
+def batched_line(ctx, stream):
+    """Config 3: 512 mixed queries, plain per-query calls vs one captured graph
+    whose variants the learned cost model chose (wall time, inputs on the GPU)."""
+    import json as _json
+
+    import torch
+
+    from query_on_opencl_fpga_gb300 import batch as qb
+    from query_on_opencl_fpga_gb300 import costmodel
+
+    qs = qb.mixed_queries(512, seed=0)
+    rows = qb.input_rows(qs)
+    qb.run_plain(ctx, qs)  # warm-up (arena sizes)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    qb.run_plain(ctx, qs)
+    torch.cuda.synchronize()
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    recs = _json.loads((ROOT / "tests" / "golden" / "costlog.json").read_text())["records"]
+    params, _ = costmodel.train(ctx, recs)
+    qb.choose_variants(ctx, params, qs)
+    b = qb.Batch(qs, autotune=True)
+    b.run()
+    b.check()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        b.run()
+    b.check()
+    batch_ms = (time.perf_counter() - t0) / 3 * 1e3
+    info = b.info()
+    b.close()
+    nops = {qb.OP_NAMES[o]: sum(1 for q in qs if q["op"] == o) for o in qb.OP_NAMES}
+    return {"queries": len(qs), "ops": nops, "input_rows": rows,
+            "plain": {"ms": plain_ms, "rows_per_s": rows / (plain_ms * 1e-3)},
+            "learned_batched": {"ms": batch_ms, "rows_per_s": rows / (batch_ms * 1e-3), **info},
+            "batched_over_plain": plain_ms / batch_ms,
+            "workload": "config3: 512 queries, op uniform over filter/groupby/fused/join, rows log-uniform "
+                        "in [4096, 16M], config 0-2 distributions, seeds 0..511"}
 
 
 def run_only(args):
@@ -476,6 +554,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-operators", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the config 3 / config 4 lines")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
