@@ -221,6 +221,18 @@ QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucke
  * from radix to the learned function. */
 QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8);
 
+/* ---- whole-column reduce (the check of host/host/Validate.cpp:372-468; the
+ * reference ships no kernel) ----  SUM (wrapping modulo 2^32), MAX and MIN
+ * (unsigned compare) or AVERAGE (wrapped sum / n, unsigned) of Record.y. */
+QG_API qg_status qg_reduce_rec(qg_ctx *ctx, const void *in_records, int64_t n, int op,
+                               uint32_t *result);
+/* ---- radix split (splitImpl, host/host/testSplit.cpp:156-209; kernels not
+ * shipped) ----  out = the records grouped by partition id (y mod num_part),
+ * stable within a partition; bound[p] (device, num_part int32) = first row of
+ * partition p. */
+QG_API qg_status qg_split_rec(qg_ctx *ctx, const void *in_records, int64_t n, int32_t num_part,
+                              void *out_records, int32_t *bound);
+
 /* ---- batched queries (no reference counterpart: the reference runs one
  * operator per call, each followed by clFinish and host reads) ----
  * A batch of filter / group-by / fused filter+group-by / join+sort queries is

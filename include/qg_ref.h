@@ -116,6 +116,11 @@ QG_API void gatherImpl(qg_buf d_R, int rLen, qg_buf d_loc, qg_buf d_S, int sLen,
 QG_API void scatterImpl(qg_buf d_R, int rLen, qg_buf d_loc, qg_buf d_S, int numThreadPB,
                         int numBlock, qg_ctx *ctx);
 
+/* host/host/testSplit.cpp:156-209 (its kernels are not shipped): records
+ * grouped by partition id y mod numPart, stable; d_bound[p] = first row of p. */
+QG_API void splitImpl(qg_buf d_R, int rLen, int numPart, qg_buf d_S, qg_buf d_bound, int numThreadPB,
+                      int numBlock, int SPLIT_TYPE, qg_ctx *ctx);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,8 @@ def lib() -> ctypes.CDLL:
                                                   c_void_p, c_void_p]),
             "orc_hash_join_ref": (c_int64, [c_void_p, c_int64, c_void_p, c_int64, c_int64, c_void_p]),
             "orc_mlp_forward": (None, [c_void_p, c_void_p, c_int64, c_void_p]),
+            "orc_reduce_rec": (ctypes.c_uint32, [c_void_p, c_int64, c_int]),
+            "orc_split_rec": (None, [c_void_p, c_int64, c_int32, c_void_p, c_void_p]),
             "orc_mlp_grad": (ctypes.c_double, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
         }
         for name, (res, args) in sig.items():
@@ -197,3 +199,16 @@ def mlp_grad(params: np.ndarray, X: np.ndarray, y: np.ndarray):
     g = np.empty(p.size, np.float64)
     loss = lib().orc_mlp_grad(_p(p), _p(x), _p(t), x.shape[0], _p(g))
     return loss, g
+
+
+def reduce_rec(rec: np.ndarray, op: int) -> int:
+    r = np.ascontiguousarray(rec, np.int32)
+    return int(lib().orc_reduce_rec(_p(r), r.shape[0], op))
+
+
+def split_rec(rec: np.ndarray, parts: int):
+    r = np.ascontiguousarray(rec, np.int32)
+    out = np.empty_like(r)
+    bound = np.empty(parts, np.int32)
+    lib().orc_split_rec(_p(r), r.shape[0], parts, _p(out), _p(bound))
+    return out, bound

@@ -578,3 +578,36 @@ ORC_EXPORT double orc_mlp_grad(const float *p, const float *X, const float *y, i
     }
     return loss / (double)n;
 }
+
+/* Whole-column reduce of Record.y as host/host/Validate.cpp:372-468 checks it:
+ * unsigned y, SUM wraps modulo 2^32, MAX/MIN compare unsigned (int
+ * accumulator promoted), AVERAGE = wrapped sum / n.  n >= 1. */
+ORC_EXPORT uint32_t orc_reduce_rec(const uint32_t *rec, int64_t n, int op) {
+    uint32_t acc = rec[1];
+    if (op == 0 || op == 3) {
+        acc = 0;
+        for (int64_t i = 0; i < n; i++) acc += rec[2 * i + 1];
+        if (op == 3) acc = acc / (uint32_t)n;
+        return acc;
+    }
+    for (int64_t i = 1; i < n; i++) {
+        uint32_t y = rec[2 * i + 1];
+        if (op == 1 ? y > acc : y < acc) acc = y;
+    }
+    return acc;
+}
+
+/* Radix split (host/host/testSplit.cpp:156-209; its map kernel is not
+ * shipped): stable counting partition by y mod parts; bound[p] = first row. */
+ORC_EXPORT void orc_split_rec(const uint32_t *rec, int64_t n, int32_t parts, uint32_t *out, int32_t *bound) {
+    int64_t *cnt = (int64_t *)calloc((size_t)parts + 1, sizeof(int64_t));
+    for (int64_t i = 0; i < n; i++) cnt[rec[2 * i + 1] % (uint32_t)parts + 1]++;
+    for (int32_t p = 0; p < parts; p++) cnt[p + 1] += cnt[p];
+    for (int32_t p = 0; p < parts; p++) bound[p] = (int32_t)cnt[p];
+    for (int64_t i = 0; i < n; i++) {
+        int64_t o = cnt[rec[2 * i + 1] % (uint32_t)parts]++;
+        out[2 * o] = rec[2 * i];
+        out[2 * o + 1] = rec[2 * i + 1];
+    }
+    free(cnt);
+}

@@ -75,6 +75,8 @@ SIGNATURES: dict[str, tuple] = {
     "qg_join_set_knobs": (c_int, [c_int, c_int, c_uint32, c_uint32]),
     "qg_join_stats": (c_int, [c_void_p, c_void_p]),
     "qg_part_model_bytes": (c_int64, []),
+    "qg_reduce_rec": (c_int, [c_void_p, c_void_p, c_int64, c_int, POINTER(c_uint32)]),
+    "qg_split_rec": (c_int, [c_void_p, c_void_p, c_int64, c_int32, c_void_p, c_void_p]),
     "qg_mlp_param_count": (c_int64, []),
     "qg_mlp_init": (c_int, [c_void_p, c_void_p, c_uint32]),
     "qg_mlp_predict": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]),
@@ -121,6 +123,7 @@ SIGNATURES.update({
     "CL_agg_avg_afterGroupBy": (None, [c_void_p, _c, c_void_p, _c, c_void_p, c_void_p, _c, _c]),
     "gatherImpl": (None, [QgBuf, _c, QgBuf, QgBuf, _c, _c, _c, c_void_p]),
     "scatterImpl": (None, [QgBuf, _c, QgBuf, QgBuf, _c, _c, c_void_p]),
+    "splitImpl": (None, [QgBuf, _c, _c, QgBuf, QgBuf, _c, _c, _c, c_void_p]),
 })
 
 class Query(ctypes.Structure):

@@ -235,6 +235,22 @@ class Context:
             self.check(st, "qg_join_filter_sort")
             return ok[: m.value], orp[: m.value], osp[: m.value]
 
+    def reduce_rec(self, rec: torch.Tensor, op: int) -> int:
+        """SUM / MAX / MIN / AVERAGE (QG_REDUCE_*) of Record.y, unsigned 32-bit as the reference checks it."""
+        _check_dev(rec)
+        r = ctypes.c_uint32()
+        self.check(self.lib.qg_reduce_rec(self.handle, _ptr(rec), rec.shape[0], op, byref(r)), "qg_reduce_rec")
+        return r.value
+
+    def split_rec(self, rec: torch.Tensor, parts: int):
+        """(records grouped by y mod parts, stable; int32 start of each partition)."""
+        _check_dev(rec)
+        out = torch.empty_like(rec)
+        bound = torch.empty(parts, dtype=torch.int32, device=rec.device)
+        self.check(self.lib.qg_split_rec(self.handle, _ptr(rec), rec.shape[0], parts, _ptr(out), _ptr(bound)),
+                   "qg_split_rec")
+        return out, bound
+
     def join_set_knobs(self, variant: int = 0, buckets_log2: int = 0, bucket_s_max: int = 0,
                        bucket_r_max: int = 0):
         """Join algorithm: 0 auto, 1 radix partitions, 2 learned partitions, 3 hash + sort."""

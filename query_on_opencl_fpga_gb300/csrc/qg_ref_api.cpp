@@ -363,4 +363,17 @@ QG_API void scatterImpl(qg_buf d_R, int rLen, qg_buf d_loc, qg_buf d_S, int numT
         ok(qg_ctx_check(ctx), "scatterImpl", ctx);
 }
 
+// host/host/testSplit.cpp:156-209: d_S gets the records grouped by partition
+// (stable; partition id = y mod numPart), d_bound the first row of each
+// partition.  SPLIT_TYPE chose the reference's (unshipped) map kernel and is
+// accepted and ignored.
+QG_API void splitImpl(qg_buf d_R, int rLen, int numPart, qg_buf d_S, qg_buf d_bound, int numThreadPB,
+                      int numBlock, int SPLIT_TYPE, qg_ctx *ctx) {
+    (void)numThreadPB;
+    (void)numBlock;
+    (void)SPLIT_TYPE;
+    ctx = pick(ctx);
+    ok(qg_split_rec(ctx, d_R.ptr, rLen, numPart, d_S.ptr, (int32_t *)d_bound.ptr), "splitImpl", ctx);
+}
+
 }  // extern "C"
