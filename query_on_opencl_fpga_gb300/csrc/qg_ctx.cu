@@ -37,10 +37,17 @@ QG_API qg_status qg_ctx_create(qg_ctx **out, void *stream) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&ctx->ctl, sizeof(qg_control));
     if (e == cudaSuccess) e = cudaMemset(ctx->ctl, 0, sizeof(qg_control));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->pinned, 8 * sizeof(long long));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->pin_ctl, sizeof(qg_control));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&ctx->pin_bases, 8 * 1024 * sizeof(uint32_t));
+    for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&ctx->pin_ev[i], cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         if (ctx->ctl) cudaFree(ctx->ctl);
         if (ctx->pinned) cudaFreeHost(ctx->pinned);
+        if (ctx->pin_ctl) cudaFreeHost(ctx->pin_ctl);
+        if (ctx->pin_bases) cudaFreeHost(ctx->pin_bases);
+        for (int i = 0; i < 8; i++)
+            if (ctx->pin_ev[i]) cudaEventDestroy(ctx->pin_ev[i]);
         free(ctx);
         return QG_ERR_CUDA;
     }
@@ -64,6 +71,10 @@ QG_API qg_status qg_ctx_destroy(qg_ctx *ctx) {
     if (ctx->aux) cudaFree(ctx->aux);
     if (ctx->ctl) cudaFree(ctx->ctl);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->pin_ctl) cudaFreeHost(ctx->pin_ctl);
+    if (ctx->pin_bases) cudaFreeHost(ctx->pin_bases);
+    for (int i = 0; i < 8; i++)
+        if (ctx->pin_ev[i]) cudaEventDestroy(ctx->pin_ev[i]);
     free(ctx);
     return QG_OK;
 }
@@ -295,6 +306,18 @@ qg_status qg_table(qg_ctx *ctx, size_t bytes, char **out) {
         ctx->table_dirty = false;
     }
     *out = ctx->table;
+    return QG_OK;
+}
+
+qg_status qg_stage_bases(qg_ctx *ctx, const uint32_t *h_bases, uint32_t *d_dst) {
+    const int slot = ctx->pin_next;
+    ctx->pin_next = (slot + 1) & 7;
+    QG_TRY_CUDA(ctx, cudaEventSynchronize(ctx->pin_ev[slot]), "wait bases slot");
+    uint32_t *p = ctx->pin_bases + (size_t)slot * 1024;
+    memcpy(p, h_bases, 1024 * sizeof(uint32_t));
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(d_dst, p, 1024 * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream),
+                "bases h2d");
+    QG_TRY_CUDA(ctx, cudaEventRecord(ctx->pin_ev[slot], ctx->stream), "record bases slot");
     return QG_OK;
 }
 

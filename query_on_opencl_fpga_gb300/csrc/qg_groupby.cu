@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(P2_THREADS)
 k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict__ gsum,
            long long *__restrict__ gcnt, long long cap, unsigned long long *__restrict__ cursor,
            unsigned long long *__restrict__ rec, unsigned int *__restrict__ flags,
-           unsigned int *__restrict__ work) {
+           unsigned int *__restrict__ work, uint32_t *__restrict__ ghist) {
     constexpr int T = 1 << P2_TLOG2;
     constexpr int NB = T / 4;
     constexpr int W = P2_THREADS / 32;
@@ -620,6 +620,7 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
     __shared__ __align__(16) uint32_t tsum[2 * (T + 1)];
     __shared__ uint32_t tc[T + 1];
     __shared__ uint32_t s_part;
+    __shared__ uint32_t dh[4][256];  // key order requested: digit counts of the emitted keys
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int P = 1 << sp.plog2, S = 1 << sp.slog2;
     const uint32_t lt = qg_lanemask_lt();
@@ -653,6 +654,8 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
         gb_acc<SUM64>(&tc[s], &tsum[gb_lo<SUM64>(s)], &tsum[gb_hi<SUM64>(s, T + 1)], cnt, sum);
     };
 
+    if (rec)
+        for (int i = tid; i < 4 * 256; i += P2_THREADS) (&dh[0][0])[i] = 0;
     while (true) {
         __syncthreads();
         if (tid == 0) s_part = atomicAdd(work, 1u);
@@ -705,10 +708,20 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
                     gkey[pos] = (int32_t)tk[s];
                     gsum[pos] = (long long)(((unsigned long long)tsum[gb_hi<SUM64>(s, T + 1)] << 32) | tsum[gb_lo<SUM64>(s)]);
                     gcnt[pos] = (long long)tc[s];
-                    if (rec) rec[pos] = ((unsigned long long)tk[s] << 32) | (unsigned long long)pos;
+                    if (rec) {
+                        const uint32_t k = tk[s];
+                        rec[pos] = ((unsigned long long)k << 32) | (unsigned long long)pos;
+#pragma unroll
+                        for (int d = 0; d < 4; d++) atomicAdd(&dh[d][(k >> (8 * d)) & 255u], 1u);
+                    }
                 }
             }
         }
+    }
+    if (rec) {  // the loop ends for every thread at once (s_part is shared)
+        __syncthreads();
+        for (int i = tid; i < 4 * 256; i += P2_THREADS)
+            if ((&dh[0][0])[i]) atomicAdd(&ghist[i], (&dh[0][0])[i]);
     }
 }
 
@@ -961,12 +974,15 @@ static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_
     QG_TRY(qg_check_launch(ctx, pred ? "k_gb_part_fused" : "k_gb_part"));
     const int g2 = P < ctx->sm_count * 6 ? P : ctx->sm_count * 6;
     qg_pre_launch(ctx);
+    if (o.rec) QG_TRY_CUDA(ctx, cudaMemsetAsync(ctx->ctl->ghist, 0, sizeof(ctx->ctl->ghist), ctx->stream), "memset ghist");
     if (s64)
         k_gb_merge<true><<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
-                                                             (unsigned long long *)d_num, o.rec, d_flags, work);
+                                                             (unsigned long long *)d_num, o.rec, d_flags, work,
+                                                             ctx->ctl->ghist);
     else
         k_gb_merge<false><<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
-                                                              (unsigned long long *)d_num, o.rec, d_flags, work);
+                                                              (unsigned long long *)d_num, o.rec, d_flags, work,
+                                                              ctx->ctl->ghist);
     return qg_check_launch(ctx, "k_gb_merge");
 }
 
@@ -1011,16 +1027,23 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     QG_TRY(gb_outputs(ctx, gkey, gsum, gcnt, cap, order, &o));
     long long g = 0;
     bool global = g_gb_mode == 1;
+    bool have_hist = false;
     if (!global) {
         QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num, flags));
-        // counter[1] (groups) and counter[2] (flags) come back together.
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, d_num, 16, cudaMemcpyDeviceToHost, ctx->stream), "d2h");
+        // One read of the control block brings the error word, the group
+        // count (counter[1]), the overflow flags (counter[2]) and, for key
+        // order, the digit counts of the emitted keys.
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pin_ctl, ctx->ctl, sizeof(qg_control), cudaMemcpyDeviceToHost,
+                                         ctx->stream), "ctl d2h");
         QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-        g = ctx->pinned[0];
-        global = (ctx->pinned[1] & 0xffffffffLL) != 0;
+        if (ctx->pin_ctl->err != 0) return qg_collect_error(ctx);
+        g = (long long)ctx->pin_ctl->counter[1];
+        const unsigned long long fl = ctx->pin_ctl->counter[2];
+        global = (fl & 0xffffffffull) != 0;
+        have_hist = !global && o.rec;
         ctx->gb_stats[0] = global ? 1u : 0u;
-        ctx->gb_stats[1] = (uint32_t)ctx->pinned[1];
-        ctx->gb_stats[2] = (uint32_t)((unsigned long long)ctx->pinned[1] >> 32);
+        ctx->gb_stats[1] = (uint32_t)fl;
+        ctx->gb_stats[2] = (uint32_t)(fl >> 32);
         ctx->gb_stats[3] = g_gb_last_capm;
     } else {
         ctx->gb_stats[0] = 1u;
@@ -1029,14 +1052,25 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     if (global) {
         QG_TRY(gb_launch_global(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num));
         QG_TRY(qg_read_i64(ctx, d_num, &g));
+        QG_TRY(qg_collect_error(ctx));
     }
-    QG_TRY(qg_collect_error(ctx));
     *num_groups = g;
     if (g > cap) return QG_ERR_CAPACITY;
     if (order == QG_ORDER_KEY && g > 1) {
         // Sort (key, index) records, then gather the sums and counts.
         unsigned long long *tmp = (unsigned long long *)(o.c + (cap > 0 ? cap : 1));
-        QG_TRY(qg_sort_rec_inplace(ctx, o.rec, tmp, g));
+        if (have_hist) {  // passes planned from the merge's digit counts: no histogram pass, no sync
+            int passes[4];
+            uint32_t bases[4 * QG_RADIX];
+            const int np = qg_sort_plan(ctx->pin_ctl->ghist, 4, g, passes, bases);
+            qg_sort_bufs A{o.rec, nullptr, nullptr, nullptr}, B{tmp, nullptr, nullptr, nullptr};
+            bool in_b = false;
+            QG_TRY(qg_radix_passes(ctx, false, A, B, g, 0u, passes, np, bases, &in_b));
+            if (in_b)
+                QG_TRY_CUDA(ctx, cudaMemcpyAsync(o.rec, tmp, (size_t)g * 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
+        } else {
+            QG_TRY(qg_sort_rec_inplace(ctx, o.rec, tmp, g));
+        }
         int gb = grid_for(ctx, g, 256, 8);
         qg_pre_launch(ctx);
         k_groupby_gather<<<gb, 256, 0, ctx->stream>>>(o.rec, g, o.s, o.c, gkey, (long long *)gsum,

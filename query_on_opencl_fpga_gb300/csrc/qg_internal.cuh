@@ -17,6 +17,7 @@ struct qg_control {
     uint32_t done_ctr;  // finished CTAs of the running single-pass kernel
     uint32_t pad0;
     unsigned long long counter[6];  // scratch counters (output cursors)
+    uint32_t ghist[4 * 256];        // digit counts of emitted group keys (group-by in key order)
 };
 
 #define QG_MAX_TIMED 4096
@@ -34,6 +35,10 @@ struct qg_ctx {
     size_t lbstat_words;
     qg_control *ctl;        // device
     long long *pinned;      // host pinned readback slots (8)
+    qg_control *pin_ctl;    // host pinned copy of the control block (one read brings error, counters, ghist)
+    uint32_t *pin_bases;    // ring of 8 host pinned 4 KB slots for radix digit bases
+    cudaEvent_t pin_ev[8];  // a slot may be refilled once its copy (event) has completed
+    int pin_next;
     uint32_t spin_limit;
     uint64_t launches;
     bool table_dirty;       // group-by table must be cleared before next use
@@ -75,6 +80,9 @@ qg_status qg_table(qg_ctx *ctx, size_t bytes, char **out);
 // data that could mimic a current-epoch word.
 struct qg_lookback;
 qg_status qg_lb_make(qg_ctx *ctx, int64_t tiles, int site, qg_lookback *out);
+// Upload 4 KB of digit bases to d_dst in stream order without synchronising
+// (through the pinned ring).
+qg_status qg_stage_bases(qg_ctx *ctx, const uint32_t *h_bases, uint32_t *d_dst);
 // Copy a device int64 to host (synchronises the stream).
 qg_status qg_read_i64(qg_ctx *ctx, const long long *d, long long *h);
 qg_status qg_check_launch(qg_ctx *ctx, const char *what);

@@ -304,8 +304,7 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
     uint32_t *dbase = (uint32_t *)scr;
     uint32_t *status = dbase + 4 * QG_RADIX;
     // 4 KB of digit bases, in stream order before the passes that read them.
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(dbase, h_bases, 4 * QG_RADIX * 4, cudaMemcpyHostToDevice, ctx->stream), "bases h2d");
-    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    QG_TRY(qg_stage_bases(ctx, h_bases, dbase));
     const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
     if (kv3) QG_TRY((rs_set_attr<true, false>(ctx)));
     else if (pf.learned) QG_TRY((rs_set_attr<false, true>(ctx)));
