@@ -360,8 +360,16 @@ def operator_lines(ctx, args, peak, stream):
 
     ms, kern, _ = timed(ctx, fstep, steps, 3, 1, stream)
     sel = res["o"].shape[0]
+    # The default column filter is two kernels (count, then write): its
+    # roofline is the operator's algorithmic bytes over their summed launch times.
+    fk = [k for k in ("k_filter_count", "k_filter_write", "k_filter_cols") if kern.get(k, (0, 0.0))[0]]
+    f_ms = sum(kern[k][1] / kern[k][0] for k in fk)
+    f_alg = n * 8 + sel * 8
     out["filter_config0"] = {"rows_per_s": n / (ms * 1e-3), "ms_per_op": ms, "rows": n, "selected": sel,
-                             "roofline": roofline(kern, "k_filter_cols", n * 8 + sel * 8, peak)}
+                             "roofline": {"bound": "hbm", "kernel": "+".join(fk),
+                                          "achieved": f_alg / (f_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                                          "frac": f_alg / (f_ms * 1e-3) / 1e9 / peak, "traffic": None,
+                                          "avg_launch_ms": f_ms, "algorithmic_bytes_per_launch": f_alg}}
     del f, res
     # config 1 unordered variants
     d = datagen.config1_groupby(N_ROWS, GROUPS, seed=0, device="cuda")

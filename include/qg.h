@@ -118,8 +118,10 @@ QG_API qg_status qg_filter_cols_noalloc(const int32_t *key, const int32_t *paylo
                                         int64_t *d_out_n, void *stream);
 
 /* Column filter kernel choice (process-wide): 0 = one 4096-row tile per CTA
- * held in registers, 1 = persistent CTAs streaming tiles through a 3-stage
- * bulk-copy (TMA) ring.  Results are identical. */
+ * held in registers with a decoupled look-back, 1 = persistent CTAs
+ * streaming tiles through a 3-stage bulk-copy (TMA) ring, 2 = two passes
+ * (per-tile counts from the keys, then the writes) with no look-back.
+ * Results are identical. */
 QG_API qg_status qg_filter_set_variant(int variant);
 
 /* ---- scan (ScanLargeArrays/prefixSum/blockAddition, host/host/testScan.cpp:278-340) */

@@ -87,8 +87,8 @@ def test_lookback_timeout_reports_and_recovers(ctx, orc):
     assert np.array_equal(got, orc.filter_rec(rin, 0, 50))
 
 
-@pytest.mark.parametrize("variant", [0, 1])
-@pytest.mark.parametrize("n", [1, 4095, 4099, 300007, 1 << 22])
+@pytest.mark.parametrize("variant", [0, 1, 2])
+@pytest.mark.parametrize("n", [1, 4095, 4099, 300007, 1 << 22, 1048576 + 4096 * 300 + 5])
 def test_filter_cols_variants(ctx, orc, variant, n):
     ctx.check(ctx.lib.qg_filter_set_variant(variant), "variant")
     try:
