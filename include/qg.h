@@ -120,8 +120,8 @@ QG_API qg_status qg_filter_cols_noalloc(const int32_t *key, const int32_t *paylo
 /* Column filter kernel choice (process-wide): 0 = one 4096-row tile per CTA
  * held in registers with a decoupled look-back, 1 = persistent CTAs
  * streaming tiles through a 3-stage bulk-copy (TMA) ring, 2 = two passes
- * (per-tile counts from the keys, then the writes) with no look-back.
- * Results are identical. */
+ * (per-tile counts from the keys, then the writes) with no look-back, the
+ * default.  Results are identical. */
 QG_API qg_status qg_filter_set_variant(int variant);
 
 /* ---- scan (ScanLargeArrays/prefixSum/blockAddition, host/host/testScan.cpp:278-340) */
@@ -251,7 +251,7 @@ QG_API qg_status qg_split_rec(qg_ctx *ctx, const void *in_records, int64_t n, in
 typedef enum { QG_OP_FILTER = 0, QG_OP_GROUPBY = 1, QG_OP_FUSED = 2, QG_OP_JOIN = 3 } qg_op;
 typedef struct {
     int op;                /* qg_op */
-    int variant;           /* -1 default; filter 0 or 1; group-by 0 two-pass, 1 global table, 2 two-pass 64-bit adds */
+    int variant;           /* -1 default; filter 0, 1 or 2 (default 2); group-by 0 two-pass (default), 1 global table, 2 two-pass 64-bit adds */
     int64_t n;             /* rows (join: S rows) */
     int64_t n2;            /* join: R rows */
     const int32_t *in[4];  /* filter: key, payload; group-by: key, value, value2 (fused); join: rkey, rpay, skey, spay */

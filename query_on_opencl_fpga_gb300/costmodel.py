@@ -5,7 +5,7 @@ The reference plans with a static table of per-variant unit costs for FPGA
 images (host/dynamic_programming.cpp:152-167).  On the GPU each operator has
 several bit-identical kernel variants whose speed depends on the input:
 
-  filter   0 one tile per CTA (registers), 1 persistent CTAs with a bulk-copy ring
+  filter   0 one tile per CTA with look-back, 1 persistent CTAs with a bulk-copy ring, 2 two passes (count, write)
   groupby  0 two-pass shared-memory tables (carry sums), 1 global hash table, 2 two-pass with 64-bit shared adds
   fused    as groupby, with the value2 predicate
   join     0 auto partition, 1 radix partition, 2 learned partition, 3 global hash table + radix sort
@@ -14,7 +14,7 @@ several bit-identical kernel variants whose speed depends on the input:
 per-launch event log (Context.timing_span); `train` fits the 16 -> 64 -> 1
 MLP on the GPU with the library's forward/backward/Adam kernels (qg_mlp.cu)
 to predict log(ms); `choose` picks the variant with the lowest prediction.
-Without a model the engine's default variants (index 0) are used.
+Without a model the engine's default variants (DEFAULT_VARIANT) are used.
 
   python -m query_on_opencl_fpga_gb300.costmodel collect --out costlog.json
 """
@@ -28,8 +28,8 @@ import sys
 import torch
 
 OPS = ("filter", "groupby", "fused", "join")
-VARIANTS = {"filter": (0, 1), "groupby": (0, 1, 2), "fused": (0, 1, 2), "join": (0, 1, 2, 3)}
-DEFAULT_VARIANT = {"filter": 0, "groupby": 0, "fused": 0, "join": 0}
+VARIANTS = {"filter": (0, 1, 2), "groupby": (0, 1, 2), "fused": (0, 1, 2), "join": (0, 1, 2, 3)}
+DEFAULT_VARIANT = {"filter": 2, "groupby": 0, "fused": 0, "join": 0}
 NFEAT = 16
 
 
@@ -84,7 +84,7 @@ def _set_variant(ctx, op: str, v: int) -> None:
 
 
 def _reset_variants(ctx) -> None:
-    ctx.lib.qg_filter_set_variant(0)
+    ctx.lib.qg_filter_set_variant(DEFAULT_VARIANT["filter"])
     ctx.lib.qg_groupby_set_knobs(0, 13, 0, 0)
     ctx.join_set_knobs(0)
 

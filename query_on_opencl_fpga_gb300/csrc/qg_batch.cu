@@ -45,7 +45,7 @@ qg_status enqueue(qg_batch *b, const BatchCfg &c) {
     qg_ctx *ctx = b->own;
     qg_status st = QG_OK;
     for (const qg_query &q : b->q) {
-        const int v = q.variant < 0 ? 0 : q.variant;
+        const int v = q.variant >= 0 ? q.variant : (q.op == QG_OP_FILTER ? 2 : 0);  // the operators' defaults
         switch (q.op) {
         case QG_OP_FILTER:
             st = qg_filter_set_variant(v);
@@ -72,7 +72,7 @@ qg_status enqueue(qg_batch *b, const BatchCfg &c) {
         }
         if (st != QG_OK) break;
     }
-    qg_filter_set_variant(0);
+    qg_filter_set_variant(2);
     qg_groupby_set_knobs(0, 13, 0, 0);
     qg_join_set_table_factor(2);
     return st;

@@ -97,4 +97,4 @@ def test_filter_cols_variants(ctx, orc, variant, n):
         got = ctx.filter_cols(dev(key), dev(pay), d["lo"], d["hi"]).cpu().numpy()
         assert np.array_equal(got, orc.filter_cols(key, pay, d["lo"], d["hi"]))
     finally:
-        ctx.lib.qg_filter_set_variant(0)
+        ctx.lib.qg_filter_set_variant(2)  # the default
