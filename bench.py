@@ -281,38 +281,60 @@ def run_ours(args, rank, world, local):
     roof_other = {n: roofline(kern, n, b, peak) for n, b in names.items()}
     kern_avg = {k: {"launches": c, "avg_ms": t / c} for k, (c, t) in kern.items() if c}
 
-    # e2e through the public API: pinned host inputs in, results out, every step
+    # e2e through the public API: every step copies its inputs from pinned
+    # host memory and reads its results back into pinned host memory.  The
+    # input copies run on a second stream into two alternating device
+    # buffers, so that step i+1's inputs arrive while step i computes (how a
+    # pipelined caller uses the API); the timed region holds all of it.
     hkey = key.cpu().pin_memory()
     hval = val.cpu().pin_memory()
     hval2 = val2.cpu().pin_memory()
-    dkey, dval, dval2 = torch.empty_like(key), torch.empty_like(val), torch.empty_like(val2)
-    out_bytes = [0]
+    dev_in = [(torch.empty_like(key), torch.empty_like(val), torch.empty_like(val2)) for _ in range(2)]
+    copy_streams = [torch.cuda.Stream() for _ in range(3)]  # one per column: several copy engines at once
+    ready = [[torch.cuda.Event() for _ in range(3)] for _ in range(2)]
+    free = [torch.cuda.Event(), torch.cuda.Event()]
+    hres = [[torch.empty(cap, dtype=dt).pin_memory() for dt in (torch.int32, torch.int64, torch.int64)]
+            for _ in range(2)]
 
-    def e2e_step():
-        dkey.copy_(hkey, non_blocking=True)
-        dval.copy_(hval, non_blocking=True)
-        dval2.copy_(hval2, non_blocking=True)
-        r1 = ctx.groupby_cols(dkey, dval, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
-        r2 = ctx.groupby_cols(dkey, dval, dval2, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+    def load(slot):
+        for cs, ev, d, h in zip(copy_streams, ready[slot], dev_in[slot], (hkey, hval, hval2)):
+            with torch.cuda.stream(cs):
+                cs.wait_event(free[slot])  # the slot's previous step has finished with it
+                d.copy_(h, non_blocking=True)
+                ev.record(cs)
+
+    def e2e_run(k):
         nb = 0
-        for t in (*r1, *r2):
-            h = t.cpu()
-            nb += h.numel() * h.element_size()
-        out_bytes[0] = nb
+        load(0)
+        for i in range(k):
+            s = i % 2
+            if i + 1 < k:
+                load(1 - s)
+            for ev in ready[s]:
+                stream.wait_event(ev)
+            dk, dv, dv2 = dev_in[s]
+            r1 = ctx.groupby_cols(dk, dv, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+            r2 = ctx.groupby_cols(dk, dv, dv2, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+            free[s].record(stream)
+            for r, hb in zip((r1, r2), hres):
+                for t, h in zip(r, hb):
+                    h[: t.numel()].copy_(t, non_blocking=True)
+                    nb += t.numel() * t.element_size()
+        torch.cuda.synchronize()
+        return nb // k
 
     e2e_steps = max(3, min(args.steps, 10))
-    for _ in range(2):
-        e2e_step()
+    e2e_run(2)
     torch.cuda.synchronize()
     barrier(world)
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        e2e_step()
-    torch.cuda.synchronize()
+    d2h = e2e_run(e2e_steps)
     barrier(world)
     e2e_ms = max_over_ranks((time.perf_counter() - t0) / e2e_steps * 1e3, world)
     e2e = {"value": rows_per_step * world / (e2e_ms * 1e-3), "unit": "rows/s",
-           "h2d_bytes_per_step": 3 * N_ROWS * 4, "d2h_bytes_per_step": out_bytes[0], "ms_per_step": e2e_ms}
+           "h2d_bytes_per_step": 3 * N_ROWS * 4, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+           "note": "inputs copied from pinned host memory on copy streams (one per column; the next step's "
+                   "copies overlap this step's compute); results copied to pinned host memory"}
 
     ops = {}
     if not args.no_operators and rank == 0:
