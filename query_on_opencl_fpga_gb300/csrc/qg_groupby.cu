@@ -472,6 +472,7 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
           unsigned int *__restrict__ flags) {
     extern __shared__ __align__(16) unsigned char p1_raw[];
     __shared__ uint32_t wsum[32];
+    __shared__ uint32_t s_max;
     const int S = 1 << sp.slog2, P = 1 << sp.plog2;
     const int blog2 = sp.slog2 - 2;
     const uint32_t bshift = 32 - blog2, pshift = 32 - blog2 - sp.plog2, pmask = (uint32_t)P - 1;
@@ -490,6 +491,7 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
     }
     for (int i = tid; i < P; i += P1_THREADS) cur[i] = 0;
     for (int i = tid; i < GB_SKETCH_WORDS; i += P1_THREADS) sk[i] = 0;
+    if (tid == 0) s_max = 0;
     __syncthreads();
     const int c = blockIdx.x, C = gridDim.x;
     uint2 *mine = sp.miss + (size_t)c * P * capm;
@@ -578,12 +580,19 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
         }
     }
     __syncthreads();
+    // Fullest bucket (for qg_groupby_stats): reduced in the CTA, then one
+    // global atomic per CTA -- a global atomic per bucket would put ~10^5
+    // atomics on one address at the kernel's end.
+    uint32_t mx = 0;
     for (int p = tid; p < P; p += P1_THREADS) {
-        atomicMax(flags + 1, cur[p]);  // fullest bucket, for qg_groupby_stats
+        mx = max(mx, cur[p]);
         sp.mcnt[(size_t)p * GB_MAX_C + c] = min(cur[p], capm);
         cur[p] = 0;
     }
+    mx = __reduce_max_sync(QG_FULL_MASK, mx);
+    if ((tid & 31) == 0 && mx) atomicMax(&s_max, mx);
     __syncthreads();
+    if (tid == 0 && s_max) atomicMax(flags + 1, s_max);
     // Counting sort of the shared-memory table by partition.
     for (int s = tid; s < S; s += P1_THREADS)
         if (hc[s]) atomicAdd(&cur[(gb_h1(hk[s]) >> pshift) & pmask], 1u);
@@ -620,6 +629,8 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
     __shared__ __align__(16) uint32_t tsum[2 * (T + 1)];
     __shared__ uint32_t tc[T + 1];
     __shared__ uint32_t s_part;
+    __shared__ uint32_t s_wc[P2_THREADS / 32];
+    __shared__ unsigned long long s_base;
     __shared__ uint32_t dh[4][256];  // key order requested: digit counts of the emitted keys
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int P = 1 << sp.plog2, S = 1 << sp.slog2;
@@ -695,15 +706,34 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
             }
         }
         __syncthreads();
+        // The partition's groups take one range of the output: count them per
+        // warp, reserve the range with one global atomic, emit.
+        uint32_t wc = 0;
+        for (int base = 0; base <= T; base += P2_THREADS) {
+            const int s = base + tid;
+            wc += __popc(__ballot_sync(QG_FULL_MASK, (s <= T) && tc[s] != 0));
+        }
+        if (lane == 0) s_wc[warp] = wc;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t t = 0;
+            for (int w = 0; w < P2_THREADS / 32; w++) {
+                const uint32_t x = s_wc[w];
+                s_wc[w] = t;
+                t += x;
+            }
+            s_base = t ? atomicAdd(cursor, (unsigned long long)t) : 0ull;
+        }
+        __syncthreads();
+        unsigned long long o = s_base + s_wc[warp];
         for (int base = 0; base <= T; base += P2_THREADS) {
             const int s = base + tid;
             const bool occ = (s <= T) && tc[s] != 0;
             const uint32_t b = __ballot_sync(QG_FULL_MASK, occ);
-            unsigned long long o = 0;
-            if (lane == 0 && b) o = atomicAdd(cursor, (unsigned long long)__popc(b));
-            o = __shfl_sync(QG_FULL_MASK, o, 0);
+            const unsigned long long o_here = o;
+            o += __popc(b);
             if (occ) {
-                const long long pos = (long long)o + __popc(b & lt);
+                const long long pos = (long long)o_here + __popc(b & lt);
                 if (pos < cap) {
                     gkey[pos] = (int32_t)tk[s];
                     gsum[pos] = (long long)(((unsigned long long)tsum[gb_hi<SUM64>(s, T + 1)] << 32) | tsum[gb_lo<SUM64>(s)]);
