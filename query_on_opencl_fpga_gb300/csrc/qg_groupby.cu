@@ -285,7 +285,11 @@ __global__ void __launch_bounds__(256)
 k_groupby_emit(GSlot *__restrict__ tab, long long nslots, int32_t *__restrict__ gkey,
                long long *__restrict__ gsum, long long *__restrict__ gcnt, long long cap,
                unsigned long long *__restrict__ cursor, unsigned long long *__restrict__ rec) {
-    const int lane = threadIdx.x & 31;
+    // One output reservation per CTA and round (not per warp): the cursor is
+    // a single global word.
+    __shared__ uint32_t s_wc[8];
+    __shared__ unsigned long long s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t lt = qg_lanemask_lt();
     long long stride = (long long)gridDim.x * blockDim.x;
     long long start = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -299,9 +303,20 @@ k_groupby_emit(GSlot *__restrict__ tab, long long nslots, int32_t *__restrict__ 
             occ = e.tag != 0;
         }
         uint32_t b = __ballot_sync(QG_FULL_MASK, occ);
-        unsigned long long basepos = 0;
-        if (lane == 0 && b) basepos = atomicAdd(cursor, (unsigned long long)__popc(b));
-        basepos = __shfl_sync(QG_FULL_MASK, basepos, 0);
+        if (lane == 0) s_wc[warp] = __popc(b);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int w = 0; w < 8; w++) {
+                const uint32_t x = s_wc[w];
+                s_wc[w] = t;
+                t += x;
+            }
+            s_base = t ? atomicAdd(cursor, (unsigned long long)t) : 0ull;
+        }
+        __syncthreads();
+        const unsigned long long basepos = s_base + s_wc[warp];
+        __syncthreads();  // s_wc and s_base are rewritten next round
         if (occ) {
             long long pos = (long long)basepos + __popc(b & lt);
             if (pos < cap) {
