@@ -168,7 +168,11 @@ QG_API qg_status qg_scatter_rec(qg_ctx *ctx, const void *R, int64_t rLen, const 
  * filter_aggregation pipeline, kernel/filter_aggregation/
  * filter_aggregation_cu_op_dp.cl).  Outputs hold `cap` groups; order is
  * QG_ORDER_KEY (ascending unsigned key, the reference's sorted order) or
- * QG_ORDER_NONE. */
+ * QG_ORDER_NONE.
+ * qg_groupby_cols_async is the same without a host round trip: the group
+ * count goes to device memory (*d_num_groups); key order is sorted on the
+ * device (two-pass path, cap < 2^30); a spill overflow is reported by
+ * qg_ctx_check as QG_ERR_TABLE_FULL instead of being redone. */
 QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, const int32_t *val,
                                  const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
                                  int32_t *gkey, int64_t *gsum, int64_t *gcount, int64_t cap,

@@ -333,10 +333,12 @@ k_groupby_emit(GSlot *__restrict__ tab, long long nslots, int32_t *__restrict__ 
 }
 
 // Gather the key-sorted order: rec[i] = {x = old index, y = key}.
+// With d_n set, the count is min(g, *d_n), read on the device.
 __global__ void k_groupby_gather(const unsigned long long *__restrict__ rec, long long g,
                                  const long long *__restrict__ tsum, const long long *__restrict__ tcnt,
                                  int32_t *__restrict__ gkey, long long *__restrict__ gsum,
-                                 long long *__restrict__ gcnt) {
+                                 long long *__restrict__ gcnt, const long long *__restrict__ d_n) {
+    if (d_n && *d_n < g) g = *d_n;
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g; i += stride) {
         unsigned long long r = rec[i];
@@ -1035,13 +1037,38 @@ __global__ void k_gb_flags_to_error(const unsigned int *flags, qg_control *ctl) 
     if (*flags) qg_record_error(ctl, QG_ERR_TABLE_FULL, QG_SITE_GROUPBY);
 }
 
+// Key order for the two-pass path, planned on the device: the merge counted
+// the digits of the keys it wrote (ctl->ghist) and the group count is in
+// d_num, so four stable passes over (key, index) records and the gather run
+// without a host round trip.  Records past cap were never written, and both
+// the passes and the gather stop at min(count, cap).
+static qg_status gb_key_order_dev(qg_ctx *ctx, const GbOut &o, int64_t cap, long long *d_num,
+                                  int32_t *gkey, int64_t *gsum, int64_t *gcnt) {
+    if (cap <= 0) return QG_OK;
+    unsigned long long *tmp = o.rec + 3 * cap;  // the aux arena's sort ping-pong (gb_outputs)
+    char *work;
+    QG_TRY(qg_scratch(ctx, qg_radix_dev_work_bytes(cap), &work));
+    qg_sort_bufs A{o.rec, nullptr, nullptr, nullptr}, B{tmp, nullptr, nullptr, nullptr};
+    bool in_b = false;
+    QG_TRY(qg_radix_passes_dev(ctx, false, A, B, cap, (const unsigned long long *)d_num, ctx->ctl->ghist, 4, 0u,
+                               work, &in_b));
+    if (in_b) return QG_ERR_INVALID;  // four passes end where they began
+    const int gb = grid_for(ctx, cap, 256, 8);
+    qg_pre_launch(ctx);
+    k_groupby_gather<<<gb, 256, 0, ctx->stream>>>(o.rec, cap, o.s, o.c, gkey, (long long *)gsum,
+                                                  (long long *)gcnt, d_num);
+    return qg_check_launch(ctx, "k_groupby_gather");
+}
+
 extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key,
                                                   const int32_t *val, const int32_t *val2,
                                                   int32_t lo2, int32_t hi2, int64_t n,
                                                   int32_t *gkey, int64_t *gsum, int64_t *gcnt,
                                                   int64_t cap, int order, int64_t *d_num) {
     if (!ctx || n < 0 || cap < 0 || !d_num || (n > 0 && (!key || !val))) return QG_ERR_INVALID;
-    if (order != QG_ORDER_NONE) return QG_ERR_UNSUPPORTED;  // key order needs the synchronous form
+    if (order != QG_ORDER_NONE && order != QG_ORDER_KEY) return QG_ERR_INVALID;
+    // key order is planned on the device by the two-pass path only
+    if (order == QG_ORDER_KEY && (g_gb_mode == 1 || cap >= (1LL << 30))) return QG_ERR_UNSUPPORTED;
     if ((((uintptr_t)key) | ((uintptr_t)val) | ((uintptr_t)val2)) & 15) return QG_ERR_INVALID;
     if (n >= (1LL << 32)) return QG_ERR_UNSUPPORTED;
     GbOut o;
@@ -1050,6 +1077,7 @@ extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *ke
         return gb_launch_global(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num);
     unsigned int *flags = (unsigned int *)&ctx->ctl->counter[2];
     QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num, flags));
+    if (o.rec) QG_TRY(gb_key_order_dev(ctx, o, cap, (long long *)d_num, gkey, gsum, gcnt));
     // An overflow cannot be redone without a host round trip here: report it
     // through the error word (qg_ctx_check returns QG_ERR_TABLE_FULL).
     k_gb_flags_to_error<<<1, 1, 0, ctx->stream>>>(flags, ctx->ctl);
@@ -1072,20 +1100,24 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     QG_TRY(gb_outputs(ctx, gkey, gsum, gcnt, cap, order, &o));
     long long g = 0;
     bool global = g_gb_mode == 1;
-    bool have_hist = false;
+    bool done = false;  // the two-pass path wrote the final output (any order)
+    // The device-planned sort takes up to 2^30 records; beyond that the key
+    // order is sorted after the host has read the count.
+    const bool dev_order = o.rec && cap < (1LL << 30);
     if (!global) {
         QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num, flags));
-        // One read of the control block brings the error word, the group
-        // count (counter[1]), the overflow flags (counter[2]) and, for key
-        // order, the digit counts of the emitted keys.
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pin_ctl, ctx->ctl, sizeof(qg_control), cudaMemcpyDeviceToHost,
-                                         ctx->stream), "ctl d2h");
+        if (dev_order) QG_TRY(gb_key_order_dev(ctx, o, cap, d_num, gkey, gsum, gcnt));
+        // One read of the control block, at the end, brings the error word,
+        // the group count (counter[1]) and the overflow flags (counter[2]).
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pin_ctl, ctx->ctl, offsetof(qg_control, ghist),
+                                         cudaMemcpyDeviceToHost, ctx->stream),
+                    "ctl d2h");
         QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
         if (ctx->pin_ctl->err != 0) return qg_collect_error(ctx);
         g = (long long)ctx->pin_ctl->counter[1];
         const unsigned long long fl = ctx->pin_ctl->counter[2];
         global = (fl & 0xffffffffull) != 0;
-        have_hist = !global && o.rec;
+        done = !global && (!o.rec || dev_order);
         ctx->gb_stats[0] = global ? 1u : 0u;
         ctx->gb_stats[1] = (uint32_t)fl;
         ctx->gb_stats[2] = (uint32_t)(fl >> 32);
@@ -1101,25 +1133,16 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     }
     *num_groups = g;
     if (g > cap) return QG_ERR_CAPACITY;
+    if (done) return QG_OK;
     if (order == QG_ORDER_KEY && g > 1) {
-        // Sort (key, index) records, then gather the sums and counts.
+        // Global-table path (or a very large cap): sort (key, index) records,
+        // then gather the sums and counts.
         unsigned long long *tmp = (unsigned long long *)(o.c + (cap > 0 ? cap : 1));
-        if (have_hist) {  // passes planned from the merge's digit counts: no histogram pass, no sync
-            int passes[4];
-            uint32_t bases[4 * QG_RADIX];
-            const int np = qg_sort_plan(ctx->pin_ctl->ghist, 4, g, passes, bases);
-            qg_sort_bufs A{o.rec, nullptr, nullptr, nullptr}, B{tmp, nullptr, nullptr, nullptr};
-            bool in_b = false;
-            QG_TRY(qg_radix_passes(ctx, false, A, B, g, 0u, passes, np, bases, &in_b));
-            if (in_b)
-                QG_TRY_CUDA(ctx, cudaMemcpyAsync(o.rec, tmp, (size_t)g * 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
-        } else {
-            QG_TRY(qg_sort_rec_inplace(ctx, o.rec, tmp, g));
-        }
+        QG_TRY(qg_sort_rec_inplace(ctx, o.rec, tmp, g));
         int gb = grid_for(ctx, g, 256, 8);
         qg_pre_launch(ctx);
         k_groupby_gather<<<gb, 256, 0, ctx->stream>>>(o.rec, g, o.s, o.c, gkey, (long long *)gsum,
-                                                      (long long *)gcnt);
+                                                      (long long *)gcnt, nullptr);
         QG_TRY(qg_check_launch(ctx, "k_groupby_gather"));
         return qg_ctx_check(ctx);
     } else if (order == QG_ORDER_KEY && g == 1) {

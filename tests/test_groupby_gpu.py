@@ -168,6 +168,27 @@ def test_groupby_async_overflow_reports_table_full(ctx, knobs):
     assert e.value.status == 4
 
 
+@pytest.mark.parametrize("n,groups,fused", [(1, 1, False), (5000, 37, True), (1 << 19, 1 << 16, False)])
+def test_groupby_async_key_order(ctx, orc, n, groups, fused):
+    # The sync-free form sorts by key on the device (digit counts from the merge,
+    # group count read by the kernels); the count comes back in d_num.
+    from ctypes import c_void_p
+
+    d = datagen.config1_groupby(n, groups, seed=n + 3)
+    key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
+    cap = 2 * groups
+    k, v, w = dev(key), dev(val), dev(val2)
+    out = [torch.empty(cap, dtype=t, device="cuda") for t in (torch.int32, torch.int64, torch.int64)]
+    d_num = torch.zeros(1, dtype=torch.int64, device="cuda")
+    p = lambda t: c_void_p(t.data_ptr())  # noqa: E731
+    st = ctx.lib.qg_groupby_cols_async(ctx.handle, p(k), p(v), p(w) if fused else c_void_p(0), d["lo2"], d["hi2"],
+                                       n, p(out[0]), p(out[1]), p(out[2]), cap, QG_ORDER_KEY, p(d_num))
+    assert st == 0
+    ctx.device_check()
+    g = int(d_num.item())
+    check_groups([t[:g] for t in out], orc.groupby_cols(key, val, val2 if fused else None, d["lo2"], d["hi2"]))
+
+
 @pytest.mark.parametrize("mode", [0, 2])
 @pytest.mark.parametrize("hot,parts", [(8, 1), (10, 6), (13, 12), (13, 13)])
 def test_groupby_knob_sweep(ctx, orc, knobs, hot, parts, mode):
