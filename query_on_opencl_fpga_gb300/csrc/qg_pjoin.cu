@@ -73,24 +73,27 @@ k_pj_rrec(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
 }
 
 // ---------------------------------------------------------------------------
-// 2. S filter + range test, compacted into S' records (stable)
+// 2. S filter + range test, compacted into S' records
 // ---------------------------------------------------------------------------
 constexpr int SF_THREADS = 256;
 constexpr int SF_WARPS = SF_THREADS / 32;
 constexpr int SF_ROUNDS = 4;  // int4 of keys + int4 of payloads per round: 4096 rows per tile
-constexpr int SF_LB_WARPS = 4;
 
-__global__ void __launch_bounds__(SF_THREADS, 5)
+// S-filter without input order: S' is repartitioned by key right after, and
+// the join leaves the order among equal keys unspecified, so a tile takes
+// its output range with one atomic on the S' counter instead of a look-back
+// over earlier tiles.  R's key range is read from device memory (no host
+// round trip before the launch).
+__global__ void __launch_bounds__(SF_THREADS, 4)
 k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay, long long n,
-             int32_t slo, int32_t shi, uint32_t kmin, uint32_t kmax,
-             unsigned long long *__restrict__ out, long long *__restrict__ d_count, qg_lookback lb) {
+               int32_t slo, int32_t shi, const PjRange *__restrict__ range,
+               unsigned long long *__restrict__ out, unsigned long long *__restrict__ cursor,
+               qg_control *ctl) {
     constexpr int TILE = SF_THREADS * SF_ROUNDS * 4;
-    __shared__ uint32_t s_tile, s_epoch, s_excl;
     __shared__ uint32_t s_woff[SF_ROUNDS * SF_WARPS];
-    __shared__ uint32_t s_tmp[2 * SF_LB_WARPS + 1];
-    const uint32_t tile = blockIdx.x;
+    __shared__ unsigned long long s_base;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long base = (long long)tile * TILE;
+    const long long base = (long long)blockIdx.x * TILE;
     const uint32_t lt = qg_lanemask_lt();
     int4 kv[SF_ROUNDS], pv[SF_ROUNDS];
 #pragma unroll
@@ -107,7 +110,7 @@ k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
             pv[r] = make_int4(p[0], p[1], p[2], p[3]);
         }
     }
-    qg_lb_begin(lb, &s_tile, &s_epoch);  // epoch read while the loads are in flight
+    const uint32_t kmin = range->kmin, kmax = range->kmax;
     uint32_t fl = 0, lpre[SF_ROUNDS];
 #pragma unroll
     for (int r = 0; r < SF_ROUNDS; r++) {
@@ -131,24 +134,36 @@ k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
         if (lane == 0) s_woff[r * SF_WARPS + warp] = tot;
         fl |= f << (4 * r);
     }
-    qg_tile_offsets_wide<SF_ROUNDS * SF_WARPS, SF_LB_WARPS>(s_woff, lb, tile, s_epoch, &s_excl, s_tmp,
-                                                           d_count, gridDim.x - 1);
-    const uint32_t excl = s_excl;  // n < 2^30 rows on this path
+    __syncthreads();
+    if (warp == 0) {  // exclusive offsets of the tile's (round, warp) pieces; one atomic for the tile
+        const uint32_t x = s_woff[lane];  // SF_ROUNDS * SF_WARPS == 32
+        uint32_t inc = x;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(QG_FULL_MASK, inc, d);
+            if (lane >= d) inc += y;
+        }
+        s_woff[lane] = inc - x;
+        if (lane == 31) s_base = inc ? atomicAdd(cursor, (unsigned long long)inc) : 0ull;
+    }
+    __syncthreads();
+    const unsigned long long tb = s_base;
 #pragma unroll
     for (int r = 0; r < SF_ROUNDS; r++) {
-        uint32_t pos = excl + s_woff[r * SF_WARPS + warp] + lpre[r];
+        unsigned long long pos = tb + s_woff[r * SF_WARPS + warp] + lpre[r];
         const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
         const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
 #pragma unroll
         for (int j = 0; j < 4; j++)
             if ((fl >> (4 * r + j)) & 1u) {
-                if (pos < n) out[pos] = ((unsigned long long)(uint32_t)kk[j] << 32) | (uint32_t)pp[j];
-                else qg_record_error(lb.ctl, QG_ERR_INVALID, QG_SITE_PJ_FILTER);
+                if (pos < (unsigned long long)n) out[pos] = ((unsigned long long)(uint32_t)kk[j] << 32) | (uint32_t)pp[j];
+                else qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_FILTER);
                 pos++;
             }
     }
-    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
 }
+static_assert(SF_ROUNDS * SF_WARPS == 32, "one warp scans the tile's pieces");
+
 
 // ---------------------------------------------------------------------------
 // 3. digit histograms of the bucket id, bucket bounds, CDF sample and fit
@@ -1168,19 +1183,17 @@ extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey
     qg_pre_launch(ctx);
     k_pj_rrec<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, R, range);
     QG_TRY(qg_check_launch(ctx, "k_pj_rrec"));
+    constexpr int SF_TILE = SF_THREADS * SF_ROUNDS * 4;
+    const long long tiles = (nS + SF_TILE - 1) / SF_TILE;
+    qg_pre_launch(ctx);
+    k_pj_sfilter<<<(unsigned)tiles, SF_THREADS, 0, ctx->stream>>>(skey, spay, nS, slo, shi, range, S,
+                                                                   &range->count, ctx->ctl);
+    QG_TRY(qg_check_launch(ctx, "k_pj_sfilter"));
+    // one read brings R's key range and the S' count
     PjRange hr;
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(&hr, range, sizeof(hr), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-    constexpr int SF_TILE = SF_THREADS * SF_ROUNDS * 4;
-    const long long tiles = (nS + SF_TILE - 1) / SF_TILE;
-    qg_lookback lbs;
-    QG_TRY(qg_lb_make(ctx, tiles, QG_SITE_FILTER, &lbs));
-    qg_pre_launch(ctx);
-    k_pj_sfilter<<<(unsigned)tiles, SF_THREADS, 0, ctx->stream>>>(skey, spay, nS, slo, shi, hr.kmin, hr.kmax, S,
-                                                                 (long long *)&range->count, lbs);
-    QG_TRY(qg_check_launch(ctx, "k_pj_sfilter"));
-    long long ns1 = 0;
-    QG_TRY(qg_read_i64(ctx, (const long long *)&range->count, &ns1));
+    const long long ns1 = (long long)hr.count;
     QG_TRY(qg_collect_error(ctx));
     long long M = 0;
     QG_TRY(pj_core(ctx, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, g_pj_variant, (uint32_t *)out_key,
