@@ -420,6 +420,7 @@ constexpr int PB_HEADS_LOG2 = 12;
 constexpr int PB_HEADS = 1 << PB_HEADS_LOG2;
 constexpr int PB_CSPAN = 8192;  // widest key span that is counting-sorted
 constexpr int PB_IPT = PB_SMAX / PB_THREADS;
+constexpr int PB_WSEG = PB_SMAX / PB_WARPS;  // sorted S' rows probed by one warp
 
 struct PbSmem {
     unsigned long long s[PB_SMAX];  // the bucket's S' rows (key << 32 | S.payload), sorted by key
@@ -489,7 +490,7 @@ k_pj_join(PbArgs a, qg_lookback lb) {
         work = false;
     }
     uint32_t my_cnt = 0;      // matches of this thread's rows
-    uint32_t q = 0, r0 = 0;   // this thread's block of sorted rows
+    uint32_t q = 0, r0 = 0;   // this warp's segment of sorted rows
     if (work) {
         // R rows -> chained table
         for (uint32_t i = tid; i < PB_HEADS; i += PB_THREADS) S.head[i] = 0;
@@ -581,17 +582,21 @@ k_pj_join(PbArgs a, qg_lookback lb) {
             }
         }
         __syncthreads();
-        // probe: thread t owns sorted rows [r0, r0 + q)
-        const uint32_t qq = (sn + PB_THREADS - 1) / PB_THREADS;
-        r0 = min(sn, tid * qq);
-        q = min(sn, r0 + qq) - r0;
-        for (uint32_t r = r0; r < r0 + q; r++) {
+        // probe: warp w owns sorted rows [w * PB_WSEG, (w + 1) * PB_WSEG), taken
+        // 32 at a time (lane L has row step * 32 + L), so that the matches of
+        // a step are consecutive in the output and their stores coalesce
+        r0 = min(sn, (uint32_t)warp * PB_WSEG);
+        q = min(sn, r0 + PB_WSEG) - r0;
+        for (uint32_t r = r0 + lane; r < r0 + q; r += 32) {
             const uint32_t k = (uint32_t)(S.s[r] >> 32);
             for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) my_cnt += (S.rk[e - 1] == k);
         }
     }
+    // warp totals -> warp offsets within the bucket
+    const uint32_t wcnt = __reduce_add_sync(QG_FULL_MASK, my_cnt);
     uint32_t total;
-    const uint32_t my_off = pb_excl(my_cnt, S.wsum, &total);
+    const uint32_t my_off = pb_excl(lane == 0 ? wcnt : 0u, S.wsum, &total);  // lane 0 holds its warp's offset
+    const uint32_t warp_off = __shfl_sync(QG_FULL_MASK, my_off, 0);
     const uint32_t bucket_cnt = outside ? (uint32_t)a.bigcnt[b] : total;
     if (warp == 0) {
         const uint32_t excl = qg_lb_warp_exclusive(lb, b, S.epoch, bucket_cnt);
@@ -602,20 +607,44 @@ k_pj_join(PbArgs a, qg_lookback lb) {
         }
     }
     __syncthreads();
-    if (work && my_cnt) {
-        long long o = (long long)S.excl + my_off;
-        for (uint32_t r = r0; r < r0 + q; r++) {
-            const unsigned long long v = S.s[r];
-            const uint32_t k = (uint32_t)(v >> 32);
-            for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) {
-                if (S.rk[e - 1] != k) continue;
-                if (o < a.cap) {
-                    a.out_k[o] = k;
-                    a.out_a[o] = S.rp[e - 1];
-                    a.out_b[o] = (uint32_t)v;
-                }
-                o++;
+    if (work && wcnt) {  // warp-uniform
+        long long o = (long long)S.excl + warp_off;  // output index of the warp's next step
+        const uint32_t lt = qg_lanemask_lt();
+        for (uint32_t s0 = r0; s0 < r0 + q; s0 += 32) {
+            const uint32_t r = s0 + lane;
+            unsigned long long v = 0;
+            uint32_t k = 0, m = 0;
+            if (r < r0 + q) {
+                v = S.s[r];
+                k = (uint32_t)(v >> 32);
+                for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) m += (S.rk[e - 1] == k);
             }
+            // exclusive prefix of the lanes' match counts (0 or 1 in the common case)
+            uint32_t pre;
+            if (__all_sync(QG_FULL_MASK, m <= 1u)) {
+                pre = __popc(__ballot_sync(QG_FULL_MASK, m != 0u) & lt);
+            } else {
+                uint32_t inc = m;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const uint32_t x = __shfl_up_sync(QG_FULL_MASK, inc, d);
+                    if (lane >= d) inc += x;
+                }
+                pre = inc - m;
+            }
+            if (m) {
+                long long oo = o + pre;
+                for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) {
+                    if (S.rk[e - 1] != k) continue;
+                    if (oo < a.cap) {
+                        a.out_k[oo] = k;
+                        a.out_a[oo] = S.rp[e - 1];
+                        a.out_b[oo] = (uint32_t)v;
+                    }
+                    oo++;
+                }
+            }
+            o += __reduce_add_sync(QG_FULL_MASK, m);
         }
     }
     qg_lb_finish(lb, b, gridDim.x - 1, S.epoch);
