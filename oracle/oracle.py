@@ -212,3 +212,93 @@ def split_rec(rec: np.ndarray, parts: int):
     bound = np.empty(parts, np.int32)
     lib().orc_split_rec(_p(r), r.shape[0], parts, _p(out), _p(bound))
     return out, bound
+
+
+# ---- the reference's own OpenCL kernels, run on host cores ------------------
+# oracle/_ref/libref_kernels.so (oracle/ref_kernels/, built by build_ref.sh
+# only where the reference checkout exists).  They pin the restatement above
+# against the reference itself; absent elsewhere (ref_kernels() is None).
+REF_KERNELS = HERE / "_ref" / "libref_kernels.so"
+_rk = None
+
+
+def ref_kernels():
+    global _rk
+    if _rk is None and REF_KERNELS.exists():
+        L = ctypes.CDLL(str(REF_KERNELS))
+        sig = {
+            "ref_filter_rec": [c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p],
+            "ref_scan": [c_void_p, c_int, c_void_p],
+            "ref_sort_rec": [c_void_p, c_int],
+            "ref_groupby_rec": [c_void_p, c_int, c_int, c_int, c_void_p, c_void_p, c_void_p],
+            "ref_aggregate": [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_void_p],
+            "ref_hash_join": [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_void_p],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.restype, f.argtypes = c_int, args
+        _rk = L
+    return _rk
+
+
+def _rk_check(st: int, what: str) -> None:
+    if st != 0:
+        raise ValueError(f"{what}: outside the reference's supported sizes")
+
+
+def refk_filter_rec(rec: np.ndarray, lo: int, hi: int, num_thread: int = 256, num_block: int = 128) -> np.ndarray:
+    """filterImpl (host/host/testFilter.cpp:92-154) over the reference kernels."""
+    r = np.ascontiguousarray(rec, np.int32)
+    out = np.empty_like(r)
+    m = c_int(0)
+    _rk_check(ref_kernels().ref_filter_rec(_p(r), r.shape[0], lo, hi, num_thread, num_block, _p(out),
+                                           ctypes.byref(m)), "ref_filter_rec")
+    return out[: m.value]
+
+
+def refk_scan(x: np.ndarray) -> np.ndarray:
+    a = np.ascontiguousarray(x, np.int32)
+    out = np.empty_like(a)
+    _rk_check(ref_kernels().ref_scan(_p(a), a.size, _p(out)), "ref_scan")
+    return out
+
+
+def refk_sort_rec(rec: np.ndarray) -> np.ndarray:
+    """radixSortImpl_sm (host/host/testSort.cpp:24-136): bitonic, not stable."""
+    r = np.array(rec, np.int32, copy=True, order="C")
+    _rk_check(ref_kernels().ref_sort_rec(_p(r), r.shape[0]), "ref_sort_rec")
+    return r
+
+
+def refk_groupby_rec(rec: np.ndarray, num_thread: int = 256, num_block: int = 4):
+    """groupByImpl (host/host/testGroupBy.cpp:81-154): (sorted records, startPos)."""
+    r = np.ascontiguousarray(rec, np.int32)
+    srt = np.empty_like(r)
+    sp = np.empty(r.shape[0], np.int32)
+    g = c_int(0)
+    _rk_check(ref_kernels().ref_groupby_rec(_p(r), r.shape[0], num_thread, num_block, _p(srt), _p(sp),
+                                            ctypes.byref(g)), "ref_groupby_rec")
+    return srt, sp[: g.value]
+
+
+def refk_aggregate(sorted_rec: np.ndarray, start_pos: np.ndarray, op: int, num_thread: int = 256) -> np.ndarray:
+    """parallelAggregate_kernel chunks (host/host/testAggAfterGB.cpp:127-193)."""
+    r = np.ascontiguousarray(sorted_rec, np.int32)
+    sp = np.ascontiguousarray(start_pos, np.int32)
+    out = np.empty(max(sp.size, 1), np.int32)
+    _rk_check(ref_kernels().ref_aggregate(_p(r), r.shape[0], _p(sp), sp.size, op, num_thread, _p(out)),
+              "ref_aggregate")
+    return out[: sp.size]
+
+
+def refk_hash_join(r_pairs: np.ndarray, s_pairs: np.ndarray, bucket_num: int = 1024, probe_groups: int = 16):
+    """buildHashTable + probeHashTable (kernel/hj_filter_sort/1/hj_filter_sort_op.cl:25-109):
+    the (S.value, R.value) pairs in the probe's slot order, holes removed."""
+    r = np.ascontiguousarray(r_pairs, np.int32)
+    s = np.ascontiguousarray(s_pairs, np.int32)
+    fullest = int(np.bincount(r[:, 0].view(np.uint32) & (bucket_num - 1), minlength=bucket_num).max()) if r.size else 1
+    out = np.empty((max(s.shape[0], 1), 2), np.int32)
+    m = c_int(0)
+    _rk_check(ref_kernels().ref_hash_join(_p(r), r.shape[0], _p(s), s.shape[0], bucket_num, max(fullest, 1),
+                                          probe_groups, _p(out), ctypes.byref(m)), "ref_hash_join")
+    return out[: m.value]

@@ -11,7 +11,11 @@ them with oracle/build_ref.sh).  For each case it
 and records the reference DP planner's printed plans
 (host/dynamic_programming.cpp) for the planner port.
 
-Usage: python tests/golden/make_golden.py
+It also writes tests/golden/golden_refk.json, digests of the reference's own
+OpenCL kernels run on host cores (oracle/_ref/libref_kernels.so) on seeded
+inputs; --refk-only writes that file alone.
+
+Usage: python tests/golden/make_golden.py [--refk-only]
 """
 from __future__ import annotations
 
@@ -158,5 +162,38 @@ def main() -> None:
     print("wrote", OUT / "golden.npz", OUT / "golden.json")
 
 
+def refk_digests() -> None:
+    """tests/golden/golden_refk.json: digests of the reference's own kernels'
+    outputs (oracle/_ref/libref_kernels.so, built from kernel/filter/filter_op.cl
+    and kernel/aggregation/1/group_by_cu_op_dp.cl), each checked against the
+    oracle here before it is written."""
+    assert orc.ref_kernels() is not None, "oracle/_ref/libref_kernels.so is not built"
+    meta = {"filter": [], "sort_keys": [], "groupby": []}
+    for n, maxmax, lo, hi, seed in [(1 << 17, 1000, 10, 400, 0), (1 << 18, 1 << 20, -(1 << 19), 1 << 18, 1),
+                                    (1 << 18, 64, 0, 0, 2)]:
+        rin = orc.generate_rand(maxmax, n, seed)
+        out = orc.refk_filter_rec(rin, lo, hi)
+        assert np.array_equal(out, orc.filter_rec(rin, lo, hi))
+        meta["filter"].append({"n": n, "maxmax": maxmax, "lo": lo, "hi": hi, "seed": seed,
+                               "count": int(out.shape[0]), "sha": sha(out)})
+    for n, seed in [(2048, 0), (1 << 14, 1), (1 << 16, 2)]:
+        rin = orc.generate_rand(1 << 24, n, seed)
+        keys = orc.refk_sort_rec(rin)[:, 1]
+        assert np.array_equal(keys, orc.sort_rec(rin)[:, 1])
+        meta["sort_keys"].append({"n": n, "maxmax": 1 << 24, "seed": seed, "sha": sha(keys)})
+    for n, groups, seed in [(1 << 17, 50, 3), (1 << 18, 4000, 4)]:
+        rin = orc.generate_rand(1 << 20, n, seed)
+        rin[:, 1] = np.mod(rin[:, 1], groups)
+        srt, sp = orc.refk_groupby_rec(rin)
+        assert np.array_equal(sp, orc.group_startpos(orc.sort_rec(rin)))
+        aggs = [orc.refk_aggregate(srt, sp, op) for op in range(4)]
+        meta["groupby"].append({"n": n, "maxmax": 1 << 20, "groups": groups, "seed": seed,
+                                "startpos_sha": sha(sp), "agg_sha": [sha(a) for a in aggs]})
+    (OUT / "golden_refk.json").write_text(json.dumps(meta, indent=1, sort_keys=True) + "\n")
+    print("wrote", OUT / "golden_refk.json")
+
+
 if __name__ == "__main__":
-    main()
+    if "--refk-only" not in sys.argv:
+        main()
+    refk_digests()
