@@ -286,13 +286,15 @@ static qg_status finish_count(qg_ctx *ctx, long long *d_count, int64_t cap, int6
 // ---------------------------------------------------------------------------
 // Column filter, two passes with no waiting between tiles (variant 2).
 //   pass A (k_filter_count): keys only; the selected-row count of every tile,
-//          and per group of 256 tiles the sum of their counts;
-//   pass B (k_filter_write): keys and payloads; each tile's output offset is
-//          the sum of the group sums before it plus its group's earlier tile
-//          counts (at most 255), read while its own loads are in flight.
-// The keys are read twice, but no tile waits for another: both passes
-// stream at the memory's pace, where the single-pass chain of look-backs
-// does not.
+//          per group of 256 tiles the sum of their counts, and every row's
+//          predicate bit (16 bits per thread);
+//   pass B (k_filter_write): the predicate bits and the payloads of the
+//          selected rows only (the output is row id + payload); each tile's
+//          output offset is the sum of the group sums before it plus its
+//          group's earlier tile counts (at most 255), read while its own
+//          loads are in flight.
+// No tile waits for another: both passes stream at the memory's pace, where
+// the single-pass chain of look-backs does not.
 // ---------------------------------------------------------------------------
 constexpr int TP_THREADS = 256;
 constexpr int TP_WARPS = TP_THREADS / 32;
@@ -317,19 +319,23 @@ __device__ __forceinline__ uint32_t tp_flags(const int4 &k, long long idx, long 
            ((uint32_t)((k.w >= lo) & (k.w <= hi) & (idx + 3 < n)) << 3);
 }
 
+// With mask set, each thread also stores its 16 rows' predicate bits (bit
+// 4 * round + j), so that pass B need not read the keys again.
 __global__ void __launch_bounds__(TP_THREADS)
 k_filter_count(const int32_t *__restrict__ key, long long n, int32_t lo, int32_t hi, uint32_t *__restrict__ counts,
-               uint32_t *__restrict__ gsum) {
+               uint32_t *__restrict__ gsum, uint16_t *__restrict__ mask) {
     __shared__ uint32_t ws[TP_WARPS];
     const int tid = threadIdx.x;
     const long long base = (long long)blockIdx.x * TP_TILE;
     int4 kv[TP_ROUNDS];
 #pragma unroll
     for (int r = 0; r < TP_ROUNDS; r++) tp_load_keys(key, base + (long long)(r * TP_THREADS + tid) * 4, n, kv[r]);
-    uint32_t c = 0;
+    uint32_t fl = 0;
 #pragma unroll
     for (int r = 0; r < TP_ROUNDS; r++)
-        c += __popc(tp_flags(kv[r], base + (long long)(r * TP_THREADS + tid) * 4, n, lo, hi));
+        fl |= tp_flags(kv[r], base + (long long)(r * TP_THREADS + tid) * 4, n, lo, hi) << (4 * r);
+    if (mask) mask[(size_t)blockIdx.x * TP_THREADS + tid] = (uint16_t)fl;
+    uint32_t c = __popc(fl);
     c = __reduce_add_sync(QG_FULL_MASK, c);
     if ((tid & 31) == 0) ws[tid >> 5] = c;
     __syncthreads();
@@ -341,32 +347,35 @@ k_filter_count(const int32_t *__restrict__ key, long long n, int32_t lo, int32_t
     }
 }
 
-__global__ void __launch_bounds__(TP_THREADS, 5)
-k_filter_write(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, long long n, int32_t lo,
-               int32_t hi, const uint32_t *__restrict__ counts, const uint32_t *__restrict__ gsum,
-               int2 *__restrict__ out, long long cap, long long *__restrict__ d_count) {
+// Pass B from pass A's predicate bits: the keys are not read again, and a
+// thread loads its four payloads only when one of them is selected (the
+// output holds row ids and payloads, never keys).
+__global__ void __launch_bounds__(TP_THREADS)
+k_filter_write(const uint16_t *__restrict__ mask, const int32_t *__restrict__ pay, long long n,
+                 const uint32_t *__restrict__ counts, const uint32_t *__restrict__ gsum, int2 *__restrict__ out,
+                 long long cap, long long *__restrict__ d_count) {
     __shared__ uint32_t s_woff[TP_ROUNDS * TP_WARPS];
     __shared__ unsigned long long s_pre[TP_WARPS];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t tile = blockIdx.x;
     const long long base = (long long)tile * TP_TILE;
     const uint32_t lt = qg_lanemask_lt();
-    int4 kv[TP_ROUNDS], pv[TP_ROUNDS];
+    const uint32_t fl = __ldg(mask + (size_t)tile * TP_THREADS + tid);
+    int4 pv[TP_ROUNDS];
 #pragma unroll
     for (int r = 0; r < TP_ROUNDS; r++) {
-        const long long idx = base + (long long)(r * TP_THREADS + tid) * 4;
-        tp_load_keys(key, idx, n, kv[r]);
-        tp_load_keys(pay, idx, n, pv[r]);
+        pv[r] = make_int4(0, 0, 0, 0);
+        if ((fl >> (4 * r)) & 0xfu) tp_load_keys(pay, base + (long long)(r * TP_THREADS + tid) * 4, n, pv[r]);
     }
     // offset of this tile: earlier groups' sums, then this group's earlier tiles
     unsigned long long pre = 0;
     const uint32_t g = tile / TP_GROUP;
     for (uint32_t i = tid; i < g; i += TP_THREADS) pre += __ldg(gsum + i);
     for (uint32_t i = g * TP_GROUP + tid; i < tile; i += TP_THREADS) pre += __ldg(counts + i);
-    uint32_t fl = 0, lpre[TP_ROUNDS];
+    uint32_t lpre[TP_ROUNDS];
 #pragma unroll
     for (int r = 0; r < TP_ROUNDS; r++) {
-        const uint32_t f = tp_flags(kv[r], base + (long long)(r * TP_THREADS + tid) * 4, n, lo, hi);
+        const uint32_t f = (fl >> (4 * r)) & 0xfu;
         uint32_t c = 0, tot = 0;
 #pragma unroll
         for (int j = 0; j < 4; j++) {
@@ -376,7 +385,6 @@ k_filter_write(const int32_t *__restrict__ key, const int32_t *__restrict__ pay,
         }
         lpre[r] = c;
         if (lane == 0) s_woff[r * TP_WARPS + warp] = tot;
-        fl |= f << (4 * r);
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) pre += __shfl_down_sync(QG_FULL_MASK, pre, d);
@@ -433,7 +441,7 @@ qg_status qg_filter_rec_launch(qg_ctx *ctx, const void *in, int64_t n, int32_t l
     return qg_check_launch(ctx, "k_filter_rec");
 }
 
-static int g_filter_variant = 2;  // two passes: fastest measured (50 us vs 70 us at 16M rows)
+static int g_filter_variant = 2;  // two passes: fastest measured (42 us vs 68 us at 16M rows)
 
 qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *pay, int64_t n,
                                 int32_t lo, int32_t hi, int32_t *out, int64_t cap,
@@ -453,15 +461,17 @@ qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *
         const long long tp_tiles = qg_ceil_div(n, TP_TILE);
         const long long groups = qg_ceil_div(tp_tiles, TP_GROUP);
         char *scr;
-        QG_TRY(qg_scratch(ctx, (size_t)(tp_tiles + groups) * 4 + 256, &scr));
+        const size_t cg_bytes = qg_align_up((size_t)(tp_tiles + groups) * 4, 256);
+        QG_TRY(qg_scratch(ctx, cg_bytes + (size_t)tp_tiles * TP_THREADS * 2, &scr));
         uint32_t *counts = (uint32_t *)scr, *gsum = counts + tp_tiles;
+        uint16_t *mask = (uint16_t *)(scr + cg_bytes);
         QG_TRY_CUDA(ctx, cudaMemsetAsync(gsum, 0, (size_t)groups * 4, ctx->stream), "memset group sums");
         qg_pre_launch(ctx);
-        k_filter_count<<<(unsigned)tp_tiles, TP_THREADS, 0, ctx->stream>>>(key, n, lo, hi, counts, gsum);
+        k_filter_count<<<(unsigned)tp_tiles, TP_THREADS, 0, ctx->stream>>>(key, n, lo, hi, counts, gsum, mask);
         QG_TRY(qg_check_launch(ctx, "k_filter_count"));
         qg_pre_launch(ctx);
-        k_filter_write<<<(unsigned)tp_tiles, TP_THREADS, 0, ctx->stream>>>(key, pay, n, lo, hi, counts, gsum,
-                                                                         (int2 *)out, cap, d_count);
+        k_filter_write<<<(unsigned)tp_tiles, TP_THREADS, 0, ctx->stream>>>(mask, pay, n, counts, gsum, (int2 *)out,
+                                                                         cap, d_count);
         return qg_check_launch(ctx, "k_filter_write");
     }
     if (g_filter_variant == 1) {
