@@ -215,14 +215,16 @@ QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey, const int
  * buckets_log2: 0 = from the input size (about 2560 rows per bucket), else
  * 1..15.  bucket_s_max / bucket_r_max: rows of a bucket that the shared-memory
  * bucket kernel takes (0 = its capacity, 4096 / 2048); smaller values send
- * more buckets to the recursive path (testing).  No reference counterpart:
+ * more buckets to the outside paths (testing).  No reference counterpart:
  * the reference has a single join kernel pair. */
 QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucket_s_max,
                                    uint32_t bucket_r_max);
 /* Diagnostics of the context's last qg_join_filter_sort: out[0] path
  * (1 radix, 2 learned, 3 hash join + sort, 0 nothing to join), out[1]
  * buckets, out[2] buckets handled outside the bucket kernel, out[3] their
- * rows, out[4] deepest recursion level, out[5] knots of the learned model,
+ * rows, out[4] those of them with several keys (joined together by the
+ * sort-merge path; the others are single-key cross products), out[5] knots
+ * of the learned model,
  * out[6] heavy keys among them, out[7] 1 when the automatic choice moved
  * from radix to the learned function. */
 QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8);

@@ -263,7 +263,7 @@ class Context:
         self.check(self.lib.qg_join_stats(self.handle, out), "qg_join_stats")
         names = {0: "none", 1: "radix", 2: "learned", 3: "hash_sort"}
         return {"path": names.get(out[0], str(out[0])), "buckets": out[1], "outside_buckets": out[2],
-                "outside_rows": out[3], "depth": out[4], "knots": out[5], "heavy_keys": out[6],
+                "outside_rows": out[3], "merge_buckets": out[4], "knots": out[5], "heavy_keys": out[6],
                 "auto_switched": out[7]}
 
     def part_learn(self, keys: torch.Tensor, nbuckets: int) -> torch.Tensor:

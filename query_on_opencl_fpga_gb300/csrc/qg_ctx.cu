@@ -63,10 +63,7 @@ QG_API qg_status qg_ctx_destroy(qg_ctx *ctx) {
         for (int i = 0; i < 2 * QG_MAX_TIMED; i++) cudaEventDestroy(ctx->ev[i]);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->lbstat) cudaFree(ctx->lbstat);
-    for (int i = 0; i < 8; i++) {
-        if (ctx->pj_pool[i]) cudaFree(ctx->pj_pool[i]);
-        if (ctx->pj_tmp[i]) cudaFree(ctx->pj_tmp[i]);
-    }
+    if (ctx->pj_tmp) cudaFree(ctx->pj_tmp);
     if (ctx->table) cudaFree(ctx->table);
     if (ctx->aux) cudaFree(ctx->aux);
     if (ctx->ctl) cudaFree(ctx->ctl);

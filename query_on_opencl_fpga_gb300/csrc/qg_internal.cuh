@@ -44,10 +44,8 @@ struct qg_ctx {
     bool table_dirty;       // group-by table must be cleared before next use
     uint32_t gb_stats[4];   // last qg_groupby_cols: path, flags, fullest bucket, bucket cap
     uint32_t pj_stats[8];   // last qg_join_filter_sort (see qg_join_stats)
-    char *pj_pool[8];       // per-depth work memory of the join's nested levels (grow-only)
-    size_t pj_pool_bytes[8];
-    char *pj_tmp[8];        // per-depth outputs of nested joins (grow-only)
-    size_t pj_tmp_bytes[8];
+    char *pj_tmp;           // the join's sort-merge arrays (grow-only)
+    size_t pj_tmp_bytes;
     char msg[256];
     // Per-kernel CUDA-event timing (qg_ctx_enable_timing): a pair of events
     // brackets every launch on the context's stream.

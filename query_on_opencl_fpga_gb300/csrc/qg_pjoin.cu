@@ -12,7 +12,8 @@
 // Pipeline (one GPU, all data in HBM):
 //   1. R columns -> R records (key << 32 | payload) and R's key range.
 //   2. S: filter on S.payload and on R's key range, compacted in one pass
-//      (decoupled look-back) into S' records (key << 32 | S.payload).
+//      into S' records (key << 32 | S.payload); the order of S' is free, so
+//      each tile takes its output range with one atomic.
 //   3. A partition function maps keys to B buckets (key ranges): radix over
 //      (k - kmin), or a learned piecewise-linear CDF model fitted on a sample
 //      (qg_part.cuh).  Bucket histograms of R and S', then one or two stable
@@ -26,9 +27,11 @@
 //      written in key order.  Buckets are key ranges, so the output is sorted
 //      with no global sort pass.
 //   5. Buckets too large for shared memory: a bucket with one key is a cross
-//      product (k_pj_cross); any other is joined recursively with its own
-//      partition into a temporary and copied into place (k_pj_place).  Both
-//      read the bucket's output offset that step 4 published.
+//      product (k_pj_cross); all the others are gathered, sorted by key and
+//      merge-joined together (k_pj_mj_*: a fixed number of launches however
+//      many such buckets there are).  Their match counts are known before
+//      step 4, which publishes every such bucket's output offset; the writes
+//      of step 5 read it.
 #include <algorithm>
 #include <string.h>
 #include <vector>
@@ -656,43 +659,118 @@ k_pj_join(PbArgs a, qg_lookback lb) {
 struct PjCross {  // a bucket with one key: every R row times every S' row
     uint32_t b, rb, rn, sb, sn;
 };
-struct PjPlace {  // a bucket joined recursively into a temporary
-    uint32_t b;
-    const uint32_t *k, *a, *c;
-    unsigned long long m;
+struct PjMj {  // a bucket with several keys, joined by the sort-merge path
+    uint32_t b, rb, rn, sb, sn;  // join group; its rows in the partitioned R and S'
+    uint32_t roff, soff;         // its rows in the gathered arrays
 };
 
-__global__ void k_pj_cross(const PjCross *__restrict__ list, const unsigned long long *__restrict__ R,
+// blockIdx.y walks the list (nlist entries) with stride gridDim.y.
+__global__ void k_pj_cross(const PjCross *__restrict__ list, uint32_t nlist, const unsigned long long *__restrict__ R,
                            const unsigned long long *__restrict__ S, const unsigned long long *__restrict__ off,
                            uint32_t *__restrict__ ok, uint32_t *__restrict__ oa, uint32_t *__restrict__ ob,
                            long long cap) {
-    const PjCross e = list[blockIdx.y];
-    const unsigned long long m = (unsigned long long)e.rn * e.sn;
-    const unsigned long long base = off[e.b];
-    for (unsigned long long o = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; o < m;
-         o += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long g = base + o;
-        if (g >= (unsigned long long)cap) break;
-        const unsigned long long si = o / e.rn, rj = o - si * e.rn;
-        const unsigned long long sv = __ldg(S + e.sb + si), rv = __ldg(R + e.rb + rj);
-        ok[g] = (uint32_t)(sv >> 32);
-        oa[g] = (uint32_t)rv;
-        ob[g] = (uint32_t)sv;
+    for (uint32_t y = blockIdx.y; y < nlist; y += gridDim.y) {
+        const PjCross e = list[y];
+        const unsigned long long m = (unsigned long long)e.rn * e.sn;
+        const unsigned long long base = off[e.b];
+        for (unsigned long long o = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; o < m;
+             o += (unsigned long long)gridDim.x * blockDim.x) {
+            const unsigned long long g = base + o;
+            if (g >= (unsigned long long)cap) break;
+            const unsigned long long si = o / e.rn, rj = o - si * e.rn;
+            const unsigned long long sv = __ldg(S + e.sb + si), rv = __ldg(R + e.rb + rj);
+            ok[g] = (uint32_t)(sv >> 32);
+            oa[g] = (uint32_t)rv;
+            ob[g] = (uint32_t)sv;
+        }
     }
 }
 
-__global__ void k_pj_place(const PjPlace *__restrict__ list, const unsigned long long *__restrict__ off,
-                           uint32_t *__restrict__ ok, uint32_t *__restrict__ oa, uint32_t *__restrict__ ob,
-                           long long cap) {
-    const PjPlace e = list[blockIdx.y];
+// Sort-merge path for the oversize buckets with several keys, all of them in
+// a fixed number of launches.  Their rows are gathered into Rb / Sb in bucket
+// order and sorted by key there; the buckets are disjoint key ranges in
+// ascending order, so every bucket keeps its own segment.  blockIdx.y is the
+// bucket.
+__global__ void k_pj_mj_gather(const PjMj *__restrict__ list, uint32_t nlist, const unsigned long long *__restrict__ R,
+                               const unsigned long long *__restrict__ S, unsigned long long *__restrict__ Rb,
+                               unsigned long long *__restrict__ Sb) {
+    for (uint32_t y = blockIdx.y; y < nlist; y += gridDim.y) {
+        const PjMj e = list[y];
+        const uint32_t m = max(e.rn, e.sn);
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+            if (i < e.rn) Rb[e.roff + i] = __ldg(R + e.rb + i);
+            if (i < e.sn) Sb[e.soff + i] = __ldg(S + e.sb + i);
+        }
+    }
+}
+
+// Per S row: its matching R rows [lob, lob + cnt) in the bucket's key-sorted
+// R segment; the bucket's match count is added to bigcnt[b] (64-bit) for the
+// bucket kernel's look-back and to *tot for the host.
+__global__ void __launch_bounds__(256)
+k_pj_mj_count(const PjMj *__restrict__ list, uint32_t nlist, const unsigned long long *__restrict__ Rb,
+              const unsigned long long *__restrict__ Sb, uint32_t *__restrict__ cnt, uint32_t *__restrict__ lob,
+              unsigned long long *__restrict__ bigcnt, unsigned long long *__restrict__ tot) {
+    __shared__ unsigned long long red[8];
+    for (uint32_t y = blockIdx.y; y < nlist; y += gridDim.y) {
+    const PjMj e = list[y];
+    unsigned long long my = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < e.sn; i += gridDim.x * blockDim.x) {
+        const uint32_t k = (uint32_t)(__ldg(Sb + e.soff + i) >> 32);
+        uint32_t lo = 0, hi = e.rn;  // first R row with key >= k
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if ((uint32_t)(__ldg(Rb + e.roff + mid) >> 32) < k) lo = mid + 1;
+            else hi = mid;
+        }
+        uint32_t up = lo, h2 = e.rn;  // first R row with key > k
+        while (up < h2) {
+            const uint32_t mid = (up + h2) >> 1;
+            if ((uint32_t)(__ldg(Rb + e.roff + mid) >> 32) <= k) up = mid + 1;
+            else h2 = mid;
+        }
+        cnt[e.soff + i] = up - lo;
+        lob[e.soff + i] = e.roff + lo;
+        my += up - lo;
+    }
+    for (int d = 16; d > 0; d >>= 1) my += __shfl_down_sync(QG_FULL_MASK, my, d);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = my;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        if (t) {
+            atomicAdd(bigcnt + e.b, t);
+            atomicAdd(tot, t);
+        }
+    }
+    __syncthreads();  // red is reused by the next entry
+    }
+}
+
+// Matches of each S row at off[b] + (its exclusive prefix within the bucket):
+// S rows in key order, so the bucket's output is in key order.
+__global__ void k_pj_mj_write(const PjMj *__restrict__ list, uint32_t nlist, const unsigned long long *__restrict__ Rb,
+                              const unsigned long long *__restrict__ Sb, const uint32_t *__restrict__ cnt,
+                              const uint32_t *__restrict__ lob, const uint32_t *__restrict__ pre,
+                              const unsigned long long *__restrict__ off, uint32_t *__restrict__ ok,
+                              uint32_t *__restrict__ oa, uint32_t *__restrict__ ob, long long cap) {
+    for (uint32_t y = blockIdx.y; y < nlist; y += gridDim.y) {
+    const PjMj e = list[y];
     const unsigned long long base = off[e.b];
-    for (unsigned long long o = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; o < e.m;
-         o += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long g = base + o;
-        if (g >= (unsigned long long)cap) break;
-        ok[g] = e.k[o];
-        oa[g] = e.a[o];
-        ob[g] = e.c[o];
+    const uint32_t p0 = __ldg(pre + e.soff);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < e.sn; i += gridDim.x * blockDim.x) {
+        const uint32_t c = cnt[e.soff + i];
+        if (!c) continue;
+        const unsigned long long sv = __ldg(Sb + e.soff + i);
+        const uint32_t l = lob[e.soff + i];
+        unsigned long long g = base + (uint32_t)(pre[e.soff + i] - p0);  // 32-bit wrap-safe difference
+        for (uint32_t j = 0; j < c && g < (unsigned long long)cap; j++, g++) {
+            ok[g] = (uint32_t)(sv >> 32);
+            oa[g] = (uint32_t)__ldg(Rb + l + j);
+            ob[g] = (uint32_t)sv;
+        }
+    }
     }
 }
 
@@ -743,7 +821,6 @@ int g_pj_variant = 0;  // 0 auto (radix; learned when a key sample shows that it
 int g_pj_blog2 = 0;    // 0: fine bucket count from the input size
 uint32_t g_pj_smax = PB_SMAX, g_pj_rmax = PB_RMAX;
 constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit (and judge) the learned model
-constexpr int PJ_MAX_DEPTH = 6;
 
 struct PjLevel {
     PjRange *range;
@@ -754,7 +831,8 @@ struct PjLevel {
     uint32_t *scnt;        // [2 nb] sample counts under radix, learned
     unsigned long long *bigcnt, *off, *total;
     PjCross *cross;
-    PjPlace *place;
+    PjMj *mj;
+    unsigned long long *mjtot;  // matches of the sort-merge buckets
     qg_cdf_model *model;             // learned model (top level only)
     unsigned long long *smp, *smp2;  // key sample (top level only)
 };
@@ -772,7 +850,8 @@ size_t pj_level_bytes(uint32_t nb, bool learned) {
     add((size_t)nb * 8);
     add(8);
     add((size_t)nb * sizeof(PjCross));
-    add((size_t)nb * sizeof(PjPlace));
+    add((size_t)nb * sizeof(PjMj));
+    add(8);
     if (learned) {
         add(sizeof(qg_cdf_model));
         add((size_t)CDF_SAMPLE * 8);
@@ -796,7 +875,8 @@ void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     L->off = (unsigned long long *)take((size_t)nb * 8);
     L->total = (unsigned long long *)take(8);
     L->cross = (PjCross *)take((size_t)nb * sizeof(PjCross));
-    L->place = (PjPlace *)take((size_t)nb * sizeof(PjPlace));
+    L->mj = (PjMj *)take((size_t)nb * sizeof(PjMj));
+    L->mjtot = (unsigned long long *)take(8);
     L->model = nullptr;
     L->smp = L->smp2 = nullptr;
     if (learned) {
@@ -806,7 +886,7 @@ void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     }
 }
 
-// Grow-only per-depth device buffers of the context.
+// Grow-only device buffer of the context (the sort-merge arrays).
 qg_status pj_pool_get(qg_ctx *ctx, char **slot, size_t *slot_bytes, size_t bytes, char **out) {
     bytes = qg_align_up(bytes ? bytes : 256, 256);
     if (bytes > *slot_bytes) {
@@ -908,27 +988,20 @@ qg_status pj_judge(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot, c
     return QG_OK;
 }
 
-struct PjTempOut {
-    uint32_t *k, *a, *c;
-    long long cap;
-    bool own;  // allocated for this group alone (its output outgrew the slice)
-};
-
+// Partition, join groups, outside buckets.  mem: the level's arrays
+// (pj_level_bytes), carved here.
 qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
                   unsigned long long *s, unsigned long long *ssp, long long nS, uint32_t kmin,
                   uint32_t kmax, int variant, uint32_t *ok, uint32_t *oa, uint32_t *ob, long long cap,
-                  long long *M_out, int depth, char *lvl_mem) {
+                  long long *M_out, char *mem) {
     *M_out = 0;
     if (nR == 0 || nS == 0) return QG_OK;
-    if (depth > PJ_MAX_DEPTH) return QG_ERR_UNSUPPORTED;
     QG_TRY(pj_attrs(ctx));
     const long long ntot = nR + nS;
-    // Fine buckets of about a quarter of the bucket kernel's capacity (join
-    // groups pack several of them); a nested level splits its key range at
-    // least 256 ways, so every level narrows it and the recursion ends in
-    // single-key buckets.
-    uint32_t nb = depth > 0 ? 256u : 1u;
-    if (g_pj_blog2 > 0 && depth == 0) {
+    // fine buckets of about a quarter of the bucket kernel's capacity (join
+    // groups pack several of them)
+    uint32_t nb = 1u;
+    if (g_pj_blog2 > 0) {
         nb = 1u << g_pj_blog2;
     } else {
         while (nb < (uint32_t)PJ_MAX_BUCKETS &&
@@ -942,11 +1015,7 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     const int bits = range ? 32 - __builtin_clz(range) : 0;
     const int shift = bits > lb2 ? bits - lb2 : 0;
     const uint32_t nb_radix = (uint32_t)(((unsigned long long)range >> shift) + 1);
-    const bool may_learn = depth == 0 && variant != 1;
-
-    char *mem = lvl_mem;
-    if (!mem) QG_TRY(pj_pool_get(ctx, &ctx->pj_pool[depth], &ctx->pj_pool_bytes[depth],
-                                 pj_level_bytes(nb, may_learn), &mem));
+    const bool may_learn = variant != 1;
     PjLevel L;
     pj_level_carve(mem, nb, may_learn, &L);
     const qg_part_fn radix{0, kmin, shift, nullptr};
@@ -1042,11 +1111,11 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     std::vector<uint32_t> bigflag(G, 0);
     for (uint32_t g = 0; g < G; g++) bigflag[g] = big[g] ? 1u : 0u;
 
-    // outside groups: single-key cross products, the rest recursively
+    // Outside groups: a bucket with one key is a cross product (k_pj_cross);
+    // the others all go through the sort-merge path together (k_pj_mj_*).
     std::vector<PjCross> cross;
-    std::vector<PjPlace> place;
-    std::vector<PjTempOut> temps;
-    int depth_max = depth;
+    std::vector<PjMj> mj;
+    long long nrb = 0, nsb = 0;
     if (!over.empty()) {
         std::vector<uint32_t> mm(2 * over.size());
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, over.data(), over.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "list h2d");
@@ -1055,58 +1124,56 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
         QG_TRY(qg_check_launch(ctx, "k_pj_minmax"));
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(mm.data(), L.mm, mm.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "mm d2h");
         QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-        // one slice of the per-depth output pool for each recursive group
-        size_t slice_rows = 0;
-        for (size_t i = 0; i < over.size(); i++)
-            if (mm[2 * i] != mm[2 * i + 1]) slice_rows += (size_t)over[i].sn + over[i].rn + 1024;
-        char *tmp = nullptr;
-        if (slice_rows)
-            QG_TRY(pj_pool_get(ctx, &ctx->pj_tmp[depth], &ctx->pj_tmp_bytes[depth], slice_rows * 12, &tmp));
-        size_t used = 0;
-        qg_status st = QG_OK;
-        for (size_t i = 0; i < over.size() && st == QG_OK; i++) {
+        for (size_t i = 0; i < over.size(); i++) {
             const PjCross &e = over[i];
             if (mm[2 * i] == mm[2 * i + 1]) {
                 bigcnt[e.b] = (unsigned long long)e.rn * e.sn;
                 cross.push_back(e);
-                continue;
+            } else {
+                mj.push_back(PjMj{e.b, e.rb, e.rn, e.sb, e.sn, (uint32_t)nrb, (uint32_t)nsb});
+                nrb += e.rn;
+                nsb += e.sn;
             }
-            const long long capt = (long long)e.sn + e.rn + 1024;
-            PjTempOut t{(uint32_t *)(tmp + used * 4), (uint32_t *)(tmp + (slice_rows + used) * 4),
-                        (uint32_t *)(tmp + (2 * slice_rows + used) * 4), capt, false};
-            used += (size_t)capt;
-            long long Mb = 0;
-            st = pj_core(ctx, r + e.rb, rsp + e.rb, e.rn, s + e.sb, ssp + e.sb, e.sn, mm[2 * i], mm[2 * i + 1], 1,
-                         t.k, t.a, t.c, t.cap, &Mb, depth + 1, nullptr);
-            if (st == QG_OK && Mb > t.cap) {  // more matches than rows: buffers of its own
-                PjTempOut u{nullptr, nullptr, nullptr, Mb, true};
-                if (cudaMalloc((void **)&u.k, (size_t)Mb * 4) != cudaSuccess ||
-                    cudaMalloc((void **)&u.a, (size_t)Mb * 4) != cudaSuccess ||
-                    cudaMalloc((void **)&u.c, (size_t)Mb * 4) != cudaSuccess) {
-                    cudaGetLastError();
-                    if (u.k) cudaFree(u.k);
-                    if (u.a) cudaFree(u.a);
-                    st = QG_ERR_OOM;
-                    break;
-                }
-                temps.push_back(u);
-                t = u;
-                st = pj_core(ctx, r + e.rb, rsp + e.rb, e.rn, s + e.sb, ssp + e.sb, e.sn, mm[2 * i], mm[2 * i + 1],
-                             1, t.k, t.a, t.c, t.cap, &Mb, depth + 1, nullptr);
-            }
-            if ((int)ctx->pj_stats[4] > depth_max) depth_max = (int)ctx->pj_stats[4];
-            bigcnt[e.b] = (unsigned long long)Mb;
-            place.push_back(PjPlace{e.b, t.k, t.a, t.c, (unsigned long long)Mb});
-        }
-        if (st != QG_OK) {
-            for (auto &t : temps) { cudaFree(t.k); cudaFree(t.a); cudaFree(t.c); }
-            return st;
         }
     }
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gr, gr.data(), (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gr h2d");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gs, gs.data(), (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gs h2d");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.big, bigflag.data(), (size_t)G * 4, cudaMemcpyHostToDevice, ctx->stream), "big h2d");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.bigcnt, bigcnt.data(), (size_t)G * 8, cudaMemcpyHostToDevice, ctx->stream), "bigcnt h2d");
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mjtot, 0, 8, ctx->stream), "memset mjtot");
+
+    // sort-merge buckets: gather, sort by key, count each S row's matches
+    // (into bigcnt, before the bucket kernel reads it), scan the counts
+    unsigned long long *Rb = nullptr, *Sb = nullptr;
+    uint32_t *mcnt = nullptr, *mlob = nullptr, *mpre = nullptr;
+    uint32_t mj_rows = 0;  // the largest bucket's rows: the grid's x extent
+    for (auto &e : mj) mj_rows = max(mj_rows, max(e.rn, e.sn));
+    const unsigned mgx = (unsigned)pj_grid(ctx, (mj_rows + 3) / 4, 256, 4);
+    const unsigned mgy = (unsigned)std::min<size_t>(mj.size(), 65535);
+    if (!mj.empty()) {
+        const size_t rbb = qg_align_up((size_t)nrb * 8, 256), sbb = qg_align_up((size_t)nsb * 8, 256),
+                     cb = qg_align_up((size_t)nsb * 4, 256);
+        char *tmp;
+        QG_TRY(pj_pool_get(ctx, &ctx->pj_tmp, &ctx->pj_tmp_bytes, 2 * rbb + 2 * sbb + 3 * cb, &tmp));
+        Rb = (unsigned long long *)tmp;
+        unsigned long long *Rt = (unsigned long long *)(tmp + rbb);
+        Sb = (unsigned long long *)(tmp + 2 * rbb);
+        unsigned long long *St = (unsigned long long *)(tmp + 2 * rbb + sbb);
+        mcnt = (uint32_t *)(tmp + 2 * rbb + 2 * sbb);
+        mlob = (uint32_t *)(tmp + 2 * rbb + 2 * sbb + cb);
+        mpre = (uint32_t *)(tmp + 2 * rbb + 2 * sbb + 2 * cb);
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.mj, mj.data(), mj.size() * sizeof(PjMj), cudaMemcpyHostToDevice, ctx->stream), "mj h2d");
+        qg_pre_launch(ctx);
+        k_pj_mj_gather<<<dim3(mgx, mgy), 256, 0, ctx->stream>>>(L.mj, (uint32_t)mj.size(), r, s, Rb, Sb);
+        QG_TRY(qg_check_launch(ctx, "k_pj_mj_gather"));
+        QG_TRY(qg_sort_rec_inplace(ctx, Rb, Rt, nrb));
+        QG_TRY(qg_sort_rec_inplace(ctx, Sb, St, nsb));
+        qg_pre_launch(ctx);
+        k_pj_mj_count<<<dim3(mgx, mgy), 256, 0, ctx->stream>>>(L.mj, (uint32_t)mj.size(), Rb, Sb, mcnt, mlob,
+                                                               L.bigcnt, L.mjtot);
+        QG_TRY(qg_check_launch(ctx, "k_pj_mj_count"));
+        QG_TRY(qg_scan_excl_i32(ctx, (const int32_t *)mcnt, (int32_t *)mpre, nsb));
+    }
 
     // the bucket kernel over the join groups
     qg_lookback lb;
@@ -1118,47 +1185,44 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     if (!cross.empty()) {
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, cross.data(), cross.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "cross h2d");
         qg_pre_launch(ctx);
-        k_pj_cross<<<dim3((unsigned)pj_grid(ctx, 1LL << 24, 256, 4), (unsigned)cross.size()), 256, 0, ctx->stream>>>(
-            L.cross, r, s, L.off, ok, oa, ob, cap);
+        k_pj_cross<<<dim3((unsigned)pj_grid(ctx, 1LL << 24, 256, 4), (unsigned)std::min<size_t>(cross.size(), 65535)),
+                     256, 0, ctx->stream>>>(L.cross, (uint32_t)cross.size(), r, s, L.off, ok, oa, ob, cap);
         QG_TRY(qg_check_launch(ctx, "k_pj_cross"));
     }
-    if (!place.empty()) {
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.place, place.data(), place.size() * sizeof(PjPlace), cudaMemcpyHostToDevice, ctx->stream), "place h2d");
+    if (!mj.empty()) {
         qg_pre_launch(ctx);
-        k_pj_place<<<dim3((unsigned)pj_grid(ctx, 1LL << 24, 256, 4), (unsigned)place.size()), 256, 0, ctx->stream>>>(
-            L.place, L.off, ok, oa, ob, cap);
-        QG_TRY(qg_check_launch(ctx, "k_pj_place"));
+        k_pj_mj_write<<<dim3(mgx, mgy), 256, 0, ctx->stream>>>(L.mj, (uint32_t)mj.size(), Rb, Sb, mcnt, mlob, mpre,
+                                                               L.off, ok, oa, ob, cap);
+        QG_TRY(qg_check_launch(ctx, "k_pj_mj_write"));
     }
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 1, L.mjtot, 8, cudaMemcpyDeviceToHost, ctx->stream), "mjtot d2h");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     const unsigned long long total = (unsigned long long)ctx->pinned[0];
-    for (auto &t : temps) { cudaFree(t.k); cudaFree(t.a); cudaFree(t.c); }
     // The look-back sums are 32-bit: report the outside groups' 64-bit sum
     // when they alone could wrap it (a capacity error follows).
     *M_out = (long long)total;
     {
-        unsigned long long outside = 0;
+        unsigned long long outside = (unsigned long long)ctx->pinned[1];
         for (uint32_t g = 0; g < G; g++) outside += bigcnt[g];
         if (outside >= (1ull << 32)) *M_out = (long long)outside;
     }
-    if (depth == 0) {
-        ctx->pj_stats[0] = use_learned ? 2 : 1;
-        ctx->pj_stats[1] = nbu;
-        ctx->pj_stats[2] = (uint32_t)over.size();
-        long long orows = 0;
-        for (auto &e : over) orows += (long long)e.rn + e.sn;
-        ctx->pj_stats[3] = orows > 0xffffffffLL ? 0xffffffffu : (uint32_t)orows;
-        ctx->pj_stats[5] = 0;
-        ctx->pj_stats[6] = 0;
-        if (use_learned) {
-            uint32_t hk[4];
-            cudaMemcpy(hk, L.model, 16, cudaMemcpyDeviceToHost);
-            ctx->pj_stats[5] = hk[0];
-            ctx->pj_stats[6] = hk[3];
-        }
-        ctx->pj_stats[7] = (judged && use_learned) ? 1 : 0;
+    ctx->pj_stats[0] = use_learned ? 2 : 1;
+    ctx->pj_stats[1] = nbu;
+    ctx->pj_stats[2] = (uint32_t)over.size();
+    long long orows = 0;
+    for (auto &e : over) orows += (long long)e.rn + e.sn;
+    ctx->pj_stats[3] = orows > 0xffffffffLL ? 0xffffffffu : (uint32_t)orows;
+    ctx->pj_stats[4] = (uint32_t)mj.size();
+    ctx->pj_stats[5] = 0;
+    ctx->pj_stats[6] = 0;
+    if (use_learned) {
+        uint32_t hk[4];
+        cudaMemcpy(hk, L.model, 16, cudaMemcpyDeviceToHost);
+        ctx->pj_stats[5] = hk[0];
+        ctx->pj_stats[6] = hk[3];
     }
-    ctx->pj_stats[4] = (uint32_t)depth_max;
+    ctx->pj_stats[7] = (judged && use_learned) ? 1 : 0;
     return QG_OK;
 }
 
@@ -1226,7 +1290,7 @@ extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey
     QG_TRY(qg_collect_error(ctx));
     long long M = 0;
     QG_TRY(pj_core(ctx, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, g_pj_variant, (uint32_t *)out_key,
-                   (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M, 0, lvl));
+                   (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M, lvl));
     QG_TRY(qg_collect_error(ctx));
     *out_n = M;
     return M > cap ? QG_ERR_CAPACITY : QG_OK;
