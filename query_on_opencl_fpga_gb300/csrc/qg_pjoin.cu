@@ -774,34 +774,42 @@ __global__ void k_pj_mj_write(const PjMj *__restrict__ list, uint32_t nlist, con
     }
 }
 
-// Key range of each listed bucket over its R and S' rows: mm[2i] = min, mm[2i+1] = max.
-__global__ void k_pj_minmax(const PjCross *__restrict__ list, const unsigned long long *__restrict__ R,
-                            const unsigned long long *__restrict__ S, uint32_t *__restrict__ mm) {
+// Key range of each listed bucket over its R and S' rows: mn[i], mx[i]
+// (preset to 0xffffffff and 0).  Several CTAs share a bucket (blockIdx.x),
+// so that a heavy key's bucket of millions of rows is not one CTA's scan;
+// blockIdx.y walks the list with stride gridDim.y.
+__global__ void __launch_bounds__(256)
+k_pj_minmax(const PjCross *__restrict__ list, uint32_t nlist, const unsigned long long *__restrict__ R,
+            const unsigned long long *__restrict__ S, uint32_t *__restrict__ mn_out, uint32_t *__restrict__ mx_out) {
     __shared__ uint32_t red[2 * 8];
-    const PjCross e = list[blockIdx.x];
-    uint32_t mn = 0xffffffffu, mx = 0;
-    for (uint32_t i = threadIdx.x; i < e.rn; i += blockDim.x) {
-        const uint32_t k = (uint32_t)(__ldg(R + e.rb + i) >> 32);
-        mn = min(mn, k);
-        mx = max(mx, k);
-    }
-    for (uint32_t i = threadIdx.x; i < e.sn; i += blockDim.x) {
-        const uint32_t k = (uint32_t)(__ldg(S + e.sb + i) >> 32);
-        mn = min(mn, k);
-        mx = max(mx, k);
-    }
-    mn = __reduce_min_sync(QG_FULL_MASK, mn);
-    mx = __reduce_max_sync(QG_FULL_MASK, mx);
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { red[w] = mn; red[8 + w] = mx; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int i = 1; i < (int)(blockDim.x >> 5); i++) {
-            mn = min(mn, red[i]);
-            mx = max(mx, red[8 + i]);
+    for (uint32_t y = blockIdx.y; y < nlist; y += gridDim.y) {
+        const PjCross e = list[y];
+        uint32_t mn = 0xffffffffu, mx = 0;
+        const uint32_t stride = gridDim.x * blockDim.x;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < e.rn; i += stride) {
+            const uint32_t k = (uint32_t)(__ldg(R + e.rb + i) >> 32);
+            mn = min(mn, k);
+            mx = max(mx, k);
         }
-        mm[2 * blockIdx.x] = mn;
-        mm[2 * blockIdx.x + 1] = mx;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < e.sn; i += stride) {
+            const uint32_t k = (uint32_t)(__ldg(S + e.sb + i) >> 32);
+            mn = min(mn, k);
+            mx = max(mx, k);
+        }
+        mn = __reduce_min_sync(QG_FULL_MASK, mn);
+        mx = __reduce_max_sync(QG_FULL_MASK, mx);
+        const int w = threadIdx.x >> 5;
+        if ((threadIdx.x & 31) == 0) { red[w] = mn; red[8 + w] = mx; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int i = 1; i < (int)(blockDim.x >> 5); i++) {
+                mn = min(mn, red[i]);
+                mx = max(mx, red[8 + i]);
+            }
+            if (mn != 0xffffffffu) atomicMin(mn_out + y, mn);
+            if (mx != 0) atomicMax(mx_out + y, mx);
+        }
+        __syncthreads();  // red is reused by the next entry
     }
 }
 
@@ -1117,16 +1125,22 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     std::vector<PjMj> mj;
     long long nrb = 0, nsb = 0;
     if (!over.empty()) {
-        std::vector<uint32_t> mm(2 * over.size());
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, over.data(), over.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "list h2d");
+        const size_t no = over.size();
+        std::vector<uint32_t> mm(2 * no);  // [mins][maxes]
+        uint32_t most = 0;
+        for (auto &e : over) most = max(most, max(e.rn, e.sn));
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, over.data(), no * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "list h2d");
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mm, 0xff, no * 4, ctx->stream), "memset mins");
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mm + no, 0, no * 4, ctx->stream), "memset maxes");
         qg_pre_launch(ctx);
-        k_pj_minmax<<<(unsigned)over.size(), 256, 0, ctx->stream>>>(L.cross, r, s, L.mm);
+        k_pj_minmax<<<dim3((unsigned)pj_grid(ctx, (most + 3) / 4, 256, 4), (unsigned)std::min<size_t>(no, 65535)), 256, 0,
+                      ctx->stream>>>(L.cross, (uint32_t)no, r, s, L.mm, L.mm + no);
         QG_TRY(qg_check_launch(ctx, "k_pj_minmax"));
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(mm.data(), L.mm, mm.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "mm d2h");
         QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-        for (size_t i = 0; i < over.size(); i++) {
+        for (size_t i = 0; i < no; i++) {
             const PjCross &e = over[i];
-            if (mm[2 * i] == mm[2 * i + 1]) {
+            if (mm[i] == mm[no + i]) {
                 bigcnt[e.b] = (unsigned long long)e.rn * e.sn;
                 cross.push_back(e);
             } else {
