@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(RS_THREADS, 4)
 k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
              const qg_cdf_model *model, const uint32_t *__restrict__ dbase,
              uint32_t *__restrict__ status, qg_control *ctl, uint32_t spin_limit,
-             const unsigned long long *__restrict__ d_n) {
+             const unsigned long long *__restrict__ d_n, const uint32_t *__restrict__ trivial) {
     extern __shared__ __align__(16) unsigned char rs_raw[];
     RsSmem<KV3> &S = *reinterpret_cast<RsSmem<KV3> *>(rs_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -95,6 +95,40 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
     // tile before them waits on them).
     if (d_n && *d_n < (unsigned long long)n) n = (long long)*d_n;
     if ((long long)blockIdx.x * RS_TILE >= n) return;
+    if (trivial && __ldg(trivial)) {  // one digit value holds every item: a stable pass is the identity
+        // every load of the tile before any store (the buffers are distinct,
+        // which the compiler cannot see)
+        const long long b0 = (long long)blockIdx.x * RS_TILE;
+        const int cnt = (int)min((long long)RS_TILE, n - b0);
+        unsigned long long v[RS_ITEMS];
+        uint32_t kk[KV3 ? RS_ITEMS : 1];
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; i++) {
+            const int j = i * RS_THREADS + tid;
+            if (j < cnt) {
+                if (KV3) {
+                    kk[i] = __ldcs(src.k + b0 + j);
+                    v[i] = ((unsigned long long)__ldcs(src.b + b0 + j) << 32) | __ldcs(src.a + b0 + j);
+                } else {
+                    v[i] = __ldcs(src.rec + b0 + j);
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; i++) {
+            const int j = i * RS_THREADS + tid;
+            if (j < cnt) {
+                if (KV3) {
+                    dst.k[b0 + j] = kk[i];
+                    dst.a[b0 + j] = (uint32_t)v[i];
+                    dst.b[b0 + j] = (uint32_t)(v[i] >> 32);
+                } else {
+                    dst.rec[b0 + j] = v[i];
+                }
+            }
+        }
+        return;
+    }
     for (int i = tid; i < RS_WARPS * QG_RADIX; i += RS_THREADS) (&S.whist[0][0])[i] = 0;
     __syncthreads();
     // Tile i is CTA i (started in index order); the status words are cleared
@@ -322,13 +356,13 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
         qg_pre_launch(ctx);
         if (kv3)
             k_radix_pass<true, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr);
+                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
         else if (pf.learned)
             k_radix_pass<false, true><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, 0u, pf.model, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr);
+                s, d, n, shift, 0u, pf.model, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
         else
             k_radix_pass<false, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr);
+                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
         in_a = !in_a;
     }
@@ -336,9 +370,12 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
     return QG_OK;
 }
 
-// Exclusive digit bases of every position from a device histogram [npos][256].
-__global__ void k_radix_bases(const uint32_t *__restrict__ hist, int npos, uint32_t *__restrict__ bases) {
-    __shared__ uint32_t ws[QG_RADIX / 32];
+// Exclusive digit bases of every position from a device histogram [npos][256];
+// trivial[p] = 1 when one digit value holds every item of position p (that
+// pass is then a copy).
+__global__ void k_radix_bases(const uint32_t *__restrict__ hist, int npos, uint32_t *__restrict__ bases,
+                              uint32_t *__restrict__ trivial) {
+    __shared__ uint32_t ws[QG_RADIX / 32], wm[QG_RADIX / 32];
     const int d = threadIdx.x, lane = d & 31, w = d >> 5;
     for (int p = 0; p < npos; p++) {
         const uint32_t c = hist[p * QG_RADIX + d];
@@ -348,11 +385,21 @@ __global__ void k_radix_bases(const uint32_t *__restrict__ hist, int npos, uint3
             const uint32_t x = __shfl_up_sync(QG_FULL_MASK, inc, k);
             if (lane >= k) inc += x;
         }
+        const uint32_t mx = __reduce_max_sync(QG_FULL_MASK, c);
         if (lane == 31) ws[w] = inc;
+        if (lane == 0) wm[w] = mx;
         __syncthreads();
         uint32_t off = 0;
         for (int i = 0; i < w; i++) off += ws[i];
         bases[p * QG_RADIX + d] = off + inc - c;
+        if (d == 0) {
+            uint32_t tot = 0, big = 0;
+            for (int i = 0; i < QG_RADIX / 32; i++) {
+                tot += ws[i];
+                big = max(big, wm[i]);
+            }
+            trivial[p] = big == tot ? 1u : 0u;
+        }
         __syncthreads();
     }
 }
@@ -365,12 +412,13 @@ qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_buf
     if (n_bound >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
     const long long tiles = (n_bound + RS_TILE - 1) / RS_TILE;
     uint32_t *dbase = (uint32_t *)work;
-    uint32_t *status = dbase + 4 * QG_RADIX;
+    uint32_t *trivial = dbase + 4 * QG_RADIX;  // [4], in a 256-byte slot
+    uint32_t *status = trivial + 64;
     const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
     if (kv3) QG_TRY((rs_set_attr<true, false>(ctx)));
     else QG_TRY((rs_set_attr<false, false>(ctx)));
     qg_pre_launch(ctx);
-    k_radix_bases<<<1, QG_RADIX, 0, ctx->stream>>>(d_hist, npos, dbase);
+    k_radix_bases<<<1, QG_RADIX, 0, ctx->stream>>>(d_hist, npos, dbase, trivial);
     QG_TRY(qg_check_launch(ctx, "k_radix_bases"));
     bool in_a = true;
     for (int p = 0; p < npos; p++) {
@@ -380,10 +428,12 @@ qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_buf
         qg_pre_launch(ctx);
         if (kv3)
             k_radix_pass<true, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n);
+                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n,
+                trivial + p);
         else
             k_radix_pass<false, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n);
+                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n,
+                trivial + p);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
         in_a = !in_a;
     }
@@ -392,7 +442,7 @@ qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_buf
 }
 
 size_t qg_radix_dev_work_bytes(long long n_bound) {
-    return 4 * QG_RADIX * 4 + (size_t)((n_bound + RS_TILE - 1) / RS_TILE) * QG_RADIX * 4;
+    return 4 * QG_RADIX * 4 + 256 + (size_t)((n_bound + RS_TILE - 1) / RS_TILE) * QG_RADIX * 4;
 }
 
 qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,

@@ -66,7 +66,8 @@ def test_join_variants(ctx, orc, knobs, variant, nR, nS, kr, ks):
 @pytest.mark.parametrize("variant", [1, 2])
 def test_join_outside_buckets(ctx, orc, knobs, variant):
     # Tiny bucket capacities and few buckets: most buckets leave the bucket
-    # kernel -- heavy single keys become cross products, the rest recurse.
+    # kernel -- heavy single keys become cross products, the rest take the
+    # sort-merge path.
     knobs(variant, 4, 64, 32)
     rng = np.random.default_rng(5)
     base = rng.integers(0, 1 << 20, 3000)
@@ -80,6 +81,26 @@ def test_join_outside_buckets(ctx, orc, knobs, variant):
     st = ctx.join_stats()
     assert st["outside_buckets"] > 0
     exp = orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 499, cap=skey.size * 8, mt=True)
+    check_join(got, exp)
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_join_sort_merge_with_duplicate_build_keys(ctx, orc, knobs, variant):
+    # Every build key three times, tiny bucket capacities: the oversize buckets
+    # hold several keys each (the sort-merge path) and every probe row that
+    # hits matches three build rows.
+    knobs(variant, 6, 256, 96)
+    rng = np.random.default_rng(9)
+    keys = rng.choice(1 << 22, 20000, replace=False).astype(np.int32)
+    rkey = np.repeat(keys, 3)
+    rng.shuffle(rkey)
+    rpay = rng.integers(0, 1000, rkey.size).astype(np.int32)
+    skey = np.concatenate([rng.choice(keys, 150000), rng.integers(0, 1 << 22, 20000)]).astype(np.int32)
+    spay = rng.integers(0, 1000, skey.size).astype(np.int32)
+    got = ctx.join_filter_sort(dev(rkey), dev(rpay), dev(skey), dev(spay), -(2 ** 31), 599, cap=skey.size * 4)
+    st = ctx.join_stats()
+    assert st["merge_buckets"] > 0
+    exp = orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 599, cap=skey.size * 4, mt=True)
     check_join(got, exp)
 
 
