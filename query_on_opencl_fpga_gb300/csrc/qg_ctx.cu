@@ -70,6 +70,7 @@ QG_API qg_status qg_ctx_destroy(qg_ctx *ctx) {
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->pin_ctl) cudaFreeHost(ctx->pin_ctl);
     if (ctx->pin_bases) cudaFreeHost(ctx->pin_bases);
+    if (ctx->pin_join) cudaFreeHost(ctx->pin_join);
     for (int i = 0; i < 8; i++)
         if (ctx->pin_ev[i]) cudaEventDestroy(ctx->pin_ev[i]);
     free(ctx);

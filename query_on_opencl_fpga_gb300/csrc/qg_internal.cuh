@@ -46,6 +46,7 @@ struct qg_ctx {
     uint32_t pj_stats[8];   // last qg_join_filter_sort (see qg_join_stats)
     char *pj_tmp;           // the join's sort-merge arrays (grow-only)
     size_t pj_tmp_bytes;
+    void *pin_join;         // host pinned bucket bounds and group plan of the join (allocated on first use)
     char msg[256];
     // Per-kernel CUDA-event timing (qg_ctx_enable_timing): a pair of events
     // brackets every launch on the context's stream.

@@ -996,6 +996,36 @@ qg_status pj_judge(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot, c
     return QG_OK;
 }
 
+// Pinned host staging of one join's bucket bounds and group plan (grow-once:
+// sized for the largest bucket count).  The call ends with a stream sync, so
+// the next call may overwrite it.
+struct PjPlan {
+    uint32_t *rbk, *sbk;             // [nb + 1] first row of each fine bucket
+    uint32_t *gr, *gs;               // [G + 1] first row of each join group
+    uint32_t *big;                   // [G] 1: handled outside the bucket kernel
+    unsigned long long *bigcnt;      // [G] output rows of outside groups
+};
+
+qg_status pj_plan_host(qg_ctx *ctx, PjPlan *p) {
+    const size_t n = (size_t)PJ_MAX_BUCKETS + 2;
+    if (!ctx->pin_join) {
+        if (cudaMallocHost(&ctx->pin_join, n * (8 + 5 * 4)) != cudaSuccess) {
+            cudaGetLastError();
+            ctx->pin_join = nullptr;
+            return QG_ERR_OOM;
+        }
+    }
+    char *q = (char *)ctx->pin_join;
+    p->bigcnt = (unsigned long long *)q;
+    q += n * 8;
+    p->rbk = (uint32_t *)q;
+    p->sbk = p->rbk + n;
+    p->gr = p->sbk + n;
+    p->gs = p->gr + n;
+    p->big = p->gs + n;
+    return QG_OK;
+}
+
 // Partition, join groups, outside buckets.  mem: the level's arrays
 // (pj_level_bytes), carved here.
 qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
@@ -1077,47 +1107,46 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     qg_pre_launch(ctx);
     k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(s, nS, pf, nbu, L.sbk);
     QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
-    std::vector<uint32_t> rbk(nbu + 1), sbk(nbu + 1);
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(rbk.data(), L.rbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "rbk d2h");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(sbk.data(), L.sbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "sbk d2h");
+    PjPlan P;
+    QG_TRY(pj_plan_host(ctx, &P));
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(P.rbk, L.rbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "rbk d2h");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(P.sbk, L.sbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "sbk d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
 
     // Pack consecutive fine buckets into join groups up to the bucket
     // kernel's capacity.  A bucket above it is a group of its own, handled
-    // outside the kernel when both sides have rows (flag 1) and skipped when
-    // one side is empty (flag 2).
-    std::vector<uint32_t> gr{0}, gs{0}, big;
+    // outside the kernel (flag 1): listed in `over` when both sides have rows,
+    // an empty group otherwise.  The plan is written straight into pinned
+    // memory (one pass, no per-group allocation).
     std::vector<PjCross> over;
+    uint32_t G = 0;
     {
-        uint32_t cr = 0, cs = 0;
+        const uint32_t *R = P.rbk, *S = P.sbk;
+        const uint32_t rmax = g_pj_rmax, smax = g_pj_smax;
+        uint32_t r0 = 0, s0 = 0;  // first rows of the open group
         bool open = false;
-        auto close = [&](uint32_t b) {
-            if (open) { gr.push_back(rbk[b]); gs.push_back(sbk[b]); big.push_back(0); }
-            open = false;
-            cr = cs = 0;
-        };
+        P.gr[0] = R[0];
+        P.gs[0] = S[0];
         for (uint32_t b = 0; b < nbu; b++) {
-            const uint32_t rc = rbk[b + 1] - rbk[b], sc = sbk[b + 1] - sbk[b];
-            if (rc > g_pj_rmax || sc > g_pj_smax) {
-                close(b);
-                gr.push_back(rbk[b + 1]);
-                gs.push_back(sbk[b + 1]);
-                const bool joinable = rc && sc;
-                big.push_back(joinable ? 1u : 2u);
-                if (joinable) over.push_back(PjCross{(uint32_t)(big.size() - 1), rbk[b], rc, sbk[b], sc});
+            const uint32_t rb = R[b], sb = S[b], re = R[b + 1], se = S[b + 1];
+            if (re - rb > rmax || se - sb > smax) {
+                if (open) {
+                    P.gr[G + 1] = rb; P.gs[G + 1] = sb; P.big[G] = 0; P.bigcnt[G] = 0; G++;
+                    open = false;
+                }
+                if (re > rb && se > sb) over.push_back(PjCross{G, rb, re - rb, sb, se - sb});
+                P.gr[G + 1] = re; P.gs[G + 1] = se; P.big[G] = 1; P.bigcnt[G] = 0; G++;
                 continue;
             }
-            if (cr + rc > g_pj_rmax || cs + sc > g_pj_smax) close(b);
-            cr += rc;
-            cs += sc;
-            open = true;
+            if (open && (re - r0 > rmax || se - s0 > smax)) {
+                P.gr[G + 1] = rb; P.gs[G + 1] = sb; P.big[G] = 0; P.bigcnt[G] = 0; G++;
+                open = false;
+            }
+            if (!open) { r0 = rb; s0 = sb; open = true; }
         }
-        close(nbu);
+        if (open) { P.gr[G + 1] = R[nbu]; P.gs[G + 1] = S[nbu]; P.big[G] = 0; P.bigcnt[G] = 0; G++; }
     }
-    const uint32_t G = (uint32_t)big.size();
-    std::vector<unsigned long long> bigcnt(G, 0);
-    std::vector<uint32_t> bigflag(G, 0);
-    for (uint32_t g = 0; g < G; g++) bigflag[g] = big[g] ? 1u : 0u;
+    unsigned long long *bigcnt = P.bigcnt;
 
     // Outside groups: a bucket with one key is a cross product (k_pj_cross);
     // the others all go through the sort-merge path together (k_pj_mj_*).
@@ -1150,10 +1179,10 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
             }
         }
     }
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gr, gr.data(), (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gr h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gs, gs.data(), (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gs h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.big, bigflag.data(), (size_t)G * 4, cudaMemcpyHostToDevice, ctx->stream), "big h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.bigcnt, bigcnt.data(), (size_t)G * 8, cudaMemcpyHostToDevice, ctx->stream), "bigcnt h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gr, P.gr, (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gr h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gs, P.gs, (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gs h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.big, P.big, (size_t)G * 4, cudaMemcpyHostToDevice, ctx->stream), "big h2d");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.bigcnt, P.bigcnt, (size_t)G * 8, cudaMemcpyHostToDevice, ctx->stream), "bigcnt h2d");
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mjtot, 0, 8, ctx->stream), "memset mjtot");
 
     // sort-merge buckets: gather, sort by key, count each S row's matches
