@@ -177,7 +177,7 @@ constexpr int PJ_MAX_BUCKETS = 1 << 16;  // two 8-bit partition passes
 // privatised), for the partition passes' digit bases.
 __global__ void __launch_bounds__(256)
 k_pj_dhist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn pf, uint32_t nb,
-           uint32_t *__restrict__ hist, qg_control *ctl) {
+           uint32_t *__restrict__ hist, qg_control *ctl, uint16_t *__restrict__ bid) {
     __shared__ uint32_t h[2][256];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) (&h[0][0])[i] = 0;
     __syncthreads();
@@ -188,6 +188,7 @@ k_pj_dhist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn p
             qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_HIST);
             continue;
         }
+        if (bid) bid[i] = (uint16_t)b;  // nb <= 2^16: the id for the partition passes
         atomicAdd(&h[0][b & 255u], 1u);
         atomicAdd(&h[1][b >> 8], 1u);
     }
@@ -930,16 +931,17 @@ int pj_grid(qg_ctx *ctx, long long work, int per_block, int per_sm) {
     return (int)b;
 }
 
-// Digit histograms of both sides' bucket ids into h[0 .. 1024) (synchronises).
+// Digit histograms of both sides' bucket ids into h[0 .. 1024) (synchronises);
+// with bid_r / bid_s set, every row's bucket id is also written there.
 qg_status pj_dhist(qg_ctx *ctx, const PjLevel &L, const qg_part_fn &pf, uint32_t nb,
                    const unsigned long long *r, long long nR, const unsigned long long *s, long long nS,
-                   uint32_t *h) {
+                   uint32_t *h, uint16_t *bid_r = nullptr, uint16_t *bid_s = nullptr) {
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 4 * 256 * 4, ctx->stream), "memset dhist");
     qg_pre_launch(ctx);
-    k_pj_dhist<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, pf, nb, L.dh, ctx->ctl);
+    k_pj_dhist<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, pf, nb, L.dh, ctx->ctl, bid_r);
     QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     qg_pre_launch(ctx);
-    k_pj_dhist<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl);
+    k_pj_dhist<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl, bid_s);
     QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
@@ -1079,7 +1081,19 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
         QG_TRY(pj_judge(ctx, L, m, ntot, radix, nb_radix, learned, nb, &orad, &olrn));
         use_learned = olrn < 0.5 * orad;
     }
-    if (use_learned) QG_TRY(pj_dhist(ctx, L, learned, nb, r, nR, s, nS, h));
+    // The learned function is evaluated once per row: its bucket ids go to a
+    // sidecar that the partition passes carry along (ping-pong per side).
+    uint16_t *bidr[2] = {nullptr, nullptr}, *bids[2] = {nullptr, nullptr};
+    if (use_learned) {
+        const size_t rb2 = qg_align_up((size_t)nR * 2, 256), sb2 = qg_align_up((size_t)nS * 2, 256);
+        char *side;
+        QG_TRY(pj_pool_get(ctx, &ctx->pj_tmp, &ctx->pj_tmp_bytes, 2 * rb2 + 2 * sb2, &side));
+        bidr[0] = (uint16_t *)side;
+        bidr[1] = (uint16_t *)(side + rb2);
+        bids[0] = (uint16_t *)(side + 2 * rb2);
+        bids[1] = (uint16_t *)(side + 2 * rb2 + sb2);
+        QG_TRY(pj_dhist(ctx, L, learned, nb, r, nR, s, nS, h, bidr[0], bids[0]));
+    }
     const qg_part_fn &pf = use_learned ? learned : radix;
     const uint32_t nbu = use_learned ? nb : nb_radix;
 
@@ -1091,13 +1105,15 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
         bool in_b = false;
         memcpy(hist, h, 512 * 4);
         np = qg_sort_plan(hist, npos, nR, passes, bases);
-        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{r, nullptr, nullptr, nullptr},
-                                  qg_sort_bufs{rsp, nullptr, nullptr, nullptr}, nR, pf, passes, np, bases, &in_b));
+        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{r, nullptr, nullptr, nullptr, bidr[0]},
+                                  qg_sort_bufs{rsp, nullptr, nullptr, nullptr, bidr[1]}, nR, pf, passes, np, bases,
+                                  &in_b));
         if (in_b) std::swap(r, rsp);
         memcpy(hist, h + 512, 512 * 4);
         np = qg_sort_plan(hist, npos, nS, passes, bases);
-        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{s, nullptr, nullptr, nullptr},
-                                  qg_sort_bufs{ssp, nullptr, nullptr, nullptr}, nS, pf, passes, np, bases, &in_b));
+        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{s, nullptr, nullptr, nullptr, bids[0]},
+                                  qg_sort_bufs{ssp, nullptr, nullptr, nullptr, bids[1]}, nS, pf, passes, np, bases,
+                                  &in_b));
         if (in_b) std::swap(s, ssp);
     }
     // fine bucket bounds

@@ -56,7 +56,7 @@ k_radix_hist(const uint32_t *__restrict__ kin, const unsigned long long *__restr
     }
 }
 
-template <bool KV3>
+template <bool KV3, bool SIDE = false>
 struct RsSmem {
     uint32_t whist[RS_WARPS][QG_RADIX];
     uint32_t dstart[QG_RADIX];
@@ -66,6 +66,7 @@ struct RsSmem {
     // REC: v holds the u64 items; KV3: v holds (a, b) pairs and k the keys
     unsigned long long v[RS_TILE];
     uint32_t k[KV3 ? RS_TILE : 1];
+    uint16_t bid[SIDE ? RS_TILE : 1];  // REC with a bucket-id sidecar: the reordered ids
     uint8_t dg[RS_TILE];  // digit of each reordered item
 };
 
@@ -81,14 +82,17 @@ __device__ __forceinline__ uint32_t rs_digit(uint32_t k, uint32_t key_off, int s
 // Four CTAs per SM (64 registers; a few bytes spill): one CTA's load phase
 // overlaps another's ranking and writes.  Three passes over 64M REC items
 // took 1.29 ms this way against 1.57 ms with two CTAs at 126 registers.
-template <bool KV3, bool LEARNED>
+// DIG: 0 radix digit of the key, 1 learned partition function of the key,
+// 2 bits of the bucket id in the source's sidecar (REC only).
+template <bool KV3, int DIG>
 __global__ void __launch_bounds__(RS_THREADS, 4)
 k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
              const qg_cdf_model *model, const uint32_t *__restrict__ dbase,
              uint32_t *__restrict__ status, qg_control *ctl, uint32_t spin_limit,
              const unsigned long long *__restrict__ d_n, const uint32_t *__restrict__ trivial) {
     extern __shared__ __align__(16) unsigned char rs_raw[];
-    RsSmem<KV3> &S = *reinterpret_cast<RsSmem<KV3> *>(rs_raw);
+    constexpr bool side = !KV3 && DIG == 2;  // digits from the bucket-id sidecar
+    RsSmem<KV3, side> &S = *reinterpret_cast<RsSmem<KV3, side> *>(rs_raw);
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // Item count known only on the device (graph-captured sorts): the grid
     // covers the bound n, and CTAs past the real count leave at once (no
@@ -124,6 +128,7 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
                     dst.b[b0 + j] = (uint32_t)(v[i] >> 32);
                 } else {
                     dst.rec[b0 + j] = v[i];
+                    if (side && dst.bid) dst.bid[b0 + j] = src.bid[b0 + j];
                 }
             }
         }
@@ -155,10 +160,12 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
                 val[i] = ((unsigned long long)__ldcs(src.b + idx) << 32) | __ldcs(src.a + idx);
             } else {
                 val[i] = __ldcs(src.rec + idx);
+                if (side) rd[i] = __ldcs(src.bid + idx);  // the bucket id, until its digit replaces it
             }
         } else {
             val[i] = 0;
             if (KV3) key[i] = 0;
+            if (side) rd[i] = 0;
         }
     }
 #pragma unroll
@@ -166,7 +173,7 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
         long long idx = wbase + i * 32 + lane;
         bool valid = idx < n;
         const uint32_t ki = KV3 ? key[i] : (uint32_t)(val[i] >> 32);
-        uint32_t d = rs_digit<LEARNED>(ki, key_off, shift, model);
+        const uint32_t d = side ? (rd[i] >> shift) & 255u : rs_digit<DIG == 1>(ki, key_off, shift, model);
         rd[i] = d << 24;
         uint32_t peers = __ballot_sync(QG_FULL_MASK, valid);
 #pragma unroll
@@ -258,6 +265,7 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
             S.v[pos] = val[i];
             S.dg[pos] = (uint8_t)d;
             if (KV3) S.k[pos] = key[i];
+            if (!KV3 && side && dst.bid) S.bid[pos] = __ldg(src.bid + idx);  // read again: no register held
         }
     }
     __syncthreads();
@@ -274,6 +282,7 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
             dst.b[g] = (uint32_t)(v >> 32);
         } else {
             dst.rec[g] = v;
+            if (side && dst.bid) dst.bid[g] = S.bid[p];
         }
     }
 }
@@ -316,12 +325,12 @@ int qg_sort_plan(const uint32_t *h_hist, int npos, long long n, int *passes, uin
     return np;
 }
 
-template <bool KV3, bool LEARNED>
+template <bool KV3, int DIG>
 static qg_status rs_set_attr(qg_ctx *ctx) {
     static bool done = false;
     if (!done) {
-        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, LEARNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)sizeof(RsSmem<KV3>)), "attr");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
         done = true;
     }
     return QG_OK;
@@ -342,26 +351,34 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
     uint32_t *status = dbase + 4 * QG_RADIX;
     // 4 KB of digit bases, in stream order before the passes that read them.
     QG_TRY(qg_stage_bases(ctx, h_bases, dbase));
-    const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
-    if (kv3) QG_TRY((rs_set_attr<true, false>(ctx)));
-    else if (pf.learned) QG_TRY((rs_set_attr<false, true>(ctx)));
-    else QG_TRY((rs_set_attr<false, false>(ctx)));
+    // REC items with a bucket-id sidecar: digits come from the sidecar, whatever
+    // the partition function (it was evaluated once, when the ids were written).
+    const bool side = !kv3 && a.bid != nullptr && b.bid != nullptr;
+    const size_t smem = kv3 ? sizeof(RsSmem<true>) : side ? sizeof(RsSmem<false, true>) : sizeof(RsSmem<false>);
+    if (kv3) QG_TRY((rs_set_attr<true, 0>(ctx)));
+    else if (side) QG_TRY((rs_set_attr<false, 2>(ctx)));
+    else if (pf.learned) QG_TRY((rs_set_attr<false, 1>(ctx)));
+    else QG_TRY((rs_set_attr<false, 0>(ctx)));
     bool in_a = true;
     for (int i = 0; i < np; i++) {
         const int p = passes[i];
         QG_TRY_CUDA(ctx, cudaMemsetAsync(status, 0, (size_t)tiles * QG_RADIX * 4, ctx->stream), "memset status");
         const qg_sort_bufs &s = in_a ? a : b;
-        const qg_sort_bufs &d = in_a ? b : a;
-        const int shift = pf.learned ? 8 * p : pf.shift + 8 * p;
+        qg_sort_bufs d = in_a ? b : a;
+        if (side && i == np - 1) d.bid = nullptr;  // the last pass's ids are not read again
+        const int shift = (pf.learned || side) ? 8 * p : pf.shift + 8 * p;
         qg_pre_launch(ctx);
         if (kv3)
-            k_radix_pass<true, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+            k_radix_pass<true, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
                 s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
+        else if (side)
+            k_radix_pass<false, 2><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+                s, d, n, shift, 0u, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
         else if (pf.learned)
-            k_radix_pass<false, true><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+            k_radix_pass<false, 1><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
                 s, d, n, shift, 0u, pf.model, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
         else
-            k_radix_pass<false, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+            k_radix_pass<false, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
                 s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
         in_a = !in_a;
@@ -415,8 +432,8 @@ qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_buf
     uint32_t *trivial = dbase + 4 * QG_RADIX;  // [4], in a 256-byte slot
     uint32_t *status = trivial + 64;
     const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
-    if (kv3) QG_TRY((rs_set_attr<true, false>(ctx)));
-    else QG_TRY((rs_set_attr<false, false>(ctx)));
+    if (kv3) QG_TRY((rs_set_attr<true, 0>(ctx)));
+    else QG_TRY((rs_set_attr<false, 0>(ctx)));
     qg_pre_launch(ctx);
     k_radix_bases<<<1, QG_RADIX, 0, ctx->stream>>>(d_hist, npos, dbase, trivial);
     QG_TRY(qg_check_launch(ctx, "k_radix_bases"));
@@ -427,11 +444,11 @@ qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_buf
         const qg_sort_bufs &d = in_a ? b : a;
         qg_pre_launch(ctx);
         if (kv3)
-            k_radix_pass<true, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+            k_radix_pass<true, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
                 s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n,
                 trivial + p);
         else
-            k_radix_pass<false, false><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
+            k_radix_pass<false, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
                 s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n,
                 trivial + p);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));

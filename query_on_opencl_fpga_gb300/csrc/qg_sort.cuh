@@ -6,11 +6,17 @@ constexpr int QG_RADIX = 256;
 
 // Buffers of one side of the ping-pong: REC uses `rec` (u64 items, key in the
 // high word); KV3 uses the three u32 columns k (key), a, b.
+// REC items may carry a sidecar of 16-bit bucket ids (bid, aligned with rec):
+// a pass whose source has one takes its digits from it instead of computing
+// them, and writes the reordered ids to the destination's sidecar if that has
+// one (a learned partition function is then evaluated once per row, not once
+// per pass).
 struct qg_sort_bufs {
     unsigned long long *rec;
     uint32_t *k;
     uint32_t *a;
     uint32_t *b;
+    uint16_t *bid;
 };
 
 // Number of 8-bit digit positions covering `bits` key bits (1..4).
