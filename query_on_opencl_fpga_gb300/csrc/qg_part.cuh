@@ -41,25 +41,74 @@ struct qg_part_fn {
     const qg_cdf_model *model;      // learned: device model
 };
 
-__device__ __forceinline__ uint32_t qg_cdf_bucket(const qg_cdf_model *__restrict__ m, uint32_t u) {
-    const uint32_t K = __ldg(&m->nknots);
-    const uint32_t x0 = __ldg(&m->x[0]);
-    if (u <= x0) return u == x0 ? __ldg(&m->bk[0]) : 0u;
-    const uint32_t xl = __ldg(&m->x[K - 1]);
-    if (u >= xl) return u == xl ? __ldg(&m->bk[K - 1]) : __ldg(&m->nbuckets) - 1u;
+// The model may live in global memory (read through the read-only cache) or
+// in shared memory (a kernel that evaluates it for every row stages a copy).
+template <bool SHARED>
+__device__ __forceinline__ uint32_t qg_cdf_ld(const uint32_t *p) { return SHARED ? *p : __ldg(p); }
+template <bool SHARED>
+__device__ __forceinline__ float qg_cdf_ldf(const float *p) { return SHARED ? *p : __ldg(p); }
+
+template <bool SHARED>
+__device__ __forceinline__ uint32_t qg_cdf_bucket_t(const qg_cdf_model *__restrict__ m, uint32_t u) {
+    const uint32_t K = qg_cdf_ld<SHARED>(&m->nknots);
+    const uint32_t x0 = qg_cdf_ld<SHARED>(&m->x[0]);
+    if (u <= x0) return u == x0 ? qg_cdf_ld<SHARED>(&m->bk[0]) : 0u;
+    const uint32_t xl = qg_cdf_ld<SHARED>(&m->x[K - 1]);
+    if (u >= xl) return u == xl ? qg_cdf_ld<SHARED>(&m->bk[K - 1]) : qg_cdf_ld<SHARED>(&m->nbuckets) - 1u;
     // Largest i with x[i] <= u lies in [idx[t], idx[t+1]]; x[hi] > u.
-    const uint32_t t = (u - x0) >> __ldg(&m->ishift);
-    uint32_t lo = __ldg(&m->idx[t]);
-    uint32_t hi = min(__ldg(&m->idx[t + 1]) + 1u, K - 1u);
+    const uint32_t t = (u - x0) >> qg_cdf_ld<SHARED>(&m->ishift);
+    uint32_t lo = qg_cdf_ld<SHARED>(&m->idx[t]);
+    uint32_t hi = min(qg_cdf_ld<SHARED>(&m->idx[t + 1]) + 1u, K - 1u);
     while (hi - lo > 1) {
         const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&m->x[mid]) <= u) lo = mid;
+        if (qg_cdf_ld<SHARED>(&m->x[mid]) <= u) lo = mid;
         else hi = mid;
     }
-    const uint32_t xi = __ldg(&m->x[lo]);
-    if (u == xi) return __ldg(&m->bk[lo]);
-    const uint32_t b0 = __ldg(&m->b0[lo]), span = __ldg(&m->b1[lo]) - b0;
-    const float f = __ldg(&m->slope[lo]) * (float)(u - xi - 1u);
+    const uint32_t xi = qg_cdf_ld<SHARED>(&m->x[lo]);
+    if (u == xi) return qg_cdf_ld<SHARED>(&m->bk[lo]);
+    const uint32_t b0 = qg_cdf_ld<SHARED>(&m->b0[lo]), span = qg_cdf_ld<SHARED>(&m->b1[lo]) - b0;
+    const float f = qg_cdf_ldf<SHARED>(&m->slope[lo]) * (float)(u - xi - 1u);
+    return b0 + (f >= (float)span ? span : (uint32_t)f);
+}
+
+__device__ __forceinline__ uint32_t qg_cdf_bucket(const qg_cdf_model *__restrict__ m, uint32_t u) {
+    return qg_cdf_bucket_t<false>(m, u);
+}
+
+// The model's scalar fields, read once by a kernel that evaluates many keys.
+struct qg_cdf_head {
+    uint32_t K, x0, xl, ishift, nb1, bk0, bkl;
+};
+template <bool SHARED>
+__device__ __forceinline__ qg_cdf_head qg_cdf_load_head(const qg_cdf_model *__restrict__ m) {
+    qg_cdf_head h;
+    h.K = qg_cdf_ld<SHARED>(&m->nknots);
+    h.x0 = qg_cdf_ld<SHARED>(&m->x[0]);
+    h.xl = qg_cdf_ld<SHARED>(&m->x[h.K - 1]);
+    h.ishift = qg_cdf_ld<SHARED>(&m->ishift);
+    h.nb1 = qg_cdf_ld<SHARED>(&m->nbuckets) - 1u;
+    h.bk0 = qg_cdf_ld<SHARED>(&m->bk[0]);
+    h.bkl = qg_cdf_ld<SHARED>(&m->bk[h.K - 1]);
+    return h;
+}
+// qg_cdf_bucket_t with the scalar fields already in registers.
+template <bool SHARED>
+__device__ __forceinline__ uint32_t qg_cdf_bucket_h(const qg_cdf_model *__restrict__ m, const qg_cdf_head &h,
+                                                    uint32_t u) {
+    if (u <= h.x0) return u == h.x0 ? h.bk0 : 0u;
+    if (u >= h.xl) return u == h.xl ? h.bkl : h.nb1;
+    const uint32_t t = (u - h.x0) >> h.ishift;
+    uint32_t lo = qg_cdf_ld<SHARED>(&m->idx[t]);
+    uint32_t hi = min(qg_cdf_ld<SHARED>(&m->idx[t + 1]) + 1u, h.K - 1u);
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (qg_cdf_ld<SHARED>(&m->x[mid]) <= u) lo = mid;
+        else hi = mid;
+    }
+    const uint32_t xi = qg_cdf_ld<SHARED>(&m->x[lo]);
+    if (u == xi) return qg_cdf_ld<SHARED>(&m->bk[lo]);
+    const uint32_t b0 = qg_cdf_ld<SHARED>(&m->b0[lo]), span = qg_cdf_ld<SHARED>(&m->b1[lo]) - b0;
+    const float f = qg_cdf_ldf<SHARED>(&m->slope[lo]) * (float)(u - xi - 1u);
     return b0 + (f >= (float)span ? span : (uint32_t)f);
 }
 

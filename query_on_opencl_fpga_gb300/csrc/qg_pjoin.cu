@@ -175,15 +175,28 @@ constexpr int PJ_MAX_BUCKETS = 1 << 16;  // two 8-bit partition passes
 
 // Histograms of the two 8-bit digits of each row's bucket (shared-memory
 // privatised), for the partition passes' digit bases.
+template <bool LEARNED>
 __global__ void __launch_bounds__(256)
 k_pj_dhist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn pf, uint32_t nb,
            uint32_t *__restrict__ hist, qg_control *ctl, uint16_t *__restrict__ bid) {
     __shared__ uint32_t h[2][256];
+    // A learned function is evaluated from a shared-memory copy of the model.
+    __shared__ __align__(16) unsigned char sm_model[LEARNED ? sizeof(qg_cdf_model) : 16];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) (&h[0][0])[i] = 0;
+    if (LEARNED) {
+        static_assert(sizeof(qg_cdf_model) % 4 == 0, "model copied in words");
+        const uint32_t *gsrc = reinterpret_cast<const uint32_t *>(pf.model);
+        uint32_t *sdst = reinterpret_cast<uint32_t *>(sm_model);
+        for (int i = threadIdx.x; i < (int)(sizeof(qg_cdf_model) / 4); i += blockDim.x) sdst[i] = __ldg(gsrc + i);
+    }
     __syncthreads();
+    const qg_cdf_model *sm = reinterpret_cast<const qg_cdf_model *>(sm_model);
+    qg_cdf_head hd{};
+    if (LEARNED) hd = qg_cdf_load_head<true>(sm);
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t b = qg_part_bucket(pf, (uint32_t)(__ldg(rec + i) >> 32));
+        const uint32_t u = (uint32_t)(__ldg(rec + i) >> 32);
+        const uint32_t b = LEARNED ? qg_cdf_bucket_h<true>(sm, hd, u) : qg_part_bucket(pf, u);
         if (b >= nb) {  // a key outside the partition function's domain
             qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_HIST);
             continue;
@@ -272,9 +285,24 @@ __device__ long long smp_upper(const unsigned long long *s, long long m, uint32_
 constexpr int FIT_THREADS = 1024;
 constexpr int FIT_SORT = 2048;  // >= QG_CDF_MAX_KNOTS, power of two
 
+// Heavy keys of the sorted sample: runs of at least hthr equal keys (the
+// first QG_CDF_MAX_HEAVY found are kept; which ones, when there are more,
+// changes only where rows are processed).  heavy[0] counts them, heavy[1..]
+// holds them; heavy[0] is zero on entry.
+__global__ void __launch_bounds__(256)
+k_cdf_heavy(const unsigned long long *__restrict__ smp, long long m, long long hthr, uint32_t *__restrict__ heavy) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+        const uint32_t u = smp_key(smp, i);
+        if (i > 0 && smp_key(smp, i - 1) == u) continue;
+        if (i + hthr - 1 >= m || smp_key(smp, i + hthr - 1) != u) continue;
+        const uint32_t h = atomicAdd(heavy, 1u);
+        if (h < QG_CDF_MAX_HEAVY) heavy[1 + h] = u;
+    }
+}
+
 __global__ void __launch_bounds__(FIT_THREADS)
 k_cdf_fit(const unsigned long long *__restrict__ smp, long long m, uint32_t nb, long long hthr,
-          qg_cdf_model *__restrict__ model) {
+          const uint32_t *__restrict__ heavy, qg_cdf_model *__restrict__ model) {
     __shared__ uint32_t cand[FIT_SORT];
     __shared__ uint32_t ncand;
     __shared__ uint32_t s_heavy_n;
@@ -289,14 +317,11 @@ k_cdf_fit(const unsigned long long *__restrict__ smp, long long m, uint32_t nb, 
     }
     if (tid == 0) ncand = QG_CDF_SEGMENTS + 1;
     __syncthreads();
-    // heavy keys: runs of at least hthr equal keys in the sorted sample
-    for (long long i = tid; i < m; i += FIT_THREADS) {
-        const uint32_t u = smp_key(smp, i);
-        if (i > 0 && smp_key(smp, i - 1) == u) continue;
-        if (i + hthr - 1 >= m || smp_key(smp, i + hthr - 1) != u) continue;
-        const uint32_t h = atomicAdd(&s_heavy_n, 1u);
-        if (h < QG_CDF_MAX_HEAVY) cand[QG_CDF_SEGMENTS + 1 + h] = u;
-    }
+    // heavy keys (k_cdf_heavy)
+    if (tid == 0) s_heavy_n = heavy[0];
+    __syncthreads();
+    for (uint32_t h = tid; h < min(s_heavy_n, (uint32_t)QG_CDF_MAX_HEAVY); h += FIT_THREADS)
+        cand[QG_CDF_SEGMENTS + 1 + h] = heavy[1 + h];
     __syncthreads();
     // bitonic sort of the candidates (unused entries are 0xffffffff and sort last)
     for (int k = 2; k <= FIT_SORT; k <<= 1) {
@@ -843,6 +868,7 @@ struct PjLevel {
     PjMj *mj;
     unsigned long long *mjtot;  // matches of the sort-merge buckets
     qg_cdf_model *model;             // learned model (top level only)
+    uint32_t *heavy;                 // [1 + QG_CDF_MAX_HEAVY] heavy keys of the sample
     unsigned long long *smp, *smp2;  // key sample (top level only)
 };
 
@@ -863,6 +889,7 @@ size_t pj_level_bytes(uint32_t nb, bool learned) {
     add(8);
     if (learned) {
         add(sizeof(qg_cdf_model));
+        add((size_t)(1 + QG_CDF_MAX_HEAVY) * 4);
         add((size_t)CDF_SAMPLE * 8);
         add((size_t)CDF_SAMPLE * 8);
     }
@@ -887,9 +914,11 @@ void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     L->mj = (PjMj *)take((size_t)nb * sizeof(PjMj));
     L->mjtot = (unsigned long long *)take(8);
     L->model = nullptr;
+    L->heavy = nullptr;
     L->smp = L->smp2 = nullptr;
     if (learned) {
         L->model = (qg_cdf_model *)take(sizeof(qg_cdf_model));
+        L->heavy = (uint32_t *)take((size_t)(1 + QG_CDF_MAX_HEAVY) * 4);
         L->smp = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
         L->smp2 = (unsigned long long *)take((size_t)CDF_SAMPLE * 8);
     }
@@ -938,10 +967,11 @@ qg_status pj_dhist(qg_ctx *ctx, const PjLevel &L, const qg_part_fn &pf, uint32_t
                    uint32_t *h, uint16_t *bid_r = nullptr, uint16_t *bid_s = nullptr) {
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 4 * 256 * 4, ctx->stream), "memset dhist");
     qg_pre_launch(ctx);
-    k_pj_dhist<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, pf, nb, L.dh, ctx->ctl, bid_r);
+    auto kern = pf.learned ? k_pj_dhist<true> : k_pj_dhist<false>;
+    kern<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, pf, nb, L.dh, ctx->ctl, bid_r);
     QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     qg_pre_launch(ctx);
-    k_pj_dhist<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl, bid_s);
+    kern<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl, bid_s);
     QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
@@ -963,8 +993,12 @@ qg_status pj_train(qg_ctx *ctx, const PjLevel &L, uint32_t nb, const unsigned lo
     QG_TRY(qg_sort_rec_inplace(ctx, L.smp, L.smp2, m));
     long long hthr = (3 * m + nb - 1) / nb;
     if (hthr < 2) hthr = 2;
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(L.heavy, 0, 4, ctx->stream), "memset heavy");
     qg_pre_launch(ctx);
-    k_cdf_fit<<<1, FIT_THREADS, 0, ctx->stream>>>(L.smp, m, nb, hthr, L.model);
+    k_cdf_heavy<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(L.smp, m, hthr, L.heavy);
+    QG_TRY(qg_check_launch(ctx, "k_cdf_heavy"));
+    qg_pre_launch(ctx);
+    k_cdf_fit<<<1, FIT_THREADS, 0, ctx->stream>>>(L.smp, m, nb, hthr, L.heavy, L.model);
     QG_TRY(qg_check_launch(ctx, "k_cdf_fit"));
     *m_out = m;
     return QG_OK;
@@ -1373,16 +1407,21 @@ extern "C" QG_API qg_status qg_part_learn(qg_ctx *ctx, const uint32_t *keys, int
         return QG_ERR_INVALID;
     const long long m = n < CDF_SAMPLE ? n : CDF_SAMPLE;
     char *aux;
-    QG_TRY(qg_aux(ctx, (size_t)m * 16 + 256, &aux));
+    QG_TRY(qg_aux(ctx, (size_t)m * 16 + (size_t)(1 + QG_CDF_MAX_HEAVY) * 4 + 256, &aux));
     unsigned long long *smp = (unsigned long long *)aux, *smp2 = smp + m;
+    uint32_t *heavy = (uint32_t *)(smp2 + m);
     qg_pre_launch(ctx);
     k_keys_to_items<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(keys, n, m, smp);
     QG_TRY(qg_check_launch(ctx, "k_keys_to_items"));
     QG_TRY(qg_sort_rec_inplace(ctx, smp, smp2, m));
     long long hthr = (3 * m + nbuckets - 1) / nbuckets;
     if (hthr < 2) hthr = 2;
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(heavy, 0, 4, ctx->stream), "memset heavy");
     qg_pre_launch(ctx);
-    k_cdf_fit<<<1, FIT_THREADS, 0, ctx->stream>>>(smp, m, nbuckets, hthr, (qg_cdf_model *)d_model);
+    k_cdf_heavy<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(smp, m, hthr, heavy);
+    QG_TRY(qg_check_launch(ctx, "k_cdf_heavy"));
+    qg_pre_launch(ctx);
+    k_cdf_fit<<<1, FIT_THREADS, 0, ctx->stream>>>(smp, m, nbuckets, hthr, heavy, (qg_cdf_model *)d_model);
     QG_TRY(qg_check_launch(ctx, "k_cdf_fit"));
     return qg_ctx_check(ctx);
 }
