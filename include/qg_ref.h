@@ -1,5 +1,5 @@
 /*
- * qg_ref.h -- the reference's operator surface (host/host/*.h of
+ * qg_ref.h -- the reference's operator surface (the host/host headers of
  * Xtra-Computing/Query_on_OpenCL_FPGA) over libqg.so.
  *
  * Same function names, argument order and meaning as the reference, so a

@@ -388,7 +388,6 @@ constexpr int GB_MAX_C = 256;  // pass-1 CTAs (one per SM)
 constexpr int P1_THREADS = 1024;
 constexpr int P2_THREADS = 256;
 constexpr int P2_TLOG2 = 11;  // pass-2 table slots (2048) + 1 for key 0xffffffff
-constexpr int HOT_MAX_PROBE = 4;
 constexpr int GB_SKETCH_WORDS = 8192;  // 16K 16-bit admission counters (32 KB)
 
 // In-place exclusive scan of a[0..L) in shared memory by the whole CTA;

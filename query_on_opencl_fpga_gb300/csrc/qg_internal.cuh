@@ -414,12 +414,6 @@ __device__ __forceinline__ void qg_tile_compact_offsets(uint32_t *s_woff, const 
     }
 }
 
-// Bulk prefetch of [p, p + bytes) into L2 by the TMA engine (no registers,
-// no shared memory).  p 16-byte aligned, bytes a multiple of 16.
-__device__ __forceinline__ void qg_prefetch_l2_bulk(const void *p, uint32_t bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
 // ---- mbarrier / bulk-copy (TMA engine) helpers (PTX ISA: mbarrier, cp.async.bulk)
 __device__ __forceinline__ uint32_t qg_smem_u32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);

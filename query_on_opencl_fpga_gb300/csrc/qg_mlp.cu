@@ -20,7 +20,8 @@
 namespace {
 
 constexpr int MI = 16, MH = 64;
-constexpr int P_W1 = 0, P_B1 = MI * MH, P_W2 = P_B1 + MH, P_B2 = P_W2 + MH;
+// parameter layout: W1 at 0, then b1, W2, b2
+constexpr int P_B1 = MI * MH, P_W2 = P_B1 + MH, P_B2 = P_W2 + MH;
 constexpr int NPARAM = P_B2 + 1;  // 1153
 
 // Forward for n samples; keeps the hidden pre-activations (for backward) when z != null.
