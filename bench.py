@@ -549,6 +549,10 @@ def run_only(args):
         ctx.join_set_knobs(max(args.variant, 0))
         fn = lambda: ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"],  # noqa: E731
                                           j["shi"], cap=int(n * 0.3) + 1024)
+    elif args.only == "batched":
+        print(json.dumps({"only": "batched", **batched_line(ctx, stream)}), flush=True)
+        ctx.close()
+        return
     elif args.only == "sort":
         n = rows or (1 << 26)
         from query_on_opencl_fpga_gb300.datagen import records, uniform_i32
@@ -574,7 +578,7 @@ def run_only(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--only", default=None, help="groupby|fused|filter|join|skew|sort: one operator alone")
+    ap.add_argument("--only", default=None, help="groupby|fused|filter|join|skew|sort|batched: one operator alone")
     ap.add_argument("--rows", type=int, default=0, help="row count for --only (default: the config size)")
     ap.add_argument("--variant", type=int, default=-1, help="column filter kernel variant for --only filter")
     ap.add_argument("--rows2", type=int, default=0, help="build-side rows for --only join")

@@ -276,6 +276,10 @@ QG_API qg_status qg_batch_check(qg_batch *b, void *stream);
 /* out4: group-by table slots log2, join table factor, best replay in us, graph nodes. */
 QG_API qg_status qg_batch_info(const qg_batch *b, int32_t *out4);
 QG_API qg_status qg_batch_destroy(qg_batch *b);
+/* Lanes of the batches created after this call (process-wide, 1..16; default
+ * 8): the queries are spread over that many streams, each with a private
+ * context, and the graph runs the lanes side by side. */
+QG_API qg_status qg_batch_set_lanes(int lanes);
 
 /* ---- learned cost model (no reference counterpart; it stands beside the
  * static unit-cost table of host/dynamic_programming.cpp:152-167) ----

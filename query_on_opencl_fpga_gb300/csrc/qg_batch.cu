@@ -17,6 +17,7 @@
 // variant comes from the query (chosen by the caller, e.g. by the learned
 // cost model) or is the default.  The batch owns a private context, so its
 // arenas are never moved by other calls.
+#include <algorithm>
 #include <vector>
 #include "qg_internal.cuh"
 
@@ -26,10 +27,21 @@ qg_status qg_join_hash_sort_async(qg_ctx *ctx, const int32_t *rkey, const int32_
                                   int64_t cap, int64_t *d_count);
 void qg_join_set_table_factor(int factor);
 
+// The queries are independent, so they are spread over lanes: each lane has
+// its own stream and private context (arenas, control block), and the graph
+// forks into the lanes and joins them, so that small queries run beside
+// large ones instead of one after another.
+constexpr int QG_BATCH_MAX_LANES = 16;
+static int g_batch_lanes = 8;
+
 struct qg_batch {
-    qg_ctx *own = nullptr;
-    cudaStream_t stream = nullptr;  // capture stream of the private context
+    int lanes = 1;
+    qg_ctx *own[QG_BATCH_MAX_LANES] = {};
+    cudaStream_t ls[QG_BATCH_MAX_LANES] = {};  // lane streams; lane 0's is the capture origin
+    cudaEvent_t fork = nullptr, join[QG_BATCH_MAX_LANES] = {};
+    cudaStream_t stream = nullptr;  // == ls[0]
     std::vector<qg_query> q;
+    std::vector<int> lane;  // lane of each query
     cudaGraphExec_t exec = nullptr;
     int32_t info[4] = {0, 0, 0, 0};  // hot slots log2, table factor, best replay us, graph nodes
 };
@@ -42,9 +54,10 @@ struct BatchCfg {
 };
 
 qg_status enqueue(qg_batch *b, const BatchCfg &c) {
-    qg_ctx *ctx = b->own;
     qg_status st = QG_OK;
-    for (const qg_query &q : b->q) {
+    for (size_t i = 0; i < b->q.size(); i++) {
+        const qg_query &q = b->q[i];
+        qg_ctx *ctx = b->own[b->lane[i]];
         const int v = q.variant >= 0 ? q.variant : (q.op == QG_OP_FILTER ? 2 : 0);  // the operators' defaults
         switch (q.op) {
         case QG_OP_FILTER:
@@ -78,20 +91,40 @@ qg_status enqueue(qg_batch *b, const BatchCfg &c) {
     return st;
 }
 
+// Lanes 1.. wait on lane 0 before their queries; lane 0 waits on all of them
+// after.  Inside a capture this makes the fork and join of the graph; in an
+// eager run it orders the lanes the same way.
+cudaError_t fork_lanes(qg_batch *b) {
+    cudaError_t e = cudaEventRecord(b->fork, b->ls[0]);
+    for (int l = 1; l < b->lanes && e == cudaSuccess; l++) e = cudaStreamWaitEvent(b->ls[l], b->fork, 0);
+    return e;
+}
+cudaError_t join_lanes(qg_batch *b) {
+    cudaError_t e = cudaSuccess;
+    for (int l = 1; l < b->lanes && e == cudaSuccess; l++) {
+        e = cudaEventRecord(b->join[l], b->ls[l]);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->ls[0], b->join[l], 0);
+    }
+    return e;
+}
+
 qg_status capture(qg_batch *b, const BatchCfg &c, cudaGraphExec_t *exec, size_t *nodes) {
     cudaGraph_t g = nullptr;
-    QG_TRY_CUDA(b->own, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-    const qg_status st = enqueue(b, c);
+    QG_TRY_CUDA(b->own[0], cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t ef = fork_lanes(b);
+    const qg_status st = ef == cudaSuccess ? enqueue(b, c) : QG_ERR_CUDA;
+    const cudaError_t ej = join_lanes(b);
     const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
-    if (st != QG_OK) {
+    if (st != QG_OK || ef != cudaSuccess || ej != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
-        return st;
+        cudaGetLastError();
+        return st != QG_OK ? st : QG_ERR_CUDA;
     }
-    QG_TRY_CUDA(b->own, e, "end capture");
+    QG_TRY_CUDA(b->own[0], e, "end capture");
     cudaError_t ei = cudaGraphGetNodes(g, nullptr, nodes);
     if (ei == cudaSuccess) ei = cudaGraphInstantiate(exec, g, 0);
     cudaGraphDestroy(g);
-    QG_TRY_CUDA(b->own, ei, "instantiate graph");
+    QG_TRY_CUDA(b->own[0], ei, "instantiate graph");
     return QG_OK;
 }
 
@@ -119,12 +152,37 @@ QG_API qg_status qg_batch_create(const qg_query *queries, int nq, int autotune, 
     *out = nullptr;
     qg_batch *b = new qg_batch();
     b->q.assign(queries, queries + nq);
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        cudaGetLastError();
-        delete b;
-        return QG_ERR_CUDA;
+    b->lanes = std::min(g_batch_lanes, nq);
+    qg_status st = QG_OK;
+    if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) st = QG_ERR_CUDA;
+    for (int l = 0; l < b->lanes && st == QG_OK; l++) {
+        if (cudaStreamCreateWithFlags(&b->ls[l], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->join[l], cudaEventDisableTiming) != cudaSuccess)
+            st = QG_ERR_CUDA;
+        if (st == QG_OK) st = qg_ctx_create(&b->own[l], b->ls[l]);
     }
-    qg_status st = qg_ctx_create(&b->own, b->stream);
+    if (st != QG_OK) {
+        cudaGetLastError();
+        qg_batch_destroy(b);
+        return st;
+    }
+    b->stream = b->ls[0];
+    // Largest queries first, each to the lane with the fewest rows so far.
+    {
+        std::vector<int> order(nq);
+        for (int i = 0; i < nq; i++) order[i] = i;
+        auto rows = [&](int i) { return b->q[i].n + (b->q[i].op == QG_OP_JOIN ? b->q[i].n2 : 0); };
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rows(x) > rows(y); });
+        std::vector<long long> load(b->lanes, 0);
+        b->lane.assign(nq, 0);
+        for (int i : order) {
+            int best = 0;
+            for (int l = 1; l < b->lanes; l++)
+                if (load[l] < load[best]) best = l;
+            b->lane[i] = best;
+            load[best] += rows(i);
+        }
+    }
     std::vector<BatchCfg> cands;
     if (autotune) {
         for (int h : {12, 13})
@@ -134,8 +192,10 @@ QG_API qg_status qg_batch_create(const qg_query *queries, int nq, int autotune, 
     }
     // 1. eager runs of every candidate: the arenas reach their final sizes
     for (size_t i = 0; i < cands.size() && st == QG_OK; i++) {
-        st = enqueue(b, cands[i]);
-        if (st == QG_OK) st = qg_ctx_check(b->own);
+        if (fork_lanes(b) != cudaSuccess) st = QG_ERR_CUDA;
+        if (st == QG_OK) st = enqueue(b, cands[i]);
+        if (st == QG_OK && join_lanes(b) != cudaSuccess) st = QG_ERR_CUDA;
+        for (int l = 0; l < b->lanes && st == QG_OK; l++) st = qg_ctx_check(b->own[l]);
     }
     // 2. capture and time every candidate, keep the fastest
     float best = 0.f;
@@ -145,7 +205,7 @@ QG_API qg_status qg_batch_create(const qg_query *queries, int nq, int autotune, 
         st = capture(b, cands[i], &ex, &nodes);
         if (st != QG_OK) break;
         const float ms = replay_ms(b, ex, 3);
-        st = qg_ctx_check(b->own);
+        for (int l = 0; l < b->lanes && st == QG_OK; l++) st = qg_ctx_check(b->own[l]);
         if (st != QG_OK || ms < 0.f) {
             cudaGraphExecDestroy(ex);
             if (st == QG_OK) st = QG_ERR_CUDA;
@@ -186,7 +246,9 @@ QG_API qg_status qg_batch_check(qg_batch *b, void *stream) {
         cudaGetLastError();
         return QG_ERR_CUDA;
     }
-    return qg_ctx_check(b->own);
+    qg_status st = QG_OK;
+    for (int l = 0; l < b->lanes && st == QG_OK; l++) st = qg_ctx_check(b->own[l]);
+    return st;
 }
 
 QG_API qg_status qg_batch_info(const qg_batch *b, int32_t *out4) {
@@ -198,9 +260,20 @@ QG_API qg_status qg_batch_info(const qg_batch *b, int32_t *out4) {
 QG_API qg_status qg_batch_destroy(qg_batch *b) {
     if (!b) return QG_ERR_INVALID;
     if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->own) qg_ctx_destroy(b->own);
-    if (b->stream) cudaStreamDestroy(b->stream);
+    for (int l = 0; l < QG_BATCH_MAX_LANES; l++) {
+        if (b->own[l]) qg_ctx_destroy(b->own[l]);
+        if (b->ls[l]) cudaStreamDestroy(b->ls[l]);
+        if (b->join[l]) cudaEventDestroy(b->join[l]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     delete b;
+    return QG_OK;
+}
+
+// Lanes of the batches created after this call (1..16; default 8).
+QG_API qg_status qg_batch_set_lanes(int lanes) {
+    if (lanes < 1 || lanes > QG_BATCH_MAX_LANES) return QG_ERR_INVALID;
+    g_batch_lanes = lanes;
     return QG_OK;
 }
 
