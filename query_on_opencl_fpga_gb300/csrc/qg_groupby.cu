@@ -647,6 +647,7 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
     __shared__ uint32_t s_part;
     __shared__ uint32_t s_wc[P2_THREADS / 32];
     __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_m[GB_MAX_C], s_q0[GB_MAX_C], s_q1[GB_MAX_C];  // per source: spill rows, partial range
     __shared__ uint32_t dh[4][256];  // key order requested: digit counts of the emitted keys
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int P = 1 << sp.plog2, S = 1 << sp.slog2;
@@ -698,13 +699,34 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
         const uint32_t *mcnt = sp.mcnt + (size_t)p * GB_MAX_C;
         const uint32_t *po = sp.poff + (size_t)p * GB_MAX_C;
         const uint32_t *po1 = sp.poff + (size_t)(p + 1) * GB_MAX_C;
-        // One warp per source CTA: its spill bucket (4 loads in flight per
-        // lane), then its partials.
+        // Every source's spill count and partial range in one round trip ...
+        for (int cc = tid; cc < C; cc += P2_THREADS) {
+            s_m[cc] = mcnt[cc];
+            s_q0[cc] = po[cc];
+            s_q1[cc] = po1[cc];
+        }
+        __syncthreads();
+        // ... then one warp per source CTA: its first 128 spill rows and its
+        // first 32 partials are loaded together (one round trip per source in
+        // the common case), the rest after.
         for (int cc = warp; cc < C; cc += W) {
-            const uint32_t m = mcnt[cc];
+            const uint32_t m = s_m[cc], q0 = s_q0[cc], q1 = s_q1[cc];
             const uint2 *bk = sp.miss + ((size_t)cc * P + p) * sp.capm;
-            for (uint32_t e0 = 0; e0 < m; e0 += 128) {
-                uint2 r[4];
+            const GPartial *g = sp.part + (size_t)cc * S;
+            uint2 r[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const uint32_t e = u * 32 + lane;
+                r[u] = e < m ? bk[e] : make_uint2(0, 0);
+            }
+            GPartial x;
+            const bool hx = q0 + lane < q1;
+            if (hx) x = g[q0 + lane];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (u * 32 + lane < m) insert(r[u].x, 1u, (long long)(int32_t)r[u].y);
+            if (hx) insert(x.key, x.cnt, x.sum);
+            for (uint32_t e0 = 128; e0 < m; e0 += 128) {
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     const uint32_t e = e0 + u * 32 + lane;
@@ -714,11 +736,9 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
                 for (int u = 0; u < 4; u++)
                     if (e0 + u * 32 + lane < m) insert(r[u].x, 1u, (long long)(int32_t)r[u].y);
             }
-            const uint32_t q0 = po[cc], q1 = po1[cc];
-            const GPartial *g = sp.part + (size_t)cc * S;
-            for (uint32_t e = q0 + lane; e < q1; e += 32) {
-                const GPartial x = g[e];
-                insert(x.key, x.cnt, x.sum);
+            for (uint32_t e = q0 + 32 + lane; e < q1; e += 32) {
+                const GPartial y = g[e];
+                insert(y.key, y.cnt, y.sum);
             }
         }
         __syncthreads();
