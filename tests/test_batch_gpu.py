@@ -74,3 +74,25 @@ def test_batch_join_over_capacity_reports_error(ctx):
     assert e.value.status == 3  # QG_ERR_CAPACITY, seen by the eager run
     # the context of ordinary calls is unaffected
     ctx.check(ctx.lib.qg_ctx_check(ctx.handle), "qg_ctx_check")
+
+
+@pytest.mark.parametrize("lanes", [1, 3, 16])
+def test_batch_lanes_match_plain_calls(ctx, lanes):
+    # The queries spread over `lanes` streams, each with a private context, in
+    # one fork/join graph: the same results whatever the number of lanes.
+    qs = qb.mixed_queries(20, seed=13, lo=4096, hi=1 << 18)
+    plain = qb.run_plain(ctx, qs)
+    lib = ctx.lib
+    assert lib.qg_batch_set_lanes(lanes) == 0
+    try:
+        b = qb.Batch(qs, autotune=False)
+        try:
+            b.run()
+            b.check()
+            for q, got, exp in zip(qs, qb.batch_results(qs), plain):
+                _same(q["op"], got, exp)
+        finally:
+            b.close()
+    finally:
+        lib.qg_batch_set_lanes(8)
+    assert lib.qg_batch_set_lanes(0) != 0 and lib.qg_batch_set_lanes(17) != 0
