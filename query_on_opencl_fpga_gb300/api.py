@@ -191,14 +191,24 @@ class Context:
         return agg[:g]
 
     def groupby_cols(self, key, val, val2=None, lo2: int = INT32_MIN, hi2: int = INT32_MAX,
-                     cap: int = 1 << 20, order: int = QG_ORDER_KEY):
-        """Per-group (key, SUM(val) int64, COUNT int64), optionally only rows with lo2<=val2<=hi2."""
+                     cap: int = 1 << 20, order: int = QG_ORDER_KEY, out=None):
+        """Per-group (key, SUM(val) int64, COUNT int64), optionally only rows with lo2<=val2<=hi2.
+
+        out: optional (key int32, sum int64, count int64) CUDA tensors of at
+        least `cap` elements to write into instead of allocating; the returned
+        tensors are views of them."""
         _check_dev(key, val, val2)
         n = key.numel()
-        dev = key.device
-        gk = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
-        gs = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
-        gc = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+        if out is None:
+            dev = key.device
+            gk = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+            gs = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+            gc = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+        else:
+            gk, gs, gc = out
+            for t, dt in zip(out, (torch.int32, torch.int64, torch.int64)):
+                if t.dtype != dt or not t.is_cuda or not t.is_contiguous() or t.numel() < max(cap, 1):
+                    raise ValueError("out: contiguous CUDA (int32, int64, int64) tensors of at least cap elements")
         g = c_int64()
         st = self.lib.qg_groupby_cols(self.handle, _ptr(key), _ptr(val), _ptr(val2), lo2, hi2, n,
                                       _ptr(gk), _ptr(gs), _ptr(gc), cap, order, byref(g))

@@ -207,3 +207,19 @@ def test_groupby_config1_takes_two_pass_path(ctx):
         st = ctx.groupby_stats()
         assert st["path"] == "two_pass", st
         assert st["fullest_bucket"] <= st["bucket_cap"], st
+
+
+def test_groupby_cols_into_caller_buffers(ctx, orc):
+    # out=: the caller's (key, sum, count) buffers, reused across calls
+    d = datagen.config1_groupby(1 << 18, 1 << 12, seed=21)
+    key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
+    cap = 1 << 13
+    out = (torch.empty(cap, dtype=torch.int32, device="cuda"), torch.empty(cap, dtype=torch.int64, device="cuda"),
+           torch.empty(cap, dtype=torch.int64, device="cuda"))
+    for v2 in (None, val2):
+        got = ctx.groupby_cols(dev(key), dev(val), dev(v2) if v2 is not None else None, d["lo2"], d["hi2"], cap=cap,
+                               out=out)
+        assert got[0].data_ptr() == out[0].data_ptr()
+        check_groups(got, orc.groupby_cols(key, val, v2, d["lo2"], d["hi2"]))
+    with pytest.raises(ValueError):
+        ctx.groupby_cols(dev(key), dev(val), cap=cap, out=(out[0][:10], out[1], out[2]))
