@@ -1033,14 +1033,23 @@ static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_
     // d_flags is the low word of one control counter; the pass-2 work counter
     // is the next counter (both cleared together).
     unsigned int *work = d_flags + 2;
-    QG_TRY_CUDA(ctx, cudaMemsetAsync(d_flags, 0, 16, ctx->stream), "memset flags");
-    QG_TRY_CUDA(ctx, cudaMemsetAsync(d_num, 0, 8, ctx->stream), "memset cursor");
+    qg_control *ctl = ctx->ctl;
+    if ((void *)d_num == (void *)&ctl->counter[1] && (void *)d_flags == (void *)&ctl->counter[2]) {
+        // cursor, flags, work counter and (key order) the digit counts: one
+        // memset from counter[1] on (counters 4 and 5 hold nothing across calls)
+        const size_t from = offsetof(qg_control, counter) + 8;
+        const size_t to = o.rec ? offsetof(qg_control, ghist) + sizeof(ctl->ghist) : from + 24;
+        QG_TRY_CUDA(ctx, cudaMemsetAsync((char *)ctl + from, 0, to - from, ctx->stream), "memset control");
+    } else {
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(d_flags, 0, 16, ctx->stream), "memset flags");
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(d_num, 0, 8, ctx->stream), "memset cursor");
+        if (o.rec) QG_TRY_CUDA(ctx, cudaMemsetAsync(ctl->ghist, 0, sizeof(ctl->ghist), ctx->stream), "memset ghist");
+    }
     qg_pre_launch(ctx);
     part<<<C, P1_THREADS, smem1, ctx->stream>>>(key, val, val2, lo2, hi2, n, sp, d_flags);
     QG_TRY(qg_check_launch(ctx, pred ? "k_gb_part_fused" : "k_gb_part"));
     const int g2 = P < ctx->sm_count * 6 ? P : ctx->sm_count * 6;
     qg_pre_launch(ctx);
-    if (o.rec) QG_TRY_CUDA(ctx, cudaMemsetAsync(ctx->ctl->ghist, 0, sizeof(ctx->ctl->ghist), ctx->stream), "memset ghist");
     if (s64)
         k_gb_merge<true><<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
                                                              (unsigned long long *)d_num, o.rec, d_flags, work,

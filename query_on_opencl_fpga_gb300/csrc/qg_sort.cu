@@ -426,30 +426,33 @@ qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_buf
                               char *work, bool *result_in_b) {
     *result_in_b = false;
     if (n_bound <= 1 || npos <= 0) return QG_OK;
+    if (npos > 4) return QG_ERR_INVALID;  // the work area holds four status regions
     if (n_bound >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
     const long long tiles = (n_bound + RS_TILE - 1) / RS_TILE;
     uint32_t *dbase = (uint32_t *)work;
     uint32_t *trivial = dbase + 4 * QG_RADIX;  // [4], in a 256-byte slot
-    uint32_t *status = trivial + 64;
+    uint32_t *status = trivial + 64;           // [npos][tiles][256]: one region per pass, cleared at once
+    const size_t st_words = (size_t)tiles * QG_RADIX;
     const size_t smem = kv3 ? sizeof(RsSmem<true>) : sizeof(RsSmem<false>);
     if (kv3) QG_TRY((rs_set_attr<true, 0>(ctx)));
     else QG_TRY((rs_set_attr<false, 0>(ctx)));
     qg_pre_launch(ctx);
     k_radix_bases<<<1, QG_RADIX, 0, ctx->stream>>>(d_hist, npos, dbase, trivial);
     QG_TRY(qg_check_launch(ctx, "k_radix_bases"));
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(status, 0, (size_t)npos * st_words * 4, ctx->stream), "memset status");
     bool in_a = true;
     for (int p = 0; p < npos; p++) {
-        QG_TRY_CUDA(ctx, cudaMemsetAsync(status, 0, (size_t)tiles * QG_RADIX * 4, ctx->stream), "memset status");
         const qg_sort_bufs &s = in_a ? a : b;
         const qg_sort_bufs &d = in_a ? b : a;
+        uint32_t *stp = status + (size_t)p * st_words;
         qg_pre_launch(ctx);
         if (kv3)
             k_radix_pass<true, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n,
+                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, stp, ctx->ctl, ctx->spin_limit, d_n,
                 trivial + p);
         else
             k_radix_pass<false, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, d_n,
+                s, d, n_bound, 8 * p, key_off, nullptr, dbase + p * QG_RADIX, stp, ctx->ctl, ctx->spin_limit, d_n,
                 trivial + p);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
         in_a = !in_a;
@@ -459,7 +462,7 @@ qg_status qg_radix_passes_dev(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_buf
 }
 
 size_t qg_radix_dev_work_bytes(long long n_bound) {
-    return 4 * QG_RADIX * 4 + 256 + (size_t)((n_bound + RS_TILE - 1) / RS_TILE) * QG_RADIX * 4;
+    return 4 * QG_RADIX * 4 + 256 + 4 * (size_t)((n_bound + RS_TILE - 1) / RS_TILE) * QG_RADIX * 4;
 }
 
 qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
