@@ -637,7 +637,7 @@ __global__ void __launch_bounds__(P2_THREADS)
 k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict__ gsum,
            long long *__restrict__ gcnt, long long cap, unsigned long long *__restrict__ cursor,
            unsigned long long *__restrict__ rec, unsigned int *__restrict__ flags,
-           unsigned int *__restrict__ work, uint32_t *__restrict__ ghist) {
+           unsigned int *__restrict__ work, uint32_t *__restrict__ ghist, uint32_t *__restrict__ mm) {
     constexpr int T = 1 << P2_TLOG2;
     constexpr int NB = T / 4;
     constexpr int W = P2_THREADS / 32;
@@ -648,7 +648,8 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
     __shared__ uint32_t s_wc[P2_THREADS / 32];
     __shared__ unsigned long long s_base;
     __shared__ uint32_t s_m[GB_MAX_C], s_q0[GB_MAX_C], s_q1[GB_MAX_C];  // per source: spill rows, partial range
-    __shared__ uint32_t dh[4][256];  // key order requested: digit counts of the emitted keys
+    __shared__ uint32_t dh[4][256];  // ghist set: digit counts of the emitted keys
+    __shared__ uint32_t s_mn, s_mx;   // mm set: smallest and largest emitted key
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int P = 1 << sp.plog2, S = 1 << sp.slog2;
     const uint32_t lt = qg_lanemask_lt();
@@ -682,8 +683,13 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
         gb_acc<SUM64>(&tc[s], &tsum[gb_lo<SUM64>(s)], &tsum[gb_hi<SUM64>(s, T + 1)], cnt, sum);
     };
 
-    if (rec)
+    if (ghist)
         for (int i = tid; i < 4 * 256; i += P2_THREADS) (&dh[0][0])[i] = 0;
+    if (tid == 0) {
+        s_mn = 0xffffffffu;
+        s_mx = 0;
+    }
+    uint32_t kmn = 0xffffffffu, kmx = 0;
     while (true) {
         __syncthreads();
         if (tid == 0) s_part = atomicAdd(work, 1u);
@@ -777,17 +783,172 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
                     if (rec) {
                         const uint32_t k = tk[s];
                         rec[pos] = ((unsigned long long)k << 32) | (unsigned long long)pos;
+                        if (ghist) {
 #pragma unroll
-                        for (int d = 0; d < 4; d++) atomicAdd(&dh[d][(k >> (8 * d)) & 255u], 1u);
+                            for (int d = 0; d < 4; d++) atomicAdd(&dh[d][(k >> (8 * d)) & 255u], 1u);
+                        }
+                        kmn = min(kmn, k);
+                        kmx = max(kmx, k);
                     }
                 }
             }
         }
     }
-    if (rec) {  // the loop ends for every thread at once (s_part is shared)
+    // the loop ends for every thread at once (s_part is shared)
+    if (ghist) {
         __syncthreads();
         for (int i = tid; i < 4 * 256; i += P2_THREADS)
             if ((&dh[0][0])[i]) atomicAdd(&ghist[i], (&dh[0][0])[i]);
+    }
+    if (mm) {
+        kmn = __reduce_min_sync(QG_FULL_MASK, kmn);
+        kmx = __reduce_max_sync(QG_FULL_MASK, kmx);
+        if (lane == 0) {
+            atomicMin(&s_mn, kmn);
+            atomicMax(&s_mx, kmx);
+        }
+        __syncthreads();
+        // mm[0] keeps the largest complement (both words start at zero)
+        if (tid == 0 && s_mn <= s_mx) {
+            atomicMax(&mm[0], ~s_mn);
+            atomicMax(&mm[1], s_mx);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 2''. key order over a dense key range
+//
+// When the emitted keys span at most GB_DENSE_RANGE values, a group's place
+// in unsigned key order is the number of present keys below it.  The merge
+// records the smallest and largest key it wrote (mm); k_gb_dense_bits sets
+// one bit per group in a bitmap over [kmin, kmax]; k_gb_dense_scan turns the
+// bitmap into (bits below this word, word) pairs and clears it, so the
+// bitmap arena is all-zero again; k_gb_dense_place writes each group at its
+// word's prefix plus the popcount of the lower bits of its word.  A wider
+// range leaves all three kernels idle and the host sorts instead.
+// ---------------------------------------------------------------------------
+constexpr long long GB_DENSE_RANGE = 1LL << 27;        // bitmap 16 MB
+constexpr size_t GB_DENSE_WORDS = GB_DENSE_RANGE / 32;  // 2^22 words
+constexpr int DN_THREADS = 256;
+constexpr int DN_WPT = 8;  // bitmap words per thread and round (two 16-byte loads)
+
+__device__ __forceinline__ bool gb_dense_range(const uint32_t *mm, uint32_t *kmin, uint32_t *words) {
+    const uint32_t lo = ~mm[0], hi = mm[1];
+    if (hi < lo) return false;  // no group
+    const unsigned long long range = (unsigned long long)(hi - lo) + 1ull;
+    if (range > (unsigned long long)GB_DENSE_RANGE) return false;
+    *kmin = lo;
+    *words = (uint32_t)((range + 31) >> 5);
+    return true;
+}
+
+__global__ void __launch_bounds__(256)
+k_gb_dense_bits(const int32_t *__restrict__ gkey, long long cap, const long long *__restrict__ d_n,
+                const uint32_t *__restrict__ mm, uint32_t *__restrict__ bits) {
+    uint32_t kmin, words;
+    if (!gb_dense_range(mm, &kmin, &words)) return;
+    const long long g = *d_n < cap ? *d_n : cap;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g; i += stride) {
+        const uint32_t u = (uint32_t)__ldg(gkey + i) - kmin;
+        atomicOr(&bits[u >> 5], 1u << (u & 31));
+    }
+}
+
+// One CTA per chunk of whole 8-word groups; chunk c's prefix comes from a
+// look-back over chunks 0..c-1 (CTA index = chunk index).
+__global__ void __launch_bounds__(DN_THREADS)
+k_gb_dense_scan(uint32_t *__restrict__ bits, uint2 *__restrict__ pre, const uint32_t *__restrict__ mm,
+                qg_lookback lb) {
+    constexpr int NW = DN_THREADS / 32;
+    constexpr uint32_t ROUND = DN_THREADS * DN_WPT;
+    __shared__ uint32_t s_tile, s_epoch, s_excl;
+    __shared__ uint32_t s_woff[NW], s_tmp[2 * NW + 1];
+    uint32_t kmin, words;
+    if (!gb_dense_range(mm, &kmin, &words)) return;
+    const uint32_t w8 = (words + 7) / 8;                      // 8-word groups in the range
+    const uint32_t per = (w8 + gridDim.x - 1) / gridDim.x;   // groups per chunk
+    qg_lb_begin(lb, &s_tile, &s_epoch);
+    const uint32_t tile = s_tile;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t lo = min(w8, tile * per) * 8, hi = min(w8, (tile + 1) * per) * 8;
+    auto load8 = [&](uint32_t w, uint32_t *x) {
+        const uint4 a = reinterpret_cast<const uint4 *>(bits + w)[0];
+        const uint4 b = reinterpret_cast<const uint4 *>(bits + w)[1];
+        x[0] = a.x; x[1] = a.y; x[2] = a.z; x[3] = a.w;
+        x[4] = b.x; x[5] = b.y; x[6] = b.z; x[7] = b.w;
+    };
+    uint32_t c = 0;
+    for (uint32_t w = lo + tid * DN_WPT; w < hi; w += ROUND) {
+        uint32_t x[DN_WPT];
+        load8(w, x);
+#pragma unroll
+        for (int k = 0; k < DN_WPT; k++) c += __popc(x[k]);
+    }
+    c = __reduce_add_sync(QG_FULL_MASK, c);
+    if (lane == 0) s_woff[warp] = c;
+    qg_tile_offsets_wide<NW, NW>(s_woff, lb, tile, s_epoch, &s_excl, s_tmp, nullptr, gridDim.x - 1);
+    uint32_t run = s_excl;
+    for (uint32_t r0 = lo; r0 < hi; r0 += ROUND) {
+        const uint32_t w = r0 + tid * DN_WPT;
+        uint32_t x[DN_WPT];
+        uint32_t t = 0;
+        if (w < hi) {
+            load8(w, x);
+#pragma unroll
+            for (int k = 0; k < DN_WPT; k++) t += __popc(x[k]);
+        }
+        uint32_t incl = t;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(QG_FULL_MASK, incl, d);
+            if (lane >= d) incl += v;
+        }
+        __syncthreads();  // s_woff of the previous round is read
+        if (lane == 31) s_woff[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int k = 0; k < NW; k++) {
+            const uint32_t v = s_woff[k];
+            before += (k < warp) ? v : 0u;
+            total += v;
+        }
+        if (w < hi) {
+            uint32_t q = run + before + incl - t;
+            uint4 *dst = reinterpret_cast<uint4 *>(pre + w);
+#pragma unroll
+            for (int k = 0; k < DN_WPT; k += 2) {
+                const uint32_t q1 = q + __popc(x[k]);
+                dst[k / 2] = make_uint4(q, x[k], q1, x[k + 1]);
+                q = q1 + __popc(x[k + 1]);
+            }
+            reinterpret_cast<uint4 *>(bits + w)[0] = make_uint4(0, 0, 0, 0);
+            reinterpret_cast<uint4 *>(bits + w)[1] = make_uint4(0, 0, 0, 0);
+        }
+        run += total;
+    }
+    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
+}
+
+__global__ void __launch_bounds__(256)
+k_gb_dense_place(const unsigned long long *__restrict__ rec, long long cap, const long long *__restrict__ d_n,
+                 const uint32_t *__restrict__ mm, const uint2 *__restrict__ pre,
+                 const long long *__restrict__ tsum, const long long *__restrict__ tcnt,
+                 int32_t *__restrict__ gkey, long long *__restrict__ gsum, long long *__restrict__ gcnt) {
+    uint32_t kmin, words;
+    if (!gb_dense_range(mm, &kmin, &words)) return;
+    const long long g = *d_n < cap ? *d_n : cap;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g; i += stride) {
+        const uint32_t k = (uint32_t)(__ldg(rec + i) >> 32);
+        const uint32_t u = k - kmin;
+        const uint2 p = __ldg(pre + (u >> 5));
+        const uint32_t pos = p.x + __popc(p.y & ((1u << (u & 31)) - 1u));
+        gkey[pos] = (int32_t)k;
+        gsum[pos] = __ldg(tsum + i);
+        gcnt[pos] = __ldg(tcnt + i);
     }
 }
 
@@ -982,10 +1143,12 @@ static qg_status gb_launch_global(qg_ctx *ctx, const int32_t *key, const int32_t
 
 // Two-pass path.  *d_flags != 0 afterwards means a spill bucket or a pass-2
 // table overflowed and the call must be redone with gb_launch_global.
+// Key order: ghist receives the digit counts of the emitted keys (the
+// device-planned sort), mm their smallest and largest key (the dense order).
 static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_t *val,
                                    const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
                                    const GbOut &o, int64_t cap, long long *d_num,
-                                   unsigned int *d_flags) {
+                                   unsigned int *d_flags, uint32_t *ghist, uint32_t *mm) {
     int C = ctx->sm_count;
     if (C > GB_MAX_C) C = GB_MAX_C;
     const int slog2 = g_gb_hot_slog2;
@@ -1034,16 +1197,21 @@ static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_
     // is the next counter (both cleared together).
     unsigned int *work = d_flags + 2;
     qg_control *ctl = ctx->ctl;
-    if ((void *)d_num == (void *)&ctl->counter[1] && (void *)d_flags == (void *)&ctl->counter[2]) {
-        // cursor, flags, work counter and (key order) the digit counts: one
-        // memset from counter[1] on (counters 4 and 5 hold nothing across calls)
+    if ((void *)d_num == (void *)&ctl->counter[1] && (void *)d_flags == (void *)&ctl->counter[2] &&
+        (!ghist || ghist == ctl->ghist) && (!mm || mm == (uint32_t *)&ctl->counter[4])) {
+        // cursor, flags, work counter and (key order) the key range or the
+        // digit counts: one memset from counter[1] on (counters 4 and 5 hold
+        // nothing across calls)
         const size_t from = offsetof(qg_control, counter) + 8;
-        const size_t to = o.rec ? offsetof(qg_control, ghist) + sizeof(ctl->ghist) : from + 24;
+        const size_t to = ghist == ctl->ghist ? offsetof(qg_control, ghist) + sizeof(ctl->ghist)
+                          : mm == (uint32_t *)&ctl->counter[4] ? from + 32
+                                                                : from + 24;
         QG_TRY_CUDA(ctx, cudaMemsetAsync((char *)ctl + from, 0, to - from, ctx->stream), "memset control");
     } else {
         QG_TRY_CUDA(ctx, cudaMemsetAsync(d_flags, 0, 16, ctx->stream), "memset flags");
         QG_TRY_CUDA(ctx, cudaMemsetAsync(d_num, 0, 8, ctx->stream), "memset cursor");
-        if (o.rec) QG_TRY_CUDA(ctx, cudaMemsetAsync(ctl->ghist, 0, sizeof(ctl->ghist), ctx->stream), "memset ghist");
+        if (ghist) QG_TRY_CUDA(ctx, cudaMemsetAsync(ghist, 0, 4 * 256 * 4, ctx->stream), "memset ghist");
+        if (mm) QG_TRY_CUDA(ctx, cudaMemsetAsync(mm, 0, 8, ctx->stream), "memset key range");
     }
     qg_pre_launch(ctx);
     part<<<C, P1_THREADS, smem1, ctx->stream>>>(key, val, val2, lo2, hi2, n, sp, d_flags);
@@ -1053,11 +1221,11 @@ static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_
     if (s64)
         k_gb_merge<true><<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
                                                              (unsigned long long *)d_num, o.rec, d_flags, work,
-                                                             ctx->ctl->ghist);
+                                                             ghist, mm);
     else
         k_gb_merge<false><<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
                                                               (unsigned long long *)d_num, o.rec, d_flags, work,
-                                                              ctx->ctl->ghist);
+                                                              ghist, mm);
     return qg_check_launch(ctx, "k_gb_merge");
 }
 
@@ -1088,6 +1256,43 @@ static qg_status gb_key_order_dev(qg_ctx *ctx, const GbOut &o, int64_t cap, long
     return qg_check_launch(ctx, "k_groupby_gather");
 }
 
+// Dense key order (see k_gb_dense_bits): three launches, all idle when the
+// emitted keys span more than GB_DENSE_RANGE values.
+static qg_status gb_key_order_dense(qg_ctx *ctx, const GbOut &o, int64_t cap, const long long *d_num,
+                                    const uint32_t *mm, int32_t *gkey, int64_t *gsum, int64_t *gcnt) {
+    if (cap <= 0) return QG_OK;
+    char *bitp, *prep;
+    QG_TRY(qg_table(ctx, GB_DENSE_WORDS * 4, &bitp));
+    QG_TRY(qg_scratch(ctx, GB_DENSE_WORDS * 8, &prep));
+    qg_lookback lb;
+    QG_TRY(qg_lb_make(ctx, ctx->sm_count, QG_SITE_GROUPBY, &lb));
+    uint32_t *bits = (uint32_t *)bitp;
+    const int gb = grid_for(ctx, cap, 256, 8);
+    qg_pre_launch(ctx);
+    k_gb_dense_bits<<<gb, 256, 0, ctx->stream>>>(o.k, cap, d_num, mm, bits);
+    qg_status st = qg_check_launch(ctx, "k_gb_dense_bits");
+    if (st == QG_OK) {
+        qg_pre_launch(ctx);
+        k_gb_dense_scan<<<ctx->sm_count, DN_THREADS, 0, ctx->stream>>>(bits, (uint2 *)prep, mm, lb);
+        st = qg_check_launch(ctx, "k_gb_dense_scan");
+    }
+    if (st != QG_OK) {
+        ctx->table_dirty = true;  // bits may be left set
+        return st;
+    }
+    qg_pre_launch(ctx);
+    k_gb_dense_place<<<gb, 256, 0, ctx->stream>>>(o.rec, cap, d_num, mm, (const uint2 *)prep, o.s, o.c,
+                                                  gkey, (long long *)gsum, (long long *)gcnt);
+    return qg_check_launch(ctx, "k_gb_dense_place");
+}
+
+// Host side of gb_dense_range: did the dense order place the groups?
+static bool gb_dense_applied(const qg_control *pin) {
+    const uint32_t *mm = (const uint32_t *)&pin->counter[4];
+    const uint32_t lo = ~mm[0], hi = mm[1];
+    return hi >= lo && (unsigned long long)(hi - lo) + 1ull <= (unsigned long long)GB_DENSE_RANGE;
+}
+
 extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key,
                                                   const int32_t *val, const int32_t *val2,
                                                   int32_t lo2, int32_t hi2, int64_t n,
@@ -1104,7 +1309,8 @@ extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *ke
     if (g_gb_mode == 1)
         return gb_launch_global(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num);
     unsigned int *flags = (unsigned int *)&ctx->ctl->counter[2];
-    QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num, flags));
+    QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num, flags,
+                             o.rec ? ctx->ctl->ghist : nullptr, nullptr));
     if (o.rec) QG_TRY(gb_key_order_dev(ctx, o, cap, (long long *)d_num, gkey, gsum, gcnt));
     // An overflow cannot be redone without a host round trip here: report it
     // through the error word (qg_ctx_check returns QG_ERR_TABLE_FULL).
@@ -1129,11 +1335,17 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     long long g = 0;
     bool global = g_gb_mode == 1;
     bool done = false;  // the two-pass path wrote the final output (any order)
-    // The device-planned sort takes up to 2^30 records; beyond that the key
-    // order is sorted after the host has read the count.
-    const bool dev_order = o.rec && cap < (1LL << 30);
+    // Key order: the dense order unless the context's last key-ordered call
+    // found its keys too widely spread, then the device-planned sort (up to
+    // 2^30 records).  Whatever neither placed is sorted after the host has
+    // read the count.
+    const bool dense = o.rec && !ctx->gb_wide_keys;
+    const bool dev_order = o.rec && !dense && cap < (1LL << 30);
+    uint32_t *mm = (uint32_t *)&ctx->ctl->counter[4];
     if (!global) {
-        QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num, flags));
+        QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num, flags,
+                                 dev_order ? ctx->ctl->ghist : nullptr, o.rec ? mm : nullptr));
+        if (dense) QG_TRY(gb_key_order_dense(ctx, o, cap, d_num, mm, gkey, gsum, gcnt));
         if (dev_order) QG_TRY(gb_key_order_dev(ctx, o, cap, d_num, gkey, gsum, gcnt));
         // One read of the control block, at the end, brings the error word,
         // the group count (counter[1]) and the overflow flags (counter[2]).
@@ -1145,7 +1357,13 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
         g = (long long)ctx->pin_ctl->counter[1];
         const unsigned long long fl = ctx->pin_ctl->counter[2];
         global = (fl & 0xffffffffull) != 0;
-        done = !global && (!o.rec || dev_order);
+        bool placed = dev_order;
+        if (o.rec && g > 0) {  // the merge recorded the key range either way
+            const bool fits = gb_dense_applied(ctx->pin_ctl);
+            if (dense) placed = fits;
+            ctx->gb_wide_keys = !fits;
+        }
+        done = !global && (!o.rec || placed || g == 0);
         ctx->gb_stats[0] = global ? 1u : 0u;
         ctx->gb_stats[1] = (uint32_t)fl;
         ctx->gb_stats[2] = (uint32_t)(fl >> 32);

@@ -223,3 +223,30 @@ def test_groupby_cols_into_caller_buffers(ctx, orc):
         check_groups(got, orc.groupby_cols(key, val, v2, d["lo2"], d["hi2"]))
     with pytest.raises(ValueError):
         ctx.groupby_cols(dev(key), dev(val), cap=cap, out=(out[0][:10], out[1], out[2]))
+
+
+def test_groupby_key_order_dense_and_wide_ranges(ctx, orc):
+    # Key order places the groups by rank in a bitmap when their keys span at
+    # most 2^27 values, and sorts them otherwise; the context remembers the
+    # last call's spread.  The sequence takes every transition: dense, wide
+    # (placed after the count), wide (sorted on the device), dense (sorted,
+    # then back to the bitmap), and both sides of the 2^27 limit.
+    rng = np.random.default_rng(9)
+    n = 1 << 17
+
+    def keys(kind):
+        if kind == "dense":  # unsigned-contiguous across the signed boundary
+            return rng.integers(2 ** 31 - 3000, 2 ** 31 + 3000, n).astype(np.uint32).view(np.int32)
+        if kind == "wide":  # -5..5: the unsigned range is nearly 2^32
+            return rng.integers(-5, 6, n).astype(np.int32)
+        k = rng.integers(7, 7 + (1 << 27) - 1, n)
+        k[0], k[1] = 7, 7 + (1 << 27) - 1 + (kind == "over")  # 2^27 values, or one more
+        return k.astype(np.int32)
+
+    for kind in ["dense", "wide", "wide", "dense", "dense", "edge", "over", "over", "edge", "dense"]:
+        key = keys(kind)
+        val = rng.integers(-1000, 1000, n).astype(np.int32)
+        got = ctx.groupby_cols(dev(key), dev(val), cap=n)
+        check_groups(got, orc.groupby_cols(key, val))
+        fused = ctx.groupby_cols(dev(key), dev(val), dev(val), -10, 500, cap=n)
+        check_groups(fused, orc.groupby_cols(key, val, val, -10, 500))
