@@ -185,13 +185,17 @@ def run_reference(args, rank, world):
 # our arm
 # ---------------------------------------------------------------------------
 def timed(ctx, fn, steps, warmup, world, stream):
+    """(ms per step, {kernel: (launches, total ms)}, launches per run of `steps`).
+
+    The timed region runs the steps alone.  The per-kernel durations come from
+    the same number of steps right after it, with a CUDA event pair on the
+    context's stream around every launch: those events cost about 40 us per
+    headline step, so they stay out of the step time."""
     import torch
 
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
-    ctx.timing_report()  # drop warm-up launches
-    ctx.enable_timing(True)
     launches0 = ctx.launches
     barrier(world)
     torch.cuda.synchronize()
@@ -204,9 +208,15 @@ def timed(ctx, fn, steps, warmup, world, stream):
     torch.cuda.synchronize()
     barrier(world)
     ms = start.elapsed_time(end) / steps
+    launches = ctx.launches - launches0
+    ctx.timing_report()  # drop anything logged before
+    ctx.enable_timing(True)
+    for _ in range(steps):
+        fn()
+    torch.cuda.synchronize()
     kern = ctx.timing_report()
     ctx.enable_timing(False)
-    return ms, kern, ctx.launches - launches0
+    return ms, kern, launches
 
 
 def roofline(kern, name, bytes_per_launch, peak_gbs, traffic=None):
