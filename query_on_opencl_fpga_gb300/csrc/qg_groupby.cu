@@ -633,7 +633,7 @@ k_gb_part(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
 // Table = 2048 slots in 512 buckets of 4 ways (+1 slot for key 0xffffffff);
 // a full bucket continues in the next one.
 template <bool SUM64>
-__global__ void __launch_bounds__(P2_THREADS)
+__global__ void __launch_bounds__(P2_THREADS, 5)
 k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict__ gsum,
            long long *__restrict__ gcnt, long long cap, unsigned long long *__restrict__ cursor,
            unsigned long long *__restrict__ rec, unsigned int *__restrict__ flags,
@@ -647,7 +647,10 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
     __shared__ uint32_t s_part;
     __shared__ uint32_t s_wc[P2_THREADS / 32];
     __shared__ unsigned long long s_base;
-    __shared__ uint32_t s_m[GB_MAX_C], s_q0[GB_MAX_C], s_q1[GB_MAX_C];  // per source: spill rows, partial range
+    // per source: spill rows, first partial, exclusive prefix of the partial counts
+    __shared__ uint32_t s_m[GB_MAX_C], s_q0[GB_MAX_C], s_pp[GB_MAX_C];
+    __shared__ uint32_t s_ptot;
+    static_assert(GB_MAX_C <= P2_THREADS, "one source per thread");
     __shared__ uint32_t dh[4][256];  // ghist set: digit counts of the emitted keys
     __shared__ uint32_t s_mn, s_mx;   // mm set: smallest and largest emitted key
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -705,33 +708,84 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
         const uint32_t *mcnt = sp.mcnt + (size_t)p * GB_MAX_C;
         const uint32_t *po = sp.poff + (size_t)p * GB_MAX_C;
         const uint32_t *po1 = sp.poff + (size_t)(p + 1) * GB_MAX_C;
-        // Every source's spill count and partial range in one round trip ...
-        for (int cc = tid; cc < C; cc += P2_THREADS) {
-            s_m[cc] = mcnt[cc];
-            s_q0[cc] = po[cc];
-            s_q1[cc] = po1[cc];
+        // Every source's spill count and partial range in one round trip (one
+        // source per thread), with the exclusive prefix of the partial counts.
+        uint32_t pc = 0;
+        if (tid < C) {
+            s_m[tid] = mcnt[tid];
+            const uint32_t q0 = po[tid];
+            s_q0[tid] = q0;
+            pc = po1[tid] - q0;
         }
+        uint32_t pin = pc;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t v = __shfl_up_sync(QG_FULL_MASK, pin, d);
+            if (lane >= d) pin += v;
+        }
+        if (lane == 31) s_wc[warp] = pin;
         __syncthreads();
-        // ... then one warp per source CTA: its first 128 spill rows and its
-        // first 32 partials are loaded together (one round trip per source in
-        // the common case), the rest after.
-        for (int cc = warp; cc < C; cc += W) {
-            const uint32_t m = s_m[cc], q0 = s_q0[cc], q1 = s_q1[cc];
+        {
+            uint32_t woff = 0, tot = 0;
+#pragma unroll
+            for (int w = 0; w < W; w++) {
+                const uint32_t v = s_wc[w];
+                woff += (w < warp) ? v : 0u;
+                tot += v;
+            }
+            if (tid < C) s_pp[tid] = woff + pin - pc;
+            if (tid == 0) s_ptot = tot;
+        }
+        // The first source's spill loads are issued before the partials.
+        uint2 rn[4];
+        auto first_loads = [&](int cc) {
+            if (cc >= C) return;
+            const uint32_t m = s_m[cc];
             const uint2 *bk = sp.miss + ((size_t)cc * P + p) * sp.capm;
-            const GPartial *g = sp.part + (size_t)cc * S;
-            uint2 r[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
                 const uint32_t e = u * 32 + lane;
-                r[u] = e < m ? bk[e] : make_uint2(0, 0);
+                rn[u] = e < m ? bk[e] : make_uint2(0, 0);
             }
-            GPartial x;
-            const bool hx = q0 + lane < q1;
-            if (hx) x = g[q0 + lane];
+        };
+        first_loads(warp);
+        __syncthreads();
+        // Partials: a few per source, so they are taken as one flat list over
+        // all sources (a source found by binary search over the prefix), with
+        // every lane busy.
+        const uint32_t ptot = s_ptot;
+        for (uint32_t t0 = 0; t0 < ptot; t0 += 2 * P2_THREADS) {
+            GPartial y[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const uint32_t t = t0 + u * P2_THREADS + tid;
+                if (t < ptot) {
+                    int lo = 0, hi = C;
+                    while (hi - lo > 1) {
+                        const int mid = (lo + hi) >> 1;
+                        if (s_pp[mid] <= t) lo = mid;
+                        else hi = mid;
+                    }
+                    y[u] = sp.part[(size_t)lo * S + s_q0[lo] + (t - s_pp[lo])];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++)
+                if (t0 + u * P2_THREADS + tid < ptot) insert(y[u].key, y[u].cnt, y[u].sum);
+        }
+        // Spill rows: one warp per source CTA, its first 128 rows in one round
+        // trip, the rest after.  The warp's next source is loaded before this
+        // one is inserted, so that its round trip overlaps.
+        for (int cc = warp; cc < C; cc += W) {
+            const uint32_t m = s_m[cc];
+            const uint2 *bk = sp.miss + ((size_t)cc * P + p) * sp.capm;
+            uint2 r[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) r[u] = rn[u];
+            first_loads(cc + W);
 #pragma unroll
             for (int u = 0; u < 4; u++)
                 if (u * 32 + lane < m) insert(r[u].x, 1u, (long long)(int32_t)r[u].y);
-            if (hx) insert(x.key, x.cnt, x.sum);
             for (uint32_t e0 = 128; e0 < m; e0 += 128) {
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
@@ -741,10 +795,6 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
 #pragma unroll
                 for (int u = 0; u < 4; u++)
                     if (e0 + u * 32 + lane < m) insert(r[u].x, 1u, (long long)(int32_t)r[u].y);
-            }
-            for (uint32_t e = q0 + 32 + lane; e < q1; e += 32) {
-                const GPartial y = g[e];
-                insert(y.key, y.cnt, y.sum);
             }
         }
         __syncthreads();
