@@ -266,7 +266,9 @@ def run_ours(args, rank, world, local):
 
     d = datagen.config1_groupby(N_ROWS, GROUPS, seed=rank, device="cuda")
     key, val, val2, lo2, hi2 = d["key"], d["val"], d["val2"], d["lo2"], d["hi2"]
-    cap = GROUPS * 2
+    # output capacity: the key domain (Zipf ranks over GROUPS keys), which is
+    # also what sizes the group-by's spill partitions (~1024 groups each)
+    cap = GROUPS
 
     # one set of output columns per operator, reused by every step (as a caller
     # that owns its result buffers would; no allocation inside the step)
@@ -412,7 +414,7 @@ def operator_lines(ctx, args, peak, stream):
     d = datagen.config1_groupby(N_ROWS, GROUPS, seed=0, device="cuda")
 
     def gstep():
-        ctx.groupby_cols(d["key"], d["val"], None, d["lo2"], d["hi2"], cap=GROUPS * 2, order=QG_ORDER_NONE)
+        ctx.groupby_cols(d["key"], d["val"], None, d["lo2"], d["hi2"], cap=GROUPS, order=QG_ORDER_NONE)
 
     ms, kern, _ = timed(ctx, gstep, steps, 3, 1, stream)
     out["groupby_config1_unordered"] = {"rows_per_s": N_ROWS / (ms * 1e-3), "ms_per_op": ms,
@@ -421,7 +423,7 @@ def operator_lines(ctx, args, peak, stream):
                                         "roofline": roofline(kern, "k_gb_part", N_ROWS * 8, peak)}
 
     def fgstep():
-        ctx.groupby_cols(d["key"], d["val"], d["val2"], d["lo2"], d["hi2"], cap=GROUPS * 2, order=QG_ORDER_NONE)
+        ctx.groupby_cols(d["key"], d["val"], d["val2"], d["lo2"], d["hi2"], cap=GROUPS, order=QG_ORDER_NONE)
 
     ms, kern, _ = timed(ctx, fgstep, steps, 3, 1, stream)
     out["filter_groupby_config1_unordered"] = {
@@ -545,7 +547,7 @@ def run_only(args):
         n = rows or N_ROWS
         d = datagen.config1_groupby(n, GROUPS, seed=0, device="cuda")
         v2 = d["val2"] if args.only == "fused" else None
-        fn = lambda: ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=GROUPS * 2,  # noqa: E731
+        fn = lambda: ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=GROUPS,  # noqa: E731
                                       order=QG_ORDER_NONE)
     elif args.only == "filter":
         n = rows or (1 << 24)

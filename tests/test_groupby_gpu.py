@@ -199,13 +199,16 @@ def test_groupby_knob_sweep(ctx, orc, knobs, hot, parts, mode):
     check_groups(got, orc.groupby_cols(key, val, val2, d["lo2"], d["hi2"]))
 
 
-def test_groupby_config1_takes_two_pass_path(ctx):
-    # The full config-1 input must be handled by the two-pass path (no fallback).
+@pytest.mark.parametrize("cap", [1 << 20, 1 << 21])
+def test_groupby_config1_takes_two_pass_path(ctx, cap):
+    # The full config-1 input must be handled by the two-pass path (no
+    # fallback) with the output capacity the bench passes (the key domain,
+    # 1024 spill partitions) and with twice that (2048 partitions).
     d = datagen.config1_groupby(1 << 26, 1 << 20, seed=0, device="cuda")
     for v2 in (None, d["val2"]):
-        ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=1 << 21, order=QG_ORDER_NONE)
+        ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=cap, order=QG_ORDER_NONE)
         st = ctx.groupby_stats()
-        assert st["path"] == "two_pass", st
+        assert st["path"] == "two_pass" and st["flags"] == 0, st
         assert st["fullest_bucket"] <= st["bucket_cap"], st
 
 
