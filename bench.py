@@ -340,7 +340,10 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
         return nb // k
 
-    e2e_steps = max(3, min(args.steps, 10))
+    # Enough steps that the pipeline's fill and drain (one input copy before
+    # the first step, the last step's compute and read-back after the last
+    # copy, about 5 ms together) weigh little against the steady state.
+    e2e_steps = max(3, min(args.steps, 40))
     e2e_run(2)
     torch.cuda.synchronize()
     barrier(world)

@@ -389,6 +389,9 @@ constexpr int P1_THREADS = 1024;
 constexpr int P2_THREADS = 256;
 constexpr int P2_TLOG2 = 11;  // pass-2 table slots (2048) + 1 for key 0xffffffff
 constexpr int GB_SKETCH_WORDS = 8192;  // 16K 16-bit admission counters (32 KB)
+// Key-order bitmap window (the dense order, section 2''): 2^27 keys, 16 MB.
+constexpr long long GB_DENSE_RANGE = 1LL << 27;
+constexpr size_t GB_DENSE_WORDS = GB_DENSE_RANGE / 32;
 
 // In-place exclusive scan of a[0..L) in shared memory by the whole CTA;
 // returns the total.  `wsum` holds one word per warp.
@@ -637,7 +640,8 @@ __global__ void __launch_bounds__(P2_THREADS, 5)
 k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict__ gsum,
            long long *__restrict__ gcnt, long long cap, unsigned long long *__restrict__ cursor,
            unsigned long long *__restrict__ rec, unsigned int *__restrict__ flags,
-           unsigned int *__restrict__ work, uint32_t *__restrict__ ghist, uint32_t *__restrict__ mm) {
+           unsigned int *__restrict__ work, uint32_t *__restrict__ ghist, uint32_t *__restrict__ mm,
+           uint32_t *__restrict__ bits, uint32_t kbase) {
     constexpr int T = 1 << P2_TLOG2;
     constexpr int NB = T / 4;
     constexpr int W = P2_THREADS / 32;
@@ -839,6 +843,10 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
                         }
                         kmn = min(kmn, k);
                         kmx = max(kmx, k);
+                        if (bits) {  // the key's bit in the dense-order window
+                            const uint32_t u = k - kbase;
+                            if (u < (uint32_t)GB_DENSE_RANGE) atomicOr(&bits[u >> 5], 1u << (u & 31));
+                        }
                     }
                 }
             }
@@ -869,60 +877,59 @@ k_gb_merge(GbSpill sp, int C, int32_t *__restrict__ gkey, long long *__restrict_
 // ---------------------------------------------------------------------------
 // 2''. key order over a dense key range
 //
-// When the emitted keys span at most GB_DENSE_RANGE values, a group's place
-// in unsigned key order is the number of present keys below it.  The merge
-// records the smallest and largest key it wrote (mm); k_gb_dense_bits sets
-// one bit per group in a bitmap over [kmin, kmax]; k_gb_dense_scan turns the
-// bitmap into (bits below this word, word) pairs and clears it, so the
-// bitmap arena is all-zero again; k_gb_dense_place writes each group at its
-// word's prefix plus the popcount of the lower bits of its word.  A wider
-// range leaves all three kernels idle and the host sorts instead.
+// A group's place in unsigned key order is the number of present keys below
+// it.  The host picks a window [kbase, kbase + GB_DENSE_RANGE) (from the
+// context's previous key-ordered call); the merge sets one bit per emitted
+// key in a bitmap over that window, and records the smallest and largest key
+// it wrote (mm).  When every key fell inside the window, k_gb_dense_scan turns
+// the bitmap words of [kmin, kmax] into (bits below this word, word) pairs and
+// clears them, and k_gb_dense_place writes each group at its word's prefix
+// plus the popcount of the lower bits of its word.  Otherwise the scan clears
+// the whole window instead, the place kernel stays idle and the host sorts;
+// either way the bitmap arena is all-zero again afterwards.
 // ---------------------------------------------------------------------------
-constexpr long long GB_DENSE_RANGE = 1LL << 27;        // bitmap 16 MB
-constexpr size_t GB_DENSE_WORDS = GB_DENSE_RANGE / 32;  // 2^22 words
 constexpr int DN_THREADS = 256;
 constexpr int DN_WPT = 8;  // bitmap words per thread and round (two 16-byte loads)
 
-__device__ __forceinline__ bool gb_dense_range(const uint32_t *mm, uint32_t *kmin, uint32_t *words) {
-    const uint32_t lo = ~mm[0], hi = mm[1];
-    if (hi < lo) return false;  // no group
-    const unsigned long long range = (unsigned long long)(hi - lo) + 1ull;
-    if (range > (unsigned long long)GB_DENSE_RANGE) return false;
-    *kmin = lo;
-    *words = (uint32_t)((range + 31) >> 5);
+// Did every emitted key fall inside the window?  Then [*w0, *w1] are the
+// bitmap words that hold them.  hi < lo means no group at all.
+__host__ __device__ __forceinline__ bool gb_dense_fits(uint32_t lo, uint32_t hi, uint32_t kbase, uint32_t *w0,
+                                                       uint32_t *w1) {
+    if (hi < lo) return false;
+    const uint32_t a = lo - kbase, b = hi - kbase;
+    if (a > b || b >= (uint32_t)GB_DENSE_RANGE) return false;
+    *w0 = a >> 5;
+    *w1 = b >> 5;
     return true;
 }
 
-__global__ void __launch_bounds__(256)
-k_gb_dense_bits(const int32_t *__restrict__ gkey, long long cap, const long long *__restrict__ d_n,
-                const uint32_t *__restrict__ mm, uint32_t *__restrict__ bits) {
-    uint32_t kmin, words;
-    if (!gb_dense_range(mm, &kmin, &words)) return;
-    const long long g = *d_n < cap ? *d_n : cap;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g; i += stride) {
-        const uint32_t u = (uint32_t)__ldg(gkey + i) - kmin;
-        atomicOr(&bits[u >> 5], 1u << (u & 31));
-    }
-}
-
-// One CTA per chunk of whole 8-word groups; chunk c's prefix comes from a
-// look-back over chunks 0..c-1 (CTA index = chunk index).
+// One CTA per chunk of whole 8-word groups of [w0, w1]; chunk c's prefix
+// comes from a look-back over chunks 0..c-1 (CTA index = chunk index).
 __global__ void __launch_bounds__(DN_THREADS)
 k_gb_dense_scan(uint32_t *__restrict__ bits, uint2 *__restrict__ pre, const uint32_t *__restrict__ mm,
-                qg_lookback lb) {
+                uint32_t kbase, qg_lookback lb) {
     constexpr int NW = DN_THREADS / 32;
     constexpr uint32_t ROUND = DN_THREADS * DN_WPT;
     __shared__ uint32_t s_tile, s_epoch, s_excl;
     __shared__ uint32_t s_woff[NW], s_tmp[2 * NW + 1];
-    uint32_t kmin, words;
-    if (!gb_dense_range(mm, &kmin, &words)) return;
-    const uint32_t w8 = (words + 7) / 8;                      // 8-word groups in the range
-    const uint32_t per = (w8 + gridDim.x - 1) / gridDim.x;   // groups per chunk
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t lo_key = ~mm[0], hi_key = mm[1];
+    uint32_t w0, w1;
+    if (!gb_dense_fits(lo_key, hi_key, kbase, &w0, &w1)) {
+        if (hi_key < lo_key) return;  // no group: no bit was set
+        // Some keys fell outside the window: clear every bit the merge may
+        // have set (the whole window), with no look-back.
+        uint4 *b4 = reinterpret_cast<uint4 *>(bits);
+        for (size_t i = (size_t)blockIdx.x * DN_THREADS + tid; i < GB_DENSE_WORDS / 4;
+             i += (size_t)gridDim.x * DN_THREADS)
+            b4[i] = make_uint4(0, 0, 0, 0);
+        return;
+    }
+    const uint32_t g0 = w0 / 8, ng = w1 / 8 + 1 - g0;       // 8-word groups of [w0, w1]
+    const uint32_t per = (ng + gridDim.x - 1) / gridDim.x;  // groups per chunk
     qg_lb_begin(lb, &s_tile, &s_epoch);
     const uint32_t tile = s_tile;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t lo = min(w8, tile * per) * 8, hi = min(w8, (tile + 1) * per) * 8;
+    const uint32_t lo = (g0 + min(ng, tile * per)) * 8, hi = (g0 + min(ng, (tile + 1) * per)) * 8;
     auto load8 = [&](uint32_t w, uint32_t *x) {
         const uint4 a = reinterpret_cast<const uint4 *>(bits + w)[0];
         const uint4 b = reinterpret_cast<const uint4 *>(bits + w)[1];
@@ -984,16 +991,16 @@ k_gb_dense_scan(uint32_t *__restrict__ bits, uint2 *__restrict__ pre, const uint
 
 __global__ void __launch_bounds__(256)
 k_gb_dense_place(const unsigned long long *__restrict__ rec, long long cap, const long long *__restrict__ d_n,
-                 const uint32_t *__restrict__ mm, const uint2 *__restrict__ pre,
+                 const uint32_t *__restrict__ mm, uint32_t kbase, const uint2 *__restrict__ pre,
                  const long long *__restrict__ tsum, const long long *__restrict__ tcnt,
                  int32_t *__restrict__ gkey, long long *__restrict__ gsum, long long *__restrict__ gcnt) {
-    uint32_t kmin, words;
-    if (!gb_dense_range(mm, &kmin, &words)) return;
+    uint32_t w0, w1;
+    if (!gb_dense_fits(~mm[0], mm[1], kbase, &w0, &w1)) return;
     const long long g = *d_n < cap ? *d_n : cap;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < g; i += stride) {
         const uint32_t k = (uint32_t)(__ldg(rec + i) >> 32);
-        const uint32_t u = k - kmin;
+        const uint32_t u = k - kbase;
         const uint2 p = __ldg(pre + (u >> 5));
         const uint32_t pos = p.x + __popc(p.y & ((1u << (u & 31)) - 1u));
         gkey[pos] = (int32_t)k;
@@ -1194,11 +1201,14 @@ static qg_status gb_launch_global(qg_ctx *ctx, const int32_t *key, const int32_t
 // Two-pass path.  *d_flags != 0 afterwards means a spill bucket or a pass-2
 // table overflowed and the call must be redone with gb_launch_global.
 // Key order: ghist receives the digit counts of the emitted keys (the
-// device-planned sort), mm their smallest and largest key (the dense order).
+// device-planned sort), mm their smallest and largest key, and bits (when
+// set) one bit per key of the window [kbase, kbase + GB_DENSE_RANGE) (the
+// dense order).
 static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_t *val,
                                    const int32_t *val2, int32_t lo2, int32_t hi2, int64_t n,
                                    const GbOut &o, int64_t cap, long long *d_num,
-                                   unsigned int *d_flags, uint32_t *ghist, uint32_t *mm) {
+                                   unsigned int *d_flags, uint32_t *ghist, uint32_t *mm,
+                                   uint32_t *bits = nullptr, uint32_t kbase = 0) {
     int C = ctx->sm_count;
     if (C > GB_MAX_C) C = GB_MAX_C;
     const int slog2 = g_gb_hot_slog2;
@@ -1271,11 +1281,11 @@ static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_
     if (s64)
         k_gb_merge<true><<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
                                                              (unsigned long long *)d_num, o.rec, d_flags, work,
-                                                             ghist, mm);
+                                                             ghist, mm, bits, kbase);
     else
         k_gb_merge<false><<<g2, P2_THREADS, 0, ctx->stream>>>(sp, C, o.k, o.s, o.c, cap,
                                                               (unsigned long long *)d_num, o.rec, d_flags, work,
-                                                              ghist, mm);
+                                                              ghist, mm, bits, kbase);
     return qg_check_launch(ctx, "k_gb_merge");
 }
 
@@ -1306,41 +1316,38 @@ static qg_status gb_key_order_dev(qg_ctx *ctx, const GbOut &o, int64_t cap, long
     return qg_check_launch(ctx, "k_groupby_gather");
 }
 
-// Dense key order (see k_gb_dense_bits): three launches, all idle when the
-// emitted keys span more than GB_DENSE_RANGE values.
+// Dense key order after a merge that set the window's bits (see
+// k_gb_dense_scan): two launches, the place kernel idle when a key fell
+// outside the window.
 static qg_status gb_key_order_dense(qg_ctx *ctx, const GbOut &o, int64_t cap, const long long *d_num,
-                                    const uint32_t *mm, int32_t *gkey, int64_t *gsum, int64_t *gcnt) {
-    if (cap <= 0) return QG_OK;
-    char *bitp, *prep;
-    QG_TRY(qg_table(ctx, GB_DENSE_WORDS * 4, &bitp));
-    QG_TRY(qg_scratch(ctx, GB_DENSE_WORDS * 8, &prep));
+                                    const uint32_t *mm, uint32_t *bits, uint32_t kbase, int32_t *gkey,
+                                    int64_t *gsum, int64_t *gcnt) {
+    char *prep;
+    qg_status st = qg_scratch(ctx, GB_DENSE_WORDS * 8, &prep);
     qg_lookback lb;
-    QG_TRY(qg_lb_make(ctx, ctx->sm_count, QG_SITE_GROUPBY, &lb));
-    uint32_t *bits = (uint32_t *)bitp;
-    const int gb = grid_for(ctx, cap, 256, 8);
-    qg_pre_launch(ctx);
-    k_gb_dense_bits<<<gb, 256, 0, ctx->stream>>>(o.k, cap, d_num, mm, bits);
-    qg_status st = qg_check_launch(ctx, "k_gb_dense_bits");
+    if (st == QG_OK) st = qg_lb_make(ctx, ctx->sm_count, QG_SITE_GROUPBY, &lb);
     if (st == QG_OK) {
         qg_pre_launch(ctx);
-        k_gb_dense_scan<<<ctx->sm_count, DN_THREADS, 0, ctx->stream>>>(bits, (uint2 *)prep, mm, lb);
+        k_gb_dense_scan<<<ctx->sm_count, DN_THREADS, 0, ctx->stream>>>(bits, (uint2 *)prep, mm, kbase, lb);
         st = qg_check_launch(ctx, "k_gb_dense_scan");
     }
     if (st != QG_OK) {
-        ctx->table_dirty = true;  // bits may be left set
+        ctx->table_dirty = true;  // the merge's bits may be left set
         return st;
     }
+    if (cap <= 0) return QG_OK;
+    const int gb = grid_for(ctx, cap, 256, 8);
     qg_pre_launch(ctx);
-    k_gb_dense_place<<<gb, 256, 0, ctx->stream>>>(o.rec, cap, d_num, mm, (const uint2 *)prep, o.s, o.c,
+    k_gb_dense_place<<<gb, 256, 0, ctx->stream>>>(o.rec, cap, d_num, mm, kbase, (const uint2 *)prep, o.s, o.c,
                                                   gkey, (long long *)gsum, (long long *)gcnt);
     return qg_check_launch(ctx, "k_gb_dense_place");
 }
 
-// Host side of gb_dense_range: did the dense order place the groups?
-static bool gb_dense_applied(const qg_control *pin) {
-    const uint32_t *mm = (const uint32_t *)&pin->counter[4];
-    const uint32_t lo = ~mm[0], hi = mm[1];
-    return hi >= lo && (unsigned long long)(hi - lo) + 1ull <= (unsigned long long)GB_DENSE_RANGE;
+// The next call's window: centred on this call's keys (so that a range that
+// moves a little still fits), not below key 0.
+static uint32_t gb_dense_next_base(uint32_t lo, uint32_t hi) {
+    const uint32_t slack = (uint32_t)((GB_DENSE_RANGE - ((unsigned long long)(hi - lo) + 1)) / 2);
+    return lo > slack ? lo - slack : 0u;
 }
 
 extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key,
@@ -1392,10 +1399,17 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     const bool dense = o.rec && !ctx->gb_wide_keys;
     const bool dev_order = o.rec && !dense && cap < (1LL << 30);
     uint32_t *mm = (uint32_t *)&ctx->ctl->counter[4];
+    uint32_t *bits = nullptr;
+    const uint32_t kbase = ctx->gb_kbase;
     if (!global) {
+        if (dense) {
+            char *bitp;
+            QG_TRY(qg_table(ctx, GB_DENSE_WORDS * 4, &bitp));
+            bits = (uint32_t *)bitp;
+        }
         QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num, flags,
-                                 dev_order ? ctx->ctl->ghist : nullptr, o.rec ? mm : nullptr));
-        if (dense) QG_TRY(gb_key_order_dense(ctx, o, cap, d_num, mm, gkey, gsum, gcnt));
+                                 dev_order ? ctx->ctl->ghist : nullptr, o.rec ? mm : nullptr, bits, kbase));
+        if (dense) QG_TRY(gb_key_order_dense(ctx, o, cap, d_num, mm, bits, kbase, gkey, gsum, gcnt));
         if (dev_order) QG_TRY(gb_key_order_dev(ctx, o, cap, d_num, gkey, gsum, gcnt));
         // One read of the control block, at the end, brings the error word,
         // the group count (counter[1]) and the overflow flags (counter[2]).
@@ -1409,9 +1423,13 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
         global = (fl & 0xffffffffull) != 0;
         bool placed = dev_order;
         if (o.rec && g > 0) {  // the merge recorded the key range either way
-            const bool fits = gb_dense_applied(ctx->pin_ctl);
-            if (dense) placed = fits;
+            const uint32_t *pm = (const uint32_t *)&ctx->pin_ctl->counter[4];
+            const uint32_t lo = ~pm[0], hi = pm[1];
+            const bool fits = hi >= lo && (unsigned long long)(hi - lo) + 1ull <= (unsigned long long)GB_DENSE_RANGE;
+            uint32_t w0, w1;
+            if (dense) placed = gb_dense_fits(lo, hi, kbase, &w0, &w1);
             ctx->gb_wide_keys = !fits;
+            if (fits) ctx->gb_kbase = gb_dense_next_base(lo, hi);
         }
         done = !global && (!o.rec || placed || g == 0);
         ctx->gb_stats[0] = global ? 1u : 0u;

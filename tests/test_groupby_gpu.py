@@ -228,28 +228,52 @@ def test_groupby_cols_into_caller_buffers(ctx, orc):
         ctx.groupby_cols(dev(key), dev(val), cap=cap, out=(out[0][:10], out[1], out[2]))
 
 
-def test_groupby_key_order_dense_and_wide_ranges(ctx, orc):
-    # Key order places the groups by rank in a bitmap when their keys span at
-    # most 2^27 values, and sorts them otherwise; the context remembers the
-    # last call's spread.  The sequence takes every transition: dense, wide
-    # (placed after the count), wide (sorted on the device), dense (sorted,
-    # then back to the bitmap), and both sides of the 2^27 limit.
-    rng = np.random.default_rng(9)
-    n = 1 << 17
-
-    def keys(kind):
-        if kind == "dense":  # unsigned-contiguous across the signed boundary
-            return rng.integers(2 ** 31 - 3000, 2 ** 31 + 3000, n).astype(np.uint32).view(np.int32)
-        if kind == "wide":  # -5..5: the unsigned range is nearly 2^32
-            return rng.integers(-5, 6, n).astype(np.int32)
-        k = rng.integers(7, 7 + (1 << 27) - 1, n)
-        k[0], k[1] = 7, 7 + (1 << 27) - 1 + (kind == "over")  # 2^27 values, or one more
+def _key_order_keys(rng, n, kind):
+    if kind == "dense":  # unsigned-contiguous across the signed boundary
+        return rng.integers(2 ** 31 - 3000, 2 ** 31 + 3000, n).astype(np.uint32).view(np.int32)
+    if kind == "low":  # from key 0 up
+        k = rng.integers(0, 5000, n)
+        k[0] = 0
         return k.astype(np.int32)
+    if kind == "wide":  # -5..5: the unsigned range is nearly 2^32
+        return rng.integers(-5, 6, n).astype(np.int32)
+    k = rng.integers(7, 7 + (1 << 27) - 1, n)
+    k[0], k[1] = 7, 7 + (1 << 27) - 1 + (kind == "over")  # 2^27 values ("edge"), or one more
+    return k.astype(np.int32)
 
-    for kind in ["dense", "wide", "wide", "dense", "dense", "edge", "over", "over", "edge", "dense"]:
-        key = keys(kind)
+
+def _check_key_order_sequence(c, orc, kinds, seed):
+    rng = np.random.default_rng(seed)
+    n = 1 << 17
+    for kind in kinds:
+        key = _key_order_keys(rng, n, kind)
         val = rng.integers(-1000, 1000, n).astype(np.int32)
-        got = ctx.groupby_cols(dev(key), dev(val), cap=n)
+        got = c.groupby_cols(dev(key), dev(val), cap=n)
         check_groups(got, orc.groupby_cols(key, val))
-        fused = ctx.groupby_cols(dev(key), dev(val), dev(val), -10, 500, cap=n)
+        fused = c.groupby_cols(dev(key), dev(val), dev(val), -10, 500, cap=n)
         check_groups(fused, orc.groupby_cols(key, val, val, -10, 500))
+
+
+def test_groupby_key_order_dense_and_wide_ranges(ctx, orc):
+    # Key order places the groups by rank in a bitmap over a window of 2^27
+    # keys, which the merge fills; the window follows the context's previous
+    # key-ordered call.  Keys outside it (placed by a sort after the count),
+    # or spread wider than 2^27 (sorted on the device from then on), take the
+    # other paths.  The sequence takes every transition, both sides of the
+    # 2^27 limit and a window whose last word holds the largest key.
+    kinds = ["dense", "dense", "wide", "wide", "dense", "dense", "low", "low", "edge", "edge", "over",
+             "over", "edge", "edge", "dense", "dense"]
+    _check_key_order_sequence(ctx, orc, kinds, 9)
+
+
+def test_groupby_key_order_fresh_context_window(orc):
+    # A fresh context's first window starts at key 0: keys far from it fall
+    # back (and the merge's bits in the window are cleared), after which the
+    # window follows the keys and every later call is exact.
+    from query_on_opencl_fpga_gb300.api import Context
+
+    c = Context()
+    try:
+        _check_key_order_sequence(c, orc, ["dense", "dense", "low", "dense", "edge", "low", "low"], 10)
+    finally:
+        c.close()
