@@ -616,9 +616,18 @@ k_pj_join(PbArgs a, qg_lookback lb) {
         // a step are consecutive in the output and their stores coalesce
         r0 = min(sn, (uint32_t)warp * PB_WSEG);
         q = min(sn, r0 + PB_WSEG) - r0;
+        // The counting-sort counters are dead now: each row keeps its match
+        // count and first match there (count << 16 | 1 + R row) for the write.
         for (uint32_t r = r0 + lane; r < r0 + q; r += 32) {
             const uint32_t k = (uint32_t)(S.s[r] >> 32);
-            for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) my_cnt += (S.rk[e - 1] == k);
+            uint32_t m = 0, first = 0;
+            for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1])
+                if (S.rk[e - 1] == k) {
+                    first = m ? first : e;
+                    m++;
+                }
+            S.cnt[r] = (m << 16) | first;
+            my_cnt += m;
         }
     }
     // warp totals -> warp offsets within the bucket
@@ -643,10 +652,13 @@ k_pj_join(PbArgs a, qg_lookback lb) {
             const uint32_t r = s0 + lane;
             unsigned long long v = 0;
             uint32_t k = 0, m = 0;
+            uint32_t first = 0;
             if (r < r0 + q) {
                 v = S.s[r];
                 k = (uint32_t)(v >> 32);
-                for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) m += (S.rk[e - 1] == k);
+                const uint32_t x = S.cnt[r];
+                m = x >> 16;
+                first = x & 0xffffu;
             }
             // exclusive prefix of the lanes' match counts (0 or 1 in the common case)
             uint32_t pre;
@@ -663,7 +675,7 @@ k_pj_join(PbArgs a, qg_lookback lb) {
             }
             if (m) {
                 long long oo = o + pre;
-                for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1]) {
+                for (uint32_t e = first; e; e = S.next[e - 1]) {
                     if (S.rk[e - 1] != k) continue;
                     if (oo < a.cap) {
                         a.out_k[oo] = k;
