@@ -168,7 +168,11 @@ QG_API qg_status qg_scatter_rec(qg_ctx *ctx, const void *R, int64_t rLen, const 
  * filter_aggregation pipeline, kernel/filter_aggregation/
  * filter_aggregation_cu_op_dp.cl).  Outputs hold `cap` groups; order is
  * QG_ORDER_KEY (ascending unsigned key, the reference's sorted order) or
- * QG_ORDER_NONE.
+ * QG_ORDER_NONE.  `cap` also sizes the spill partitions (about 1024 groups
+ * each), so a cap near the true group count is fastest.  For key order the
+ * context remembers the key range of its previous call and ranks keys in a
+ * bitmap window placed there; results never depend on it, only the path
+ * does (keys outside the window are sorted after the count).
  * qg_groupby_cols_async is the same without a host round trip: the group
  * count goes to device memory (*d_num_groups); key order is sorted on the
  * device (two-pass path, cap < 2^30); a spill overflow is reported by
