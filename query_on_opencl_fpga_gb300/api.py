@@ -144,12 +144,19 @@ class Context:
         return out[: cnt.value]
 
     def filter_cols(self, key: torch.Tensor, pay: torch.Tensor, lo: int, hi: int,
-                    cap: int | None = None):
-        """Rows with lo <= key <= hi as int32 (row_id, payload) pairs, input order."""
+                    cap: int | None = None, out: torch.Tensor | None = None):
+        """Rows with lo <= key <= hi as int32 (row_id, payload) pairs, input order.
+
+        out: optional contiguous CUDA int32 tensor of shape (>= cap, 2) to
+        write into instead of allocating; the result is a view of it."""
         _check_dev(key, pay)
         n = key.numel()
         cap = n if cap is None else cap
-        out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=key.device)
+        if out is None:
+            out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=key.device)
+        elif (out.dtype != torch.int32 or not out.is_cuda or not out.is_contiguous() or out.dim() != 2
+              or out.shape[1] != 2 or out.shape[0] < max(cap, 1)):
+            raise ValueError("out: contiguous CUDA int32 tensor of shape (>= cap, 2)")
         cnt = c_int64()
         st = self.lib.qg_filter_cols(self.handle, _ptr(key), _ptr(pay), n, lo, hi, _ptr(out), cap,
                                      byref(cnt))

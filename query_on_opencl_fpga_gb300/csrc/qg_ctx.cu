@@ -97,8 +97,7 @@ QG_API qg_status qg_ctx_set_spin_limit(qg_ctx *ctx, uint32_t polls) {
 
 QG_API qg_status qg_ctx_check(qg_ctx *ctx) {
     if (!ctx) return QG_ERR_INVALID;
-    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-    return qg_collect_error(ctx);
+    return qg_collect_error(ctx);  // waits for the stream's work
 }
 
 QG_API const char *qg_last_error_message(qg_ctx *ctx) { return ctx ? ctx->msg : "no context"; }
@@ -328,20 +327,35 @@ qg_status qg_read_i64(qg_ctx *ctx, const long long *d, long long *h) {
     return QG_OK;
 }
 
+// Pinned slot 7 receives the error word and its site.
+static qg_status map_error(qg_ctx *ctx, const int32_t *h) {
+    if (h[0] == 0) return QG_OK;
+    // A kernel that gave up may have left the single-pass counters or the
+    // group-by table mid-way: reset them (in stream order).
+    cudaMemsetAsync(&ctx->ctl->err, 0, 2 * sizeof(int32_t), ctx->stream);
+    cudaMemsetAsync(&ctx->ctl->tile_ctr, 0, 2 * sizeof(uint32_t), ctx->stream);
+    cudaStreamSynchronize(ctx->stream);  // done before any later stream of this context runs
+    ctx->table_dirty = true;
+    snprintf(ctx->msg, sizeof(ctx->msg), "device error %d (%s) at site %d", h[0],
+             qg_status_string((qg_status)h[0]), h[1]);
+    return (qg_status)h[0];
+}
+
 qg_status qg_collect_error(qg_ctx *ctx) {
-    int32_t h[2] = {0, 0};
-    QG_TRY_CUDA(ctx, cudaMemcpy(h, &ctx->ctl->err, sizeof(h), cudaMemcpyDeviceToHost),
+    int32_t *h = reinterpret_cast<int32_t *>(ctx->pinned + 7);
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(h, &ctx->ctl->err, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream),
                 "read error word");
-    if (h[0] != 0) {
-        int32_t z[2] = {0, 0};
-        cudaMemcpy(&ctx->ctl->err, z, sizeof(z), cudaMemcpyHostToDevice);
-        // A kernel that gave up may have left the single-pass counters or the
-        // group-by table mid-way: reset them.
-        cudaMemset(&ctx->ctl->tile_ctr, 0, 2 * sizeof(uint32_t));
-        ctx->table_dirty = true;
-        snprintf(ctx->msg, sizeof(ctx->msg), "device error %d (%s) at site %d", h[0],
-                 qg_status_string((qg_status)h[0]), h[1]);
-        return (qg_status)h[0];
-    }
-    return QG_OK;
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    return map_error(ctx, h);
+}
+
+qg_status qg_read_count(qg_ctx *ctx, const long long *d, long long *h) {
+    int32_t *e = reinterpret_cast<int32_t *>(ctx->pinned + 7);
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, d, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream),
+                "cudaMemcpyAsync count");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(e, &ctx->ctl->err, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream),
+                "read error word");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+    *h = ctx->pinned[0];
+    return map_error(ctx, e);
 }

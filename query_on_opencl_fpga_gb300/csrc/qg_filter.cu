@@ -276,8 +276,7 @@ k_filter_cols_tma(const int32_t *__restrict__ key, const int32_t *__restrict__ p
 
 static qg_status finish_count(qg_ctx *ctx, long long *d_count, int64_t cap, int64_t *out_n) {
     long long h = 0;
-    QG_TRY(qg_read_i64(ctx, d_count, &h));
-    QG_TRY(qg_collect_error(ctx));
+    QG_TRY(qg_read_count(ctx, d_count, &h));
     *out_n = h;
     if (h > cap) return QG_ERR_CAPACITY;
     return QG_OK;

@@ -1049,8 +1049,7 @@ extern "C" QG_API qg_status qg_groupby_rec(qg_ctx *ctx, const void *in, int64_t 
                 (const uint4 *)sorted_out, n, startPos, cap_groups, d_count, lb);
             s = qg_check_launch(ctx, "k_group_bounds");
             long long h = 0;
-            if (s == QG_OK) s = qg_read_i64(ctx, d_count, &h);
-            if (s == QG_OK) s = qg_collect_error(ctx);
+            if (s == QG_OK) s = qg_read_count(ctx, d_count, &h);
             if (s == QG_OK) {
                 *num_groups = h;
                 if (h > cap_groups) s = QG_ERR_CAPACITY;
@@ -1442,8 +1441,7 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     }
     if (global) {
         QG_TRY(gb_launch_global(ctx, key, val, val2, lo2, hi2, n, o, cap, d_num));
-        QG_TRY(qg_read_i64(ctx, d_num, &g));
-        QG_TRY(qg_collect_error(ctx));
+        QG_TRY(qg_read_count(ctx, d_num, &g));
     }
     *num_groups = g;
     if (g > cap) return QG_ERR_CAPACITY;

@@ -87,8 +87,11 @@ qg_status qg_stage_bases(qg_ctx *ctx, const uint32_t *h_bases, uint32_t *d_dst);
 // Copy a device int64 to host (synchronises the stream).
 qg_status qg_read_i64(qg_ctx *ctx, const long long *d, long long *h);
 qg_status qg_check_launch(qg_ctx *ctx, const char *what);
-// Read the device error word after a synchronisation, clear it and map it.
+// Read the device error word (after the stream's work), clear it and map it.
 qg_status qg_collect_error(qg_ctx *ctx);
+// qg_read_i64 and qg_collect_error with one synchronisation: the count in *h,
+// the device error (if any) as the status.
+qg_status qg_read_count(qg_ctx *ctx, const long long *d, long long *h);
 
 #define QG_TRY_CUDA(ctx, expr, what)                            \
     do {                                                        \

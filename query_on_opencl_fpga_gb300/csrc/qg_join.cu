@@ -579,8 +579,7 @@ extern "C" QG_API qg_status qg_hash_join_ref(qg_ctx *ctx, const uint32_t *r, int
     k_join_probe_ref<<<blocks, 256, 0, ctx->stream>>>(s, nS, tab, mask, jc, out, cap);
     QG_TRY(qg_check_launch(ctx, "k_join_probe_ref"));
     long long m = 0;
-    QG_TRY(qg_read_i64(ctx, (const long long *)&jc->cursor, &m));
-    QG_TRY(qg_collect_error(ctx));
+    QG_TRY(qg_read_count(ctx, (const long long *)&jc->cursor, &m));
     *out_n = m;
     return m > cap ? QG_ERR_CAPACITY : QG_OK;
 }

@@ -95,11 +95,11 @@ extern "C" QG_API qg_status qg_reduce_rec(qg_ctx *ctx, const void *in, int64_t n
     k_reduce_rec<<<grid_of(ctx, n), 256, 0, ctx->stream>>>((const uint2 *)in, n, op, d);
     QG_TRY(qg_check_launch(ctx, "k_reduce_rec"));
     long long h = 0;
-    QG_TRY(qg_read_i64(ctx, (const long long *)d, &h));
+    QG_TRY(qg_read_count(ctx, (const long long *)d, &h));
     uint32_t v = (uint32_t)(unsigned long long)h;
     if (op == QG_REDUCE_AVERAGE) v = v / (uint32_t)n;
     *result = v;
-    return qg_ctx_check(ctx);
+    return QG_OK;
 }
 
 extern "C" QG_API qg_status qg_split_rec(qg_ctx *ctx, const void *in, int64_t n, int32_t num_part, void *out,

@@ -62,6 +62,19 @@ def test_filter_cols_config0_full_size(ctx, orc):
     assert np.array_equal(got.cpu().numpy(), exp)
 
 
+def test_filter_cols_into_caller_buffer(ctx, orc):
+    # out=: one caller-owned (cap, 2) buffer reused by calls of different selectivity
+    d = datagen.config0_filter(1 << 20, seed=12)
+    key, pay = d["key"].numpy(), d["payload"].numpy()
+    out = torch.empty((1 << 20, 2), dtype=torch.int32, device="cuda")
+    for lo, hi in ((d["lo"], d["hi"]), (0, 1 << 30), (5, 4)):
+        got = ctx.filter_cols(dev(key), dev(pay), lo, hi, out=out)
+        assert got.numel() == 0 or got.data_ptr() == out.data_ptr()  # an empty view reports 0
+        assert np.array_equal(got.cpu().numpy(), orc.filter_cols(key, pay, lo, hi))
+    with pytest.raises(ValueError):
+        ctx.filter_cols(dev(key), dev(pay), 0, 1, out=out[:10])
+
+
 def test_filter_repeat_is_deterministic(ctx):
     d = datagen.config0_filter(1 << 22, seed=5, device="cuda")
     a = ctx.filter_cols(d["key"], d["payload"], 0, 1 << 29).clone()
