@@ -986,8 +986,7 @@ qg_status pj_dhist(qg_ctx *ctx, const PjLevel &L, const qg_part_fn &pf, uint32_t
     kern<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl, bid_s);
     QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
-    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-    return qg_collect_error(ctx);
+    return qg_collect_error(ctx);  // synchronises: h is filled
 }
 
 // Fit the learned model on a sample of both sides' keys (records); the
@@ -1302,7 +1301,7 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     }
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 1, L.mjtot, 8, cudaMemcpyDeviceToHost, ctx->stream), "mjtot d2h");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
-    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    QG_TRY(qg_collect_error(ctx));  // synchronises: both counts are in
     const unsigned long long total = (unsigned long long)ctx->pinned[0];
     // The look-back sums are 32-bit: report the outside groups' 64-bit sum
     // when they alone could wrap it (a capacity error follows).
@@ -1387,16 +1386,17 @@ extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey
     k_pj_sfilter<<<(unsigned)tiles, SF_THREADS, 0, ctx->stream>>>(skey, spay, nS, slo, shi, range, S,
                                                                    &range->count, ctx->ctl);
     QG_TRY(qg_check_launch(ctx, "k_pj_sfilter"));
-    // one read brings R's key range and the S' count
-    PjRange hr;
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(&hr, range, sizeof(hr), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
-    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-    const long long ns1 = (long long)hr.count;
+    // one read brings R's key range, the S' count and the error word
+    static_assert(sizeof(PjRange) <= 2 * sizeof(long long), "two pinned slots");
+    PjRange *hp = reinterpret_cast<PjRange *>(ctx->pinned + 4);
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(hp, range, sizeof(PjRange), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
     QG_TRY(qg_collect_error(ctx));
+    const PjRange hr = *hp;
+    const long long ns1 = (long long)hr.count;
     long long M = 0;
+    // pj_core ends with a read of the output count and the error word
     QG_TRY(pj_core(ctx, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, g_pj_variant, (uint32_t *)out_key,
                    (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M, lvl));
-    QG_TRY(qg_collect_error(ctx));
     *out_n = M;
     return M > cap ? QG_ERR_CAPACITY : QG_OK;
 }
