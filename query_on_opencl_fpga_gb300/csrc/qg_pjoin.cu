@@ -1301,7 +1301,10 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     }
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 1, L.mjtot, 8, cudaMemcpyDeviceToHost, ctx->stream), "mjtot d2h");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
-    QG_TRY(qg_collect_error(ctx));  // synchronises: both counts are in
+    if (use_learned)  // the model's knot and heavy-key counts, for qg_join_stats
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 2, L.model, 16, cudaMemcpyDeviceToHost, ctx->stream),
+                    "model header d2h");
+    QG_TRY(qg_collect_error(ctx));  // synchronises: the counts (and header) are in
     const unsigned long long total = (unsigned long long)ctx->pinned[0];
     // The look-back sums are 32-bit: report the outside groups' 64-bit sum
     // when they alone could wrap it (a capacity error follows).
@@ -1321,8 +1324,7 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     ctx->pj_stats[5] = 0;
     ctx->pj_stats[6] = 0;
     if (use_learned) {
-        uint32_t hk[4];
-        cudaMemcpy(hk, L.model, 16, cudaMemcpyDeviceToHost);
+        const uint32_t *hk = reinterpret_cast<const uint32_t *>(ctx->pinned + 2);
         ctx->pj_stats[5] = hk[0];
         ctx->pj_stats[6] = hk[3];
     }
