@@ -866,7 +866,7 @@ namespace {
 int g_pj_variant = 0;  // 0 auto (radix; learned when a key sample shows that it spreads the rows better), 1 radix, 2 learned, 3 hash join + sort
 int g_pj_blog2 = 0;    // 0: fine bucket count from the input size
 uint32_t g_pj_smax = PB_SMAX, g_pj_rmax = PB_RMAX;
-constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit (and judge) the learned model
+constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit (and assess) the learned model
 
 struct PjLevel {
     PjRange *range;
@@ -1016,8 +1016,8 @@ qg_status pj_train(qg_ctx *ctx, const PjLevel &L, uint32_t nb, const unsigned lo
 }
 
 // Rows (estimated from the sample) that would land in buckets larger than the
-// bucket kernel takes, for each function: the judge between radix and learned.
-qg_status pj_judge(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot, const qg_part_fn &radix,
+// bucket kernel takes, for each function: the comparison between radix and learned.
+qg_status pj_compare(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot, const qg_part_fn &radix,
                    uint32_t nb_radix, const qg_part_fn &learned, uint32_t nb, double *over_radix,
                    double *over_learned) {
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.scnt, 0, (size_t)2 * nb * 4, ctx->stream), "memset scnt");
@@ -1107,23 +1107,23 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     const qg_part_fn learned{1, 0u, 0, L.model};
 
     // radix digit histograms; a lopsided high digit means skew, and then a
-    // key sample judges whether the learned function spreads the rows better
+    // key sample decides whether the learned function spreads the rows better
     uint32_t h[1024];
     QG_TRY(pj_dhist(ctx, L, radix, nb_radix, r, nR, s, nS, h));
     bool use_learned = may_learn && variant == 2;
-    bool judged = false;
+    bool compared = false;
     if (may_learn && variant == 0 && ntot >= (1 << 16)) {
         const uint32_t *hs = h + 512 + (nb_radix > 256 ? 256 : 0);
         const uint32_t nbin = nb_radix > 256 ? ((nb_radix - 1) >> 8) + 1 : nb_radix;
         uint32_t mx = 0;
         for (uint32_t i = 0; i < nbin; i++) mx = hs[i] > mx ? hs[i] : mx;
-        if ((double)mx > 4.0 * (double)nS / (double)nbin) judged = true;
+        if ((double)mx > 4.0 * (double)nS / (double)nbin) compared = true;
     }
     long long m = 0;
-    if (use_learned || judged) QG_TRY(pj_train(ctx, L, nb, r, nR, s, nS, &m));
-    if (judged) {
+    if (use_learned || compared) QG_TRY(pj_train(ctx, L, nb, r, nR, s, nS, &m));
+    if (compared) {
         double orad = 0, olrn = 0;
-        QG_TRY(pj_judge(ctx, L, m, ntot, radix, nb_radix, learned, nb, &orad, &olrn));
+        QG_TRY(pj_compare(ctx, L, m, ntot, radix, nb_radix, learned, nb, &orad, &olrn));
         use_learned = olrn < 0.5 * orad;
     }
     // The learned function is evaluated once per row: its bucket ids go to a
@@ -1328,7 +1328,7 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
         ctx->pj_stats[5] = hk[0];
         ctx->pj_stats[6] = hk[3];
     }
-    ctx->pj_stats[7] = (judged && use_learned) ? 1 : 0;
+    ctx->pj_stats[7] = (compared && use_learned) ? 1 : 0;
     return QG_OK;
 }
 

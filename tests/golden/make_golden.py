@@ -5,8 +5,8 @@ them with oracle/build_ref.sh).  For each case it
   1. runs the reference's own generator (host/host/generator.cpp) and checks
      that the oracle's restatement produces the same bytes,
   2. runs the oracle operator and has the reference's own validator
-     (host/host/Validate.cpp) judge the result, requiring its "passed" line,
-  3. stores input digests, the validator verdict and the oracle output (or its
+     (host/host/Validate.cpp) check the result, requiring its "passed" line,
+  3. stores input digests, the validator output and the oracle output (or its
      digest) in tests/golden/golden.npz / golden.json,
 and records the reference DP planner's printed plans
 (host/dynamic_programming.cpp) for the planner port.
@@ -69,12 +69,12 @@ def main() -> None:
         small = nxt % 100
         large = min(small + 6, 100)
         out = orc.filter_rec(rin, small, large)
-        verdict = orc.ref_tool("validate_filter", save_bin(tmp, "fin.bin", rin), n,
+        validator_output = orc.ref_tool("validate_filter", save_bin(tmp, "fin.bin", rin), n,
                                save_bin(tmp, "fout.bin", out), out.shape[0], small, large)
-        assert "filter passed" in verdict, verdict
+        assert "filter passed" in validator_output, validator_output
         meta["cases"]["filter"] = {"n": n, "maxmax": 100, "seed": 0, "small": int(small),
                                    "large": int(large), "out_n": int(out.shape[0]),
-                                   "input_sha": sha(rin), "verdict": verdict.strip()}
+                                   "input_sha": sha(rin), "validator_output": validator_output.strip()}
         arrays["filter_out"] = out
 
         # ---- scan: testScanImpl (host/host/testScan.cpp:342-390) ----------------
@@ -84,19 +84,19 @@ def main() -> None:
         sin = np.fromfile(p, np.int32)
         assert np.array_equal(sin, orc.generate_rand_int(n, n, 0))
         sout = orc.scan_excl(sin)
-        verdict = orc.ref_tool("validate_scan", p, n, save_bin(tmp, "scan_out.bin", sout))
-        assert "scan test pass!" in verdict, verdict
+        validator_output = orc.ref_tool("validate_scan", p, n, save_bin(tmp, "scan_out.bin", sout))
+        assert "scan test pass!" in validator_output, validator_output
         meta["cases"]["scan"] = {"n": n, "input_sha": sha(sin), "output_sha": sha(sout),
-                                 "verdict": verdict.strip()}
+                                 "validator_output": validator_output.strip()}
 
         # ---- sort: testSortImpl (host/host/testSort.cpp:276-296) ----------------
         for n in (2048, 1 << 15, 100003):
             rin, _ = ref_gen_rand(200, n, 0, tmp)
             srt = orc.sort_rec(rin)
-            verdict = orc.ref_tool("validate_sort", save_bin(tmp, "sorted.bin", srt), n)
-            assert "sorting passed" in verdict, verdict
+            validator_output = orc.ref_tool("validate_sort", save_bin(tmp, "sorted.bin", srt), n)
+            assert "sorting passed" in validator_output, validator_output
             meta["cases"][f"sort_{n}"] = {"n": n, "maxmax": 200, "input_sha": sha(rin),
-                                          "keys_sorted_sha": sha(srt[:, 1]), "verdict": verdict.strip()}
+                                          "keys_sorted_sha": sha(srt[:, 1]), "validator_output": validator_output.strip()}
 
         # ---- group-by: testGroupByImpl (host/host/testGroupBy.cpp:156-175) -------
         # Keys are taken mod maxmax into [0, maxmax): under glibc generateRand
@@ -108,11 +108,11 @@ def main() -> None:
         rin[:, 1] = np.mod(rin[:, 1], 64)
         srt = orc.sort_rec(rin)
         sp = orc.group_startpos(srt)
-        verdict = orc.ref_tool("validate_groupby", save_bin(tmp, "gin.bin", rin), n,
+        validator_output = orc.ref_tool("validate_groupby", save_bin(tmp, "gin.bin", rin), n,
                                save_bin(tmp, "gsrt.bin", srt), save_bin(tmp, "gsp.bin", sp), sp.size)
-        assert "GroupBy Test passed!" in verdict, verdict
+        assert "GroupBy Test passed!" in validator_output, validator_output
         meta["cases"]["groupby"] = {"n": n, "maxmax": 64, "num_groups": int(sp.size),
-                                    "input_sha": sha(rin), "verdict": verdict.strip()}
+                                    "input_sha": sha(rin), "validator_output": validator_output.strip()}
         arrays["groupby_startpos"] = sp
 
         # ---- aggregation: testAggAfterGroupByImpl (host/host/testAggAfterGB.cpp:127-255)
@@ -126,16 +126,16 @@ def main() -> None:
         aggcase = {"n": n, "maxmax": 50, "num_groups": int(sp.size), "input_sha": sha(rin)}
         for op, name in enumerate(["sum", "max", "min", "avg"]):
             agg = orc.aggregate_groups(srt, sp, op)
-            verdict = orc.ref_tool("validate_agg", save_bin(tmp, "asrt.bin", srt), n,
+            validator_output = orc.ref_tool("validate_agg", save_bin(tmp, "asrt.bin", srt), n,
                                    save_bin(tmp, "asp.bin", sp), sp.size,
                                    save_bin(tmp, "ragg.bin", ragg), save_bin(tmp, "agg.bin", agg), op)
-            assert "Test Passed!" in verdict, (name, verdict)
+            assert "Test Passed!" in validator_output, (name, validator_output)
             if op == 1:
                 easy = orc.ref_tool("validate_agg_easy", save_bin(tmp, "asrt.bin", srt), n,
                                     save_bin(tmp, "asp.bin", sp), sp.size,
                                     save_bin(tmp, "agg.bin", agg), op)
                 assert "Agg Test Passed!" in easy, easy
-            aggcase[f"{name}_verdict"] = verdict.strip()
+            aggcase[f"{name}_validator_output"] = validator_output.strip()
             arrays[f"agg_{name}"] = agg
         meta["cases"]["aggregate"] = aggcase
 

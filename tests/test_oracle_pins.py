@@ -34,7 +34,7 @@ def test_filter_golden(orc, golden):
     out = orc.filter_rec(rin, c["small"], c["large"])
     assert out.shape[0] == c["out_n"]
     assert np.array_equal(out, arrs["filter_out"])
-    assert c["verdict"] == "filter passed"
+    assert c["validator_output"] == "filter passed"
 
 
 def test_filter_cols_matches_rec_form(orc):
@@ -95,7 +95,7 @@ def test_aggregate_golden(orc, golden, op, name):
     srt = orc.sort_rec(rin)
     sp = orc.group_startpos(srt)
     assert np.array_equal(orc.aggregate_groups(srt, sp, op), arrs[f"agg_{name}"])
-    assert c[f"{name}_verdict"] == "Test Passed!"
+    assert c[f"{name}_validator_output"] == "Test Passed!"
 
 
 def test_aggregate_reference_inits(orc):
