@@ -45,6 +45,7 @@ struct qg_ctx {
     uint32_t gb_stats[4];   // last qg_groupby_cols: path, flags, fullest bucket, bucket cap
     bool gb_wide_keys;      // last key-ordered group-by's keys spanned too wide a range for the dense order
     uint32_t gb_kbase;      // first key of the next dense-order window (from the last call's keys)
+    bool sort_odd_passes;   // the last in-place record sort took an odd number of passes
     uint32_t pj_stats[8];   // last qg_join_filter_sort (see qg_join_stats)
     char *pj_tmp;           // the join's sort-merge arrays (grow-only)
     size_t pj_tmp_bytes;

@@ -21,6 +21,7 @@
 //   KV3: three u32 columns (key, a, b) -- the join output (key, R.payload,
 //        S.payload).
 #include <string.h>
+#include <utility>
 #include <vector>
 #include "qg_internal.cuh"
 #include "qg_sort.cuh"
@@ -40,13 +41,21 @@ constexpr uint32_t ST_VAL = (1u << 30) - 1;
 
 __global__ void __launch_bounds__(256)
 k_radix_hist(const uint32_t *__restrict__ kin, const unsigned long long *__restrict__ rin,
-             long long n, uint32_t key_off, int npos, uint32_t *__restrict__ ghist) {
+             long long n, uint32_t key_off, int npos, uint32_t *__restrict__ ghist,
+             unsigned long long *__restrict__ copy) {
     __shared__ uint32_t sh[4][QG_RADIX];
     for (int i = threadIdx.x; i < 4 * QG_RADIX; i += blockDim.x) (&sh[0][0])[i] = 0;
     __syncthreads();
     long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        uint32_t k = (kin ? __ldg(kin + i) : (uint32_t)(__ldg(rin + i) >> 32)) - key_off;
+        uint32_t k;
+        if (kin) {
+            k = __ldg(kin + i) - key_off;
+        } else {
+            const unsigned long long v = __ldg(rin + i);
+            if (copy) copy[i] = v;  // records: optionally a copy for the passes to start from
+            k = (uint32_t)(v >> 32) - key_off;
+        }
         for (int p = 0; p < npos; p++) atomicAdd(&sh[p][(k >> (8 * p)) & 255u], 1u);
     }
     __syncthreads();
@@ -297,7 +306,7 @@ int qg_sort_positions(int bits) {
 }
 
 qg_status qg_radix_histogram(qg_ctx *ctx, const qg_sort_bufs &src, bool kv3, long long n,
-                             uint32_t key_off, int npos, uint32_t *d_hist) {
+                             uint32_t key_off, int npos, uint32_t *d_hist, unsigned long long *copy) {
     QG_TRY_CUDA(ctx, cudaMemsetAsync(d_hist, 0, 4 * QG_RADIX * 4, ctx->stream), "memset hist");
     if (n == 0) return QG_OK;
     int hblocks = ctx->sm_count * 4;
@@ -305,7 +314,7 @@ qg_status qg_radix_histogram(qg_ctx *ctx, const qg_sort_bufs &src, bool kv3, lon
     if (hblocks > maxb) hblocks = (int)maxb;
     qg_pre_launch(ctx);
     k_radix_hist<<<hblocks, 256, 0, ctx->stream>>>(kv3 ? src.k : nullptr, kv3 ? nullptr : src.rec,
-                                                   n, key_off, npos, d_hist);
+                                                   n, key_off, npos, d_hist, kv3 ? nullptr : copy);
     return qg_check_launch(ctx, "k_radix_hist");
 }
 
@@ -482,17 +491,24 @@ qg_status qg_sort_rec_inplace(qg_ctx *ctx, unsigned long long *data, unsigned lo
     uint32_t *d_hist = (uint32_t *)scr;
     qg_sort_bufs a{};
     a.rec = data;
-    QG_TRY(qg_radix_histogram(ctx, a, false, n, 0u, 4, d_hist));
+    // An odd number of passes ends in tmp.  When the context's last sort
+    // needed an odd number, the histogram kernel (bound by its shared-memory
+    // atomics, not by DRAM) also copies the records to tmp, and the passes
+    // start there and end in data; otherwise a copy back follows.
+    const bool pre_copy = ctx->sort_odd_passes;
+    QG_TRY(qg_radix_histogram(ctx, a, false, n, 0u, 4, d_hist, pre_copy ? tmp : nullptr));
     std::vector<uint32_t> h(4 * QG_RADIX), bases(4 * QG_RADIX);
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(h.data(), d_hist, 4 * QG_RADIX * 4, cudaMemcpyDeviceToHost, ctx->stream), "hist d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
     int passes[4];
     int np = qg_sort_plan(h.data(), 4, n, passes, bases.data());
+    ctx->sort_odd_passes = (np & 1) != 0;
     qg_sort_bufs b{};
     b.rec = tmp;
+    if ((np & 1) && pre_copy) std::swap(a, b);  // from the copy in tmp into data
     bool in_b = false;
     QG_TRY(qg_radix_passes(ctx, false, a, b, n, 0u, passes, np, bases.data(), &in_b));
-    if (in_b)
+    if ((in_b ? b.rec : a.rec) != data)
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(data, tmp, (size_t)n * 8, cudaMemcpyDeviceToDevice, ctx->stream), "copy");
     return QG_OK;
 }

@@ -21,9 +21,11 @@ struct qg_sort_bufs {
 
 // Number of 8-bit digit positions covering `bits` key bits (1..4).
 int qg_sort_positions(int bits);
-// Device histogram of (key - key_off) digits for `npos` positions into d_hist[4][256].
+// Device histogram of (key - key_off) digits for `npos` positions into
+// d_hist[4][256]; for records, `copy` (if set) also receives a copy of them.
 qg_status qg_radix_histogram(qg_ctx *ctx, const qg_sort_bufs &src, bool kv3, long long n,
-                             uint32_t key_off, int npos, uint32_t *d_hist);
+                             uint32_t key_off, int npos, uint32_t *d_hist,
+                             unsigned long long *copy = nullptr);
 // From a host copy of the histogram: the non-trivial positions (returned
 // count) and every position's exclusive digit bases.
 int qg_sort_plan(const uint32_t *h_hist, int npos, long long n, int *passes, uint32_t *bases);
