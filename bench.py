@@ -384,7 +384,7 @@ def run_ours(args, rank, world, local):
 
 
 def operator_lines(ctx, args, peak, stream):
-    """Per-operator rows/s and roofline for the filter and join configurations."""
+    """Per-operator rows/s and roofline: filter, group-by, join and sort configurations."""
     import torch
 
     from query_on_opencl_fpga_gb300 import datagen
@@ -458,12 +458,55 @@ def operator_lines(ctx, args, peak, stream):
                            "roofline_sfilter": roofline(kern, "k_pj_sfilter", nS * 8 + sp * 8, peak)}
     del j, res
     torch.cuda.empty_cache()
+    out["sort_64M"] = sort_line(ctx, steps, peak, stream)
+    torch.cuda.empty_cache()
     if not args.no_learned:
         out["skew_join_config4"] = skew_line(ctx, stream)
         torch.cuda.empty_cache()
         out["batched_config3"] = batched_line(ctx, stream)
         torch.cuda.empty_cache()
     return out
+
+
+def sort_line(ctx, steps, peak, stream):
+    """In-place sort of 64M reference Records by unsigned y (radixSortImpl_sm),
+    keys uniform in [0, 2^20): three 8-bit passes.  Every step sorts a fresh
+    copy of the same unsorted records; the copy is outside the timed call."""
+    import torch
+
+    from query_on_opencl_fpga_gb300.datagen import records, uniform_i32
+
+    ns = 1 << 26
+    base = records(uniform_i32(ns, 0, 1 << 20, 0, "cuda"))
+    rec = torch.empty_like(base)
+    for _ in range(2):
+        rec.copy_(base)
+        ctx.sort_rec(rec)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for e0, e1 in ev:
+        rec.copy_(base)
+        e0.record(stream)
+        ctx.sort_rec(rec)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    keys = rec[:, 1]
+    ok = bool((keys[1:] >= keys[:-1]).all()) and int(keys.sum()) == int(base[:, 1].sum())
+    ctx.timing_report()
+    ctx.enable_timing(True)
+    for _ in range(steps):
+        rec.copy_(base)
+        ctx.sort_rec(rec)
+    torch.cuda.synchronize()
+    kern = ctx.timing_report()
+    ctx.enable_timing(False)
+    passes = kern.get("k_radix_pass", (0, 0.0))[0] // steps
+    alg = ns * 16 * passes  # one read and one write of the records per key pass
+    del base, rec
+    return {"rows_per_s": ns / (ms * 1e-3), "ms_per_op": ms, "rows": ns, "passes": passes, "sorted": ok,
+            "op_frac_of_peak": alg / (ms * 1e-3) / 1e9 / peak,
+            "kernels_ms": {k: v[1] / steps for k, v in kern.items()},
+            "roofline": roofline(kern, "k_radix_pass", ns * 16, peak)}
 
 
 def skew_line(ctx, stream):
