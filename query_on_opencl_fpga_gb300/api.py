@@ -47,9 +47,14 @@ class Context:
         self.handle = h
 
     def close(self) -> None:
+        self.release_out_buffers()
         if getattr(self, "handle", None):
             self.lib.qg_ctx_destroy(self.handle)
             self.handle = None
+
+    def release_out_buffers(self) -> None:
+        """Forget the output buffer sets remembered by groupby_cols(out=...)."""
+        self.__dict__.pop("_gb_out", None)
 
     def __del__(self):  # pragma: no cover - best effort
         try:
@@ -203,7 +208,9 @@ class Context:
 
         out: optional (key int32, sum int64, count int64) CUDA tensors of at
         least `cap` elements to write into instead of allocating; the returned
-        tensors are views of them."""
+        tensors are views of them.  The context remembers its last 4 such sets
+        (validated pointers and result views, so they stay allocated) until
+        release_out_buffers() or close()."""
         _check_dev(key, val, val2)
         n = key.numel()
         if out is None:

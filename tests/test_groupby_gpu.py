@@ -226,6 +226,10 @@ def test_groupby_cols_into_caller_buffers(ctx, orc):
         check_groups(got, orc.groupby_cols(key, val, v2, d["lo2"], d["hi2"]))
     with pytest.raises(ValueError):
         ctx.groupby_cols(dev(key), dev(val), cap=cap, out=(out[0][:10], out[1], out[2]))
+    # after the remembered sets are dropped the same buffers validate again
+    ctx.release_out_buffers()
+    got = ctx.groupby_cols(dev(key), dev(val), cap=cap, out=out)
+    check_groups(got, orc.groupby_cols(key, val))
 
 
 def _key_order_keys(rng, n, kind):
