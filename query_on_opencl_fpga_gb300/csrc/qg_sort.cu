@@ -93,7 +93,7 @@ __device__ __forceinline__ uint32_t rs_digit(uint32_t k, uint32_t key_off, int s
 // took 1.29 ms this way against 1.57 ms with two CTAs at 126 registers.
 // DIG: 0 radix digit of the key, 1 learned partition function of the key,
 // 2 bits of the bucket id in the source's sidecar (REC only).
-template <bool KV3, int DIG>
+template <bool KV3, int DIG, bool MATCH = false>
 __global__ void __launch_bounds__(RS_THREADS, 4)
 k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
              const qg_cdf_model *model, const uint32_t *__restrict__ dbase,
@@ -184,11 +184,18 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
         const uint32_t ki = KV3 ? key[i] : (uint32_t)(val[i] >> 32);
         const uint32_t d = side ? (rd[i] >> shift) & 255u : rs_digit<DIG == 1>(ki, key_off, shift, model);
         rd[i] = d << 24;
-        uint32_t peers = __ballot_sync(QG_FULL_MASK, valid);
+        // lanes holding the same digit: one match instruction (passes with
+        // few digit values in use) or eight ballots
+        uint32_t peers;
+        if (MATCH) {
+            peers = __match_any_sync(QG_FULL_MASK, valid ? d : 256u);  // the tail's invalid lanes share 256
+        } else {
+            peers = __ballot_sync(QG_FULL_MASK, valid);
 #pragma unroll
-        for (int b = 0; b < 8; b++) {
-            uint32_t bal = __ballot_sync(QG_FULL_MASK, (d >> b) & 1u);
-            peers &= ((d >> b) & 1u) ? bal : ~bal;
+            for (int b = 0; b < 8; b++) {
+                const uint32_t bal = __ballot_sync(QG_FULL_MASK, (d >> b) & 1u);
+                peers &= ((d >> b) & 1u) ? bal : ~bal;
+            }
         }
         uint32_t before = valid ? S.whist[warp][d] : 0u;
         __syncwarp();
@@ -338,11 +345,27 @@ template <bool KV3, int DIG>
 static qg_status rs_set_attr(qg_ctx *ctx) {
     static bool done = false;
     if (!done) {
-        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
         done = true;
     }
     return QG_OK;
+}
+
+// Ranking by match instruction for a pass with at most 16 digit values in
+// use (the top pass of narrow keys): measured faster there (the 64M-record
+// sort of 20-bit keys, 1.30 -> 1.22 ms over its passes), while passes with
+// many digit values were slower with it (the join's partition passes 1.10 ->
+// 1.38 ms) and keep the eight ballots.
+static bool rs_few_digits(const uint32_t *hb, long long n) {
+    int used = 0;
+    for (int d = 0; d < QG_RADIX; d++) {
+        const unsigned long long hi = d + 1 < QG_RADIX ? hb[d + 1] : (unsigned long long)n;
+        used += hi > hb[d];
+    }
+    return used <= 16;
 }
 
 qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
@@ -376,19 +399,16 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
         qg_sort_bufs d = in_a ? b : a;
         if (side && i == np - 1) d.bid = nullptr;  // the last pass's ids are not read again
         const int shift = (pf.learned || side) ? 8 * p : pf.shift + 8 * p;
+        const bool m = rs_few_digits(h_bases + p * QG_RADIX, n);
+        auto kern = kv3 ? (m ? k_radix_pass<true, 0, true> : k_radix_pass<true, 0, false>)
+                    : side ? (m ? k_radix_pass<false, 2, true> : k_radix_pass<false, 2, false>)
+                    : pf.learned ? (m ? k_radix_pass<false, 1, true> : k_radix_pass<false, 1, false>)
+                                 : (m ? k_radix_pass<false, 0, true> : k_radix_pass<false, 0, false>);
         qg_pre_launch(ctx);
-        if (kv3)
-            k_radix_pass<true, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
-        else if (side)
-            k_radix_pass<false, 2><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, 0u, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
-        else if (pf.learned)
-            k_radix_pass<false, 1><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, 0u, pf.model, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
-        else
-            k_radix_pass<false, 0><<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(
-                s, d, n, shift, pf.kmin, nullptr, dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit, nullptr, nullptr);
+        kern<<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(s, d, n, shift, (kv3 || !(side || pf.learned)) ? pf.kmin : 0u,
+                                                                 pf.learned && !side ? pf.model : nullptr,
+                                                                 dbase + p * QG_RADIX, status, ctx->ctl, ctx->spin_limit,
+                                                                 nullptr, nullptr);
         QG_TRY(qg_check_launch(ctx, "k_radix_pass"));
         in_a = !in_a;
     }
