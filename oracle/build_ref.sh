@@ -16,19 +16,23 @@
 #                            cannot express on a parameter); nothing else in
 #                            them changes.
 #
+# Usage: oracle/build_ref.sh [REFERENCE_CHECKOUT]
+# The reference checkout is the first argument, else $QG_REFERENCE_DIR; with
+# neither (or a path that does not exist) only liboracle.so is built.
+#
 # Test infrastructure only.  Outputs go to oracle/ and oracle/_ref/ (both
 # git-ignored build products).  The reference sources are read in place and
 # never copied.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${QG_REFERENCE_DIR:-/root/reference}"
+REF="${1:-${QG_REFERENCE_DIR:-}}"
 
 CC=${CC:-gcc}
 if ! $CC -O2 -fPIC -shared -fopenmp -o "$HERE/liboracle.so" "$HERE/qg_oracle.c" 2>/dev/null; then
     $CC -O2 -fPIC -shared -o "$HERE/liboracle.so" "$HERE/qg_oracle.c"
 fi
 
-if [ -d "$REF/host/host" ]; then
+if [ -n "$REF" ] && [ -d "$REF/host/host" ]; then
     OUT="$HERE/_ref"
     mkdir -p "$OUT/stub/CL"
     cp "$HERE/ref_stub/CL/opencl.h" "$OUT/stub/CL/opencl.h"
@@ -44,7 +48,7 @@ if [ -d "$REF/host/host" ]; then
         -o "$OUT/ref_tool"
 fi
 
-if [ -d "$REF/kernel" ]; then
+if [ -n "$REF" ] && [ -d "$REF/kernel" ]; then
     OUT="$HERE/_ref"
     K="$OUT/kernels"
     mkdir -p "$K"

@@ -262,8 +262,8 @@ class Context:
         """Path and spill diagnostics of the last groupby_cols call."""
         out = (ctypes.c_uint32 * 4)()
         self.check(self.lib.qg_groupby_stats(self.handle, out), "qg_groupby_stats")
-        return {"path": "global_table" if out[0] else "two_pass", "flags": out[1],
-                "fullest_bucket": out[2], "bucket_cap": out[3]}
+        path = {0: "two_pass", 1: "global_table", 2: "dense"}[out[0]]
+        return {"path": path, "flags": out[1], "fullest_bucket": out[2], "bucket_cap": out[3]}
 
     # ---- join ---------------------------------------------------------------
     def join_filter_sort(self, rkey, rpay, skey, spay, slo: int = INT32_MIN, shi: int = INT32_MAX,

@@ -1097,6 +1097,7 @@ extern "C" QG_API qg_status qg_aggregate_groups(qg_ctx *ctx, const void *sorted,
 // host: column hash group-by
 // ---------------------------------------------------------------------------
 static int g_gb_mode = 0;            // 0: two-pass (global table as fallback), 1: global table only
+static int g_gb_dense = 1;           // 1: the dense-window path first (qg_gbdense.cu), two-pass when it does not apply
 static int g_gb_hot_slog2 = 13;      // pass-1 shared-memory table slots (log2)
 static int g_gb_plog2 = 0;           // spill partitions (log2); 0 = chosen from cap
 static uint32_t g_gb_capm = 0;       // spill bucket capacity override (0 = automatic)
@@ -1108,8 +1109,9 @@ static uint32_t g_gb_last_capm = 0;  // bucket capacity of the last two-pass lau
 static const int g_gb_slog2 = 12;    // fallback kernel: shared-memory table slots (log2)
 
 // Path and overflow diagnostics of the context's last qg_groupby_cols call:
-// out[0] = 0 two-pass / 1 global table, out[1] = overflow flags (bit 0 spill
-// bucket, bit 1 pass-2 table), out[2] = fullest spill bucket, out[3] = bucket capacity.
+// out[0] = 0 two-pass / 1 global table / 2 dense window, out[1] = overflow
+// flags (bit 0 spill bucket, bit 1 pass-2 table), out[2] = fullest spill
+// bucket, out[3] = bucket capacity (the last three 0 on the dense path).
 extern "C" QG_API qg_status qg_groupby_stats(qg_ctx *ctx, uint32_t *out) {
     if (!ctx || !out) return QG_ERR_INVALID;
     for (int i = 0; i < 4; i++) out[i] = ctx->gb_stats[i];
@@ -1119,11 +1121,12 @@ static const int g_gb_blocks_per_sm = 2;
 
 extern "C" QG_API qg_status qg_groupby_set_knobs(int mode, int hot_slots_log2, int partitions_log2,
                                                  uint32_t bucket_cap) {
-    if (mode < 0 || mode > 2 || hot_slots_log2 < 8 || hot_slots_log2 > 13 || partitions_log2 < 0 ||
+    if (mode < 0 || mode > 3 || hot_slots_log2 < 8 || hot_slots_log2 > 13 || partitions_log2 < 0 ||
         partitions_log2 > 13)
         return QG_ERR_INVALID;
     g_gb_mode = mode == 1 ? 1 : 0;
     g_gb_sum64 = mode == 2 ? 1 : 0;
+    g_gb_dense = mode == 0 ? 1 : 0;
     g_gb_hot_slog2 = hot_slots_log2;
     g_gb_plog2 = partitions_log2;
     g_gb_capm = bucket_cap;
@@ -1395,6 +1398,27 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     // found its keys too widely spread, then the device-planned sort (up to
     // 2^30 records).  Whatever neither placed is sorted after the host has
     // read the count.
+    if (g_gb_dense && !global && n > 0) {
+        // Dense-window path: output in key order whatever `order` asks for;
+        // one read of the control block brings the error word, the group
+        // count and whether every row fell inside the window.
+        QG_TRY(qg_gbd_launch(ctx, key, val, val2, lo2, hi2, n, gkey, gsum, gcnt, cap, d_num));
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pin_ctl, ctx->ctl, offsetof(qg_control, ghist),
+                                         cudaMemcpyDeviceToHost, ctx->stream),
+                    "ctl d2h");
+        QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+        if (ctx->pin_ctl->err != 0) return qg_collect_error(ctx);
+        const uint32_t outside = ctx->pin_ctl->gbd[QG_GBD_OUTSIDE];
+        if (outside == 0) {
+            g = (long long)ctx->pin_ctl->counter[1];
+            ctx->gb_stats[0] = 2u;
+            ctx->gb_stats[1] = ctx->gb_stats[2] = ctx->gb_stats[3] = 0;
+            *num_groups = g;
+            return g > cap ? QG_ERR_CAPACITY : QG_OK;
+        }
+        // some key fell outside the sampled window (or the sample spread too
+        // wide for one): the two-pass path below writes the output instead
+    }
     const bool dense = o.rec && !ctx->gb_wide_keys;
     const bool dev_order = o.rec && !dense && cap < (1LL << 30);
     uint32_t *mm = (uint32_t *)&ctx->ctl->counter[4];

@@ -17,6 +17,7 @@ struct qg_control {
     uint32_t done_ctr;  // finished CTAs of the running single-pass kernel
     uint32_t pad0;
     unsigned long long counter[6];  // scratch counters (output cursors)
+    uint32_t gbd[48];               // per-call state of the dense-window group-by (qg_gbdense.cu)
     uint32_t ghist[4 * 256];        // digit counts of emitted group keys (group-by in key order)
 };
 
@@ -70,6 +71,14 @@ enum {
 };
 
 qg_status qg_cuda_fail(qg_ctx *ctx, cudaError_t e, const char *what);
+// Dense-window column group-by (qg_gbdense.cu): launches the whole path on the
+// context's stream, output in ascending unsigned key order; the caller reads
+// ctl->gbd[QG_GBD_OUTSIDE] (non-zero: the path did not apply, nothing valid
+// was written) and the group count (*d_num) after its one synchronisation.
+qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
+                        int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt,
+                        int64_t cap, long long *d_num);
+enum { QG_GBD_OUTSIDE = 6 };
 // Ensure the scratch arena holds at least `bytes`; newly grown memory is zeroed.
 qg_status qg_scratch(qg_ctx *ctx, size_t bytes, char **out);
 // Ensure the operator-temporary arena holds at least `bytes` (not zeroed).

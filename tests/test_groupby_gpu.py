@@ -139,8 +139,9 @@ def test_groupby_global_table_path(ctx, orc, knobs, fused):
 
 
 def test_groupby_spill_overflow_falls_back(ctx, orc, knobs):
-    # bucket capacity 1 overflows at once: the call is redone on the global table
-    knobs(0, 8, 4, 1)
+    # two-pass path (mode 3), bucket capacity 1 overflows at once: the call is
+    # redone on the global table
+    knobs(3, 8, 4, 1)
     d = datagen.config1_groupby(1 << 18, 1 << 14, seed=12)
     key, val = d["key"].numpy(), d["val"].numpy()
     got = ctx.groupby_cols(dev(key), dev(val), cap=1 << 15)
@@ -152,7 +153,7 @@ def test_groupby_async_overflow_reports_table_full(ctx, knobs):
 
     from query_on_opencl_fpga_gb300 import QGError
 
-    knobs(0, 8, 4, 1)
+    knobs(3, 8, 4, 1)
     n = 1 << 16
     key = torch.arange(n, dtype=torch.int32, device="cuda")
     out_k = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -189,7 +190,7 @@ def test_groupby_async_key_order(ctx, orc, n, groups, fused):
     check_groups([t[:g] for t in out], orc.groupby_cols(key, val, val2 if fused else None, d["lo2"], d["hi2"]))
 
 
-@pytest.mark.parametrize("mode", [0, 2])
+@pytest.mark.parametrize("mode", [0, 2, 3])
 @pytest.mark.parametrize("hot,parts", [(8, 1), (10, 6), (13, 12), (13, 13)])
 def test_groupby_knob_sweep(ctx, orc, knobs, hot, parts, mode):
     knobs(mode, hot, parts, 0)
@@ -200,16 +201,131 @@ def test_groupby_knob_sweep(ctx, orc, knobs, hot, parts, mode):
 
 
 @pytest.mark.parametrize("cap", [1 << 20, 1 << 21])
-def test_groupby_config1_takes_two_pass_path(ctx, cap):
-    # The full config-1 input must be handled by the two-pass path (no
-    # fallback) with the output capacity the bench passes (the key domain,
-    # 1024 spill partitions) and with twice that (2048 partitions).
+def test_groupby_config1_paths(ctx, knobs, cap):
+    # The full config-1 input (64M rows, Zipf(1.0) over 2^20 keys) stays on the
+    # dense-window path by default (every key inside the sampled window), and
+    # on the two-pass path without a fallback when that path is chosen (mode 3)
+    # with the output capacity the bench passes (the key domain, 1024 spill
+    # partitions) and with twice that (2048 partitions).
     d = datagen.config1_groupby(1 << 26, 1 << 20, seed=0, device="cuda")
+    for v2 in (None, d["val2"]):
+        ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=cap, order=QG_ORDER_NONE)
+        st = ctx.groupby_stats()
+        assert st["path"] == "dense" and st["bucket_cap"] == 0, st
+    knobs(3, 13, 0, 0)
     for v2 in (None, d["val2"]):
         ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=cap, order=QG_ORDER_NONE)
         st = ctx.groupby_stats()
         assert st["path"] == "two_pass" and st["flags"] == 0, st
         assert st["fullest_bucket"] <= st["bucket_cap"], st
+
+
+def test_groupby_config1_headline_calls_repeated(ctx, orc):
+    # The bench's step exactly: group-by then fused filter_aggregation over the
+    # same 64M-row config-1 columns, cap = 2^20 (the key domain), key order,
+    # caller-owned output columns, three steps in a row on one context; every
+    # call bit-exact against the oracle.
+    d = datagen.config1_groupby(1 << 26, 1 << 20, seed=0, device="cuda")
+    key, val, val2 = d["key"].cpu().numpy(), d["val"].cpu().numpy(), d["val2"].cpu().numpy()
+    cap = 1 << 20
+    exp = [orc.groupby_cols(key, val, None, d["lo2"], d["hi2"], cap=1 << 21, mt=True),
+           orc.groupby_cols(key, val, val2, d["lo2"], d["hi2"], cap=1 << 21, mt=True)]
+    outs = [tuple(torch.empty(cap, dtype=t, device="cuda") for t in (torch.int32, torch.int64, torch.int64))
+            for _ in range(2)]
+    for _ in range(3):
+        for i, v2 in enumerate((None, d["val2"])):
+            got = ctx.groupby_cols(d["key"], d["val"], v2, d["lo2"], d["hi2"], cap=cap, order=QG_ORDER_KEY,
+                                   out=outs[i])
+            check_groups(got, exp[i])
+            assert ctx.groupby_stats()["path"] == "dense"
+    ctx.release_out_buffers()
+
+
+def _dense_case(ctx, orc, key, val, val2=None, lo2=0, hi2=0, cap=None, path=None, order=QG_ORDER_KEY):
+    cap = cap or max(1, key.size)
+    got = ctx.groupby_cols(dev(key), dev(val), dev(val2) if val2 is not None else None, lo2, hi2, cap=cap,
+                           order=order)
+    exp = orc.groupby_cols(key, val, val2, lo2, hi2)
+    if order == QG_ORDER_NONE:
+        o = np.argsort(got[0].cpu().numpy().view(np.uint32), kind="stable")
+        got = tuple(t.cpu()[o] for t in got)
+    check_groups(got, exp)
+    if path is not None:
+        assert ctx.groupby_stats()["path"] == path, ctx.groupby_stats()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 4095, 4097, 65537, (1 << 18) + 3, (1 << 18) + 1027])
+def test_groupby_dense_ragged_sizes(ctx, orc, n):
+    # every row sampled (n <= 2^18) or runs spread over the column; tails of
+    # 1-3 rows after the 4-row vectors
+    rng = np.random.default_rng(n)
+    key = (rng.zipf(1.3, n) % 50000).astype(np.int32) + 1000
+    val = rng.integers(0, 1000, n).astype(np.int32)
+    _dense_case(ctx, orc, key, val, path="dense")
+    val2 = rng.integers(0, 1000, n).astype(np.int32)
+    _dense_case(ctx, orc, key, val, val2, -(2 ** 31), 499, path="dense")
+
+
+def test_groupby_dense_wide_and_signed_values(ctx, orc):
+    # values outside [0, fast_max] (negative, INT_MIN/INT_MAX) take the int64
+    # side table, mixed with small ones on the same keys; heavy and light keys
+    rng = np.random.default_rng(5)
+    n = 1 << 20
+    key = np.where(rng.random(n) < 0.5, rng.integers(0, 64, n), rng.integers(0, 1 << 20, n)).astype(np.int32)
+    val = rng.choice(np.array([-(2 ** 31), 2 ** 31 - 1, -1, 0, 5, 2047, 2048, 1 << 30], np.int64), n)
+    val = np.where(rng.random(n) < 0.5, val, rng.integers(0, 1000, n)).astype(np.int32)
+    _dense_case(ctx, orc, key, val, path="dense")
+    _dense_case(ctx, orc, key, val, val, -(2 ** 31), 100, path="dense")
+    # the next call on the same context starts from a clean table
+    _dense_case(ctx, orc, key[: n // 3], rng.integers(0, 1000, n // 3).astype(np.int32), path="dense")
+
+
+@pytest.mark.parametrize("lo", [0, 2 ** 31 - 1000, 2 ** 32 - 3000])
+def test_groupby_dense_window_positions(ctx, orc, lo):
+    # keys from 0 up, across the signed boundary, and at the top of the
+    # unsigned range (the window is clamped to end at 2^32); key order is
+    # ascending unsigned
+    rng = np.random.default_rng(lo & 0xffff)
+    n = 1 << 19
+    key = (lo + rng.integers(0, 3000, n)).astype(np.uint32).view(np.int32)
+    val = rng.integers(-5, 1000, n).astype(np.int32)
+    _dense_case(ctx, orc, key, val, path="dense")
+
+
+def test_groupby_dense_outside_window_falls_back(ctx, orc):
+    # Two rows far from the sampled key range, placed where no sample run
+    # reads them: the dense pass counts them as outside and the call is
+    # answered by the two-pass path, exactly.  Keys spread over more than
+    # 2^21 values get no window at all.
+    rng = np.random.default_rng(6)
+    n = 1 << 22
+    key = rng.integers(100, 100 + 50000, n).astype(np.int32)
+    runs = 1024
+    starts = np.array([(n - 256) * r // (runs - 1) for r in range(runs)])
+    gap = 300  # after run 0 ([0, 256)), before run 1
+    assert not np.any((starts <= gap + 1) & (gap < starts + 256))
+    key[gap], key[gap + 1] = 2 ** 30, -5
+    val = rng.integers(0, 1000, n).astype(np.int32)
+    _dense_case(ctx, orc, key, val, path="two_pass")
+    wide = rng.integers(-(2 ** 31), 2 ** 31, 1 << 18).astype(np.int32)
+    _dense_case(ctx, orc, wide, rng.integers(0, 1000, wide.size).astype(np.int32), path="two_pass")
+    # and the dense path applies again on the next call
+    _dense_case(ctx, orc, key[:gap], val[:gap], path="dense")
+
+
+def test_groupby_dense_capacity_and_unordered(ctx, orc):
+    from query_on_opencl_fpga_gb300 import QGError
+
+    rng = np.random.default_rng(8)
+    n = 1 << 18
+    key = rng.integers(0, 3000, n).astype(np.int32)
+    val = rng.integers(0, 1000, n).astype(np.int32)
+    g = np.unique(key).size
+    with pytest.raises(QGError) as e:
+        ctx.groupby_cols(dev(key), dev(val), cap=g - 1)
+    assert e.value.status == 3
+    _dense_case(ctx, orc, key, val, cap=g, path="dense")
+    _dense_case(ctx, orc, key, val, cap=g, path="dense", order=QG_ORDER_NONE)
 
 
 def test_groupby_cols_into_caller_buffers(ctx, orc):
