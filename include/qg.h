@@ -116,6 +116,17 @@ QG_API qg_status qg_filter_cols_async(qg_ctx *ctx, const int32_t *key, const int
 QG_API qg_status qg_filter_cols_noalloc(const int32_t *key, const int32_t *payload, int64_t n,
                                         int32_t lo, int32_t hi, int32_t *out_pairs, int64_t cap,
                                         int64_t *d_out_n, void *stream);
+/* Companions of qg_filter_cols_noalloc (no counterpart in the reference).
+ * qg_noalloc_set_spin_limit: polls a look-back wait of that filter makes
+ * before it gives up and reports -QG_ERR_TIMEOUT (process-wide; default
+ * 2^22).  qg_noalloc_forget: drops the remembered device addresses of its
+ * array; call it after cudaDeviceReset (or any teardown of a device's primary
+ * context), since the next call must look the address up again.  Note also
+ * that qg_filter_cols_noalloc returns QG_OK when the count exceeds `cap`:
+ * only `cap` pairs are written and *d_out_n holds the full count, so the
+ * caller compares the two. */
+QG_API qg_status qg_noalloc_set_spin_limit(uint32_t polls);
+QG_API qg_status qg_noalloc_forget(void);
 
 /* Column filter kernel choice (process-wide): 0 = one 4096-row tile per CTA
  * held in registers with a decoupled look-back, 1 = persistent CTAs
@@ -325,6 +336,23 @@ QG_API qg_status qg_part_eval(qg_ctx *ctx, const void *d_model, uint32_t kmin, i
 QG_API qg_status qg_hash_join_ref(qg_ctx *ctx, const uint32_t *r_pairs, int64_t nR,
                                   const uint32_t *s_pairs, int64_t nS, uint32_t *out_pairs,
                                   int64_t cap, int64_t *out_n);
+
+/* The same join in its two reference steps, so one build serves many probe
+ * batches.  Replaces buildHashTable (hj_filter_sort_op.cl:25-60), whose caller
+ * allocates the table (rHashTable, rHashCount): the caller allocates
+ * qg_hash_table_bytes(nR) bytes of device memory, 256-byte aligned, and
+ * qg_hash_build_ref fills them from the interleaved (key, val) pairs of R
+ * (synchronous; QG_ERR_CAPACITY if table_bytes is too small).  Replaces
+ * probeHashTable (hj_filter_sort_op.cl:62-109): qg_hash_probe_ref reads the
+ * table (which it does not change, so several probes, also on different
+ * contexts, may read one table) and writes every match as (S.val, R.val),
+ * compacted, order unspecified; *out_n is the match count (QG_ERR_CAPACITY
+ * when above cap).  qg_hash_table_bytes returns -1 for nR outside [0, 2^30). */
+QG_API int64_t qg_hash_table_bytes(int64_t nR);
+QG_API qg_status qg_hash_build_ref(qg_ctx *ctx, const uint32_t *r_pairs, int64_t nR, void *table,
+                                   int64_t table_bytes);
+QG_API qg_status qg_hash_probe_ref(qg_ctx *ctx, const void *table, const uint32_t *s_pairs, int64_t nS,
+                                   uint32_t *out_pairs, int64_t cap, int64_t *out_n);
 
 #ifdef __cplusplus
 }

@@ -52,6 +52,8 @@ SIGNATURES: dict[str, tuple] = {
     "qg_filter_set_variant": (c_int, [c_int]),
     "qg_filter_cols_noalloc": (c_int, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_void_p, c_int64,
                                        c_void_p, c_void_p]),
+    "qg_noalloc_set_spin_limit": (c_int, [c_uint32]),
+    "qg_noalloc_forget": (c_int, []),
     "qg_scan_excl_i32": (c_int, [c_void_p, c_void_p, c_void_p, c_int64]),
     "qg_sort_rec_by_y": (c_int, [c_void_p, c_void_p, c_int64]),
     "qg_groupby_rec": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
@@ -70,6 +72,9 @@ SIGNATURES: dict[str, tuple] = {
     "qg_join_filter_sort": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                     c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64,
                                     POINTER(c_int64)]),
+    "qg_hash_table_bytes": (c_int64, [c_int64]),
+    "qg_hash_build_ref": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64]),
+    "qg_hash_probe_ref": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, POINTER(c_int64)]),
     "qg_hash_join_ref": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64,
                                  POINTER(c_int64)]),
     "qg_join_set_knobs": (c_int, [c_int, c_int, c_uint32, c_uint32]),

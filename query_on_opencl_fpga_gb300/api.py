@@ -353,5 +353,32 @@ class Context:
             self.check(st, "qg_hash_join_ref")
             return out[: m.value]
 
+    def hash_build_ref(self, r_pairs: torch.Tensor) -> torch.Tensor:
+        """Build the reference-layout hash table of R's (key, val) pairs into a
+        new device buffer (qg_hash_table_bytes bytes) and return it."""
+        _check_dev(r_pairs)
+        nR = r_pairs.shape[0]
+        tb = int(self.lib.qg_hash_table_bytes(nR))
+        if tb < 0:
+            raise ValueError("build side too large")
+        table = torch.empty(tb, dtype=torch.uint8, device=r_pairs.device)
+        self.check(self.lib.qg_hash_build_ref(self.handle, _ptr(r_pairs), nR, _ptr(table), tb), "qg_hash_build_ref")
+        return table
+
+    def hash_probe_ref(self, table: torch.Tensor, s_pairs: torch.Tensor, cap: int | None = None):
+        """Probe a table from hash_build_ref: (S.val, R.val) pairs of every match."""
+        _check_dev(table, s_pairs)
+        nS = s_pairs.shape[0]
+        cap = nS if cap is None else cap
+        while True:
+            out = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=s_pairs.device)
+            m = c_int64()
+            st = self.lib.qg_hash_probe_ref(self.handle, _ptr(table), _ptr(s_pairs), nS, _ptr(out), cap, byref(m))
+            if st == QG_ERR_CAPACITY and m.value > cap:
+                cap = m.value
+                continue
+            self.check(st, "qg_hash_probe_ref")
+            return out[: m.value]
+
 
 __all__ = ["Context", "QGError", "QG_ORDER_KEY", "QG_ORDER_NONE", "INT32_MIN", "INT32_MAX"]

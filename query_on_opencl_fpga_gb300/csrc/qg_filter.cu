@@ -83,7 +83,9 @@ k_filter_rec(const uint4 *__restrict__ in, long long n, int32_t lo, int32_t hi,
 }
 
 // Columns: int32 key and payload, four rows per 128-bit load.  Output is the
-// int32 pair (row id, payload).
+// int32 pair (row id, payload).  The tile id is taken from the control
+// block's tile counter (the CTAs' start order), so a tile only ever waits for
+// tiles that are already running.
 template <int ROUNDS>
 __global__ void __launch_bounds__(FT_THREADS, 5)
 k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, long long n,
@@ -92,7 +94,8 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
     constexpr int TILE = FT_THREADS * ROUNDS * 4;
     __shared__ uint32_t s_tile, s_epoch, s_excl;
     __shared__ uint32_t s_woff[ROUNDS * FT_WARPS];
-    const uint32_t tile = blockIdx.x;
+    qg_lb_begin_dyn(lb, &s_tile, &s_epoch);
+    const uint32_t tile = s_tile;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const long long base = (long long)tile * TILE;
     const uint32_t lt = qg_lanemask_lt();
@@ -115,7 +118,6 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
             pv[r] = make_int4(p[0], p[1], p[2], p[3]);
         }
     }
-    qg_lb_begin(lb, &s_tile, &s_epoch);  // epoch read while the loads are in flight
 #pragma unroll
     for (int r = 0; r < ROUNDS; r++) {
         long long idx = base + (long long)(r * FT_THREADS + tid) * 4;
@@ -152,7 +154,7 @@ k_filter_cols(const int32_t *__restrict__ key, const int32_t *__restrict__ pay, 
             }
         }
     }
-    qg_lb_finish(lb, tile, gridDim.x - 1, s_epoch);
+    qg_lb_finish_dyn(lb, tile, gridDim.x - 1, s_epoch);
 }
 
 constexpr int REC_ROUNDS = 8;   // 4096 records per tile
@@ -560,17 +562,35 @@ QG_API qg_status qg_filter_cols(qg_ctx *ctx, const int32_t *key, const int32_t *
 // different threads without ordering) race on it.
 // ---------------------------------------------------------------------------
 #define QG_NOALLOC_MAX_ROWS (1LL << 26)
-#define QG_NOALLOC_MAX_TILES (QG_NOALLOC_MAX_ROWS / 4096)
+#define QG_NOALLOC_TILE (FT_THREADS * COL_ROUNDS * 4)
+#define QG_NOALLOC_MAX_TILES ((QG_NOALLOC_MAX_ROWS + QG_NOALLOC_TILE - 1) / QG_NOALLOC_TILE)
 #define QG_NOALLOC_MAX_DEVICES 64
 
 struct qg_noalloc_scratch {
     qg_control ctl;
     unsigned long long status[QG_NOALLOC_MAX_TILES];
 };
+static_assert((long long)QG_NOALLOC_MAX_TILES * QG_NOALLOC_TILE >= QG_NOALLOC_MAX_ROWS,
+              "no-alloc status words cover the largest accepted input");
 
 static __device__ __align__(256) qg_noalloc_scratch g_noalloc_scratch;
 
+// Device address of g_noalloc_scratch per device, looked up by the first call
+// on that device.  A cudaDeviceReset (or any teardown of the device's primary
+// context) makes the remembered address stale; qg_noalloc_forget() drops it.
 static qg_noalloc_scratch *g_noalloc_addr[QG_NOALLOC_MAX_DEVICES];
+// Polls a look-back wait of the no-alloc filter makes before it gives up.
+static uint32_t g_noalloc_spin = 1u << 22;
+
+extern "C" QG_API qg_status qg_noalloc_set_spin_limit(uint32_t polls) {
+    g_noalloc_spin = polls;
+    return QG_OK;
+}
+
+extern "C" QG_API qg_status qg_noalloc_forget(void) {
+    for (int i = 0; i < QG_NOALLOC_MAX_DEVICES; i++) g_noalloc_addr[i] = nullptr;
+    return QG_OK;
+}
 
 // Reports a device-side error of the call through the count (as -code) and
 // clears the error word for the next call.
@@ -586,9 +606,9 @@ __global__ void k_noalloc_report(qg_noalloc_scratch *s, long long *d_count) {
 extern "C" QG_API qg_status qg_filter_cols_noalloc(const int32_t *key, const int32_t *pay, int64_t n,
                                                    int32_t lo, int32_t hi, int32_t *out,
                                                    int64_t cap, int64_t *d_out_n, void *stream) {
-    constexpr int TILE = FT_THREADS * COL_ROUNDS * 4;
+    constexpr int TILE = QG_NOALLOC_TILE;
     if (n < 0 || cap < 0 || !d_out_n || (n > 0 && (!key || !pay || !out))) return QG_ERR_INVALID;
-    if (n > QG_NOALLOC_MAX_ROWS) return QG_ERR_UNSUPPORTED;
+    if (n > QG_NOALLOC_MAX_ROWS || (n + TILE - 1) / TILE > QG_NOALLOC_MAX_TILES) return QG_ERR_UNSUPPORTED;
     if (((uintptr_t)key & 15) || ((uintptr_t)pay & 15) || ((uintptr_t)out & 7) ||
         ((uintptr_t)d_out_n & 7))
         return QG_ERR_INVALID;
@@ -617,7 +637,7 @@ extern "C" QG_API qg_status qg_filter_cols_noalloc(const int32_t *key, const int
         cudaGetLastError();
         return QG_ERR_CUDA;
     }
-    qg_lookback lb{s->status, &s->ctl, 1u << 22, QG_SITE_FILTER};
+    qg_lookback lb{s->status, &s->ctl, g_noalloc_spin, QG_SITE_FILTER};
     k_filter_cols<COL_ROUNDS><<<(unsigned)tiles, FT_THREADS, 0, st>>>(
         key, pay, n, lo, hi, (int2 *)out, cap, (long long *)d_out_n, lb);
     k_noalloc_report<<<1, 1, 0, st>>>(s, (long long *)d_out_n);

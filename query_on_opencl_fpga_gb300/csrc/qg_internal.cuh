@@ -206,6 +206,20 @@ __device__ __forceinline__ void qg_lb_begin(const qg_lookback &lb, uint32_t *s_t
     __syncthreads();
 }
 
+// Tile id from the control block's tile counter instead of blockIdx.x:
+// tiles are numbered in the order the CTAs start, so every predecessor of a
+// waiting tile is running (or done) whatever order the hardware schedules
+// CTAs in.  Called by all threads at kernel start, before the tile's loads.
+// Pair with qg_lb_finish_dyn.
+__device__ __forceinline__ void qg_lb_begin_dyn(const qg_lookback &lb, uint32_t *s_tile,
+                                                uint32_t *s_epoch) {
+    if (threadIdx.x == 0) {
+        *s_tile = atomicAdd(&lb.ctl->tile_ctr, 1u);
+        *s_epoch = *(volatile uint32_t *)&lb.ctl->epoch;
+    }
+    __syncthreads();
+}
+
 // Called by all threads of warp 0 only.  Publishes the tile aggregate, looks
 // back over predecessors and returns the exclusive prefix of this tile (mod 2^32).
 __device__ __forceinline__ uint32_t qg_lb_warp_exclusive(const qg_lookback &lb, uint32_t tile,
@@ -369,6 +383,16 @@ __device__ __forceinline__ void qg_tile_offsets_wide(uint32_t *s_woff, const qg_
 __device__ __forceinline__ void qg_lb_finish(const qg_lookback &lb, uint32_t tile,
                                              uint32_t last_tile, uint32_t epoch) {
     if (threadIdx.x == 0 && tile == last_tile) *(volatile uint32_t *)&lb.ctl->epoch = epoch + 1u;
+}
+
+// qg_lb_finish for tiles numbered by qg_lb_begin_dyn: the last tile also
+// resets the tile counter (every CTA has taken its tile by then).
+__device__ __forceinline__ void qg_lb_finish_dyn(const qg_lookback &lb, uint32_t tile,
+                                                 uint32_t last_tile, uint32_t epoch) {
+    if (threadIdx.x == 0 && tile == last_tile) {
+        lb.ctl->tile_ctr = 0;
+        *(volatile uint32_t *)&lb.ctl->epoch = epoch + 1u;
+    }
 }
 
 // End of a persistent look-back kernel whose CTAs take tiles from

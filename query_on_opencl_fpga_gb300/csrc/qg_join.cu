@@ -43,6 +43,17 @@ struct JoinCtl {
     uint32_t hist[4][QG_RADIX];
 };
 
+// Reference-layout hash table (qg_hash_build_ref / qg_hash_probe_ref): this
+// header, padded to 256 bytes, then `slots` 8-byte slots (key << 32 | value,
+// EMPTY_SLOT = free).
+struct RefHashHdr {
+    JoinCtl jc;      // key range and the count of build rows equal to EMPTY_SLOT
+    uint32_t slots;  // a power of two
+    uint32_t magic;
+};
+constexpr uint32_t REF_HASH_MAGIC = 0x71684a31u;
+constexpr size_t REF_HASH_HDR = (sizeof(RefHashHdr) + 255) / 256 * 256;
+
 __global__ void k_join_ctl_init(JoinCtl *jc) {
     int t = threadIdx.x;
     if (t == 0) {
@@ -322,12 +333,13 @@ k_join_probe(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay,
 
 // Reference-layout probe: interleaved (key, val) S pairs, output (S.val, R.val).
 __global__ void __launch_bounds__(256)
-k_join_probe_ref(const uint32_t *__restrict__ s, long long nS,
-                 const unsigned long long *__restrict__ tab, uint32_t mask, JoinCtl *jc,
+k_join_probe_ref(const uint32_t *__restrict__ s, long long nS, const unsigned long long *__restrict__ tab,
+                 const RefHashHdr *__restrict__ hdr, unsigned long long *__restrict__ cursor,
                  uint32_t *__restrict__ out, long long cap) {
     const int lane = threadIdx.x & 31;
     const uint32_t lt = qg_lanemask_lt();
-    const unsigned long long nspec = jc->n_special;
+    const unsigned long long nspec = hdr->jc.n_special;
+    const uint32_t mask = hdr->slots - 1;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long iters = (nS + stride - 1) / stride;
     for (long long it = 0; it < iters; it++) {
@@ -360,7 +372,7 @@ k_join_probe_ref(const uint32_t *__restrict__ s, long long nS,
             }
             uint32_t b = __ballot_sync(QG_FULL_MASK, hit);
             unsigned long long base = 0;
-            if (lane == 0 && b) base = atomicAdd(&jc->cursor, (unsigned long long)__popc(b));
+            if (lane == 0 && b) base = atomicAdd(cursor, (unsigned long long)__popc(b));
             base = __shfl_sync(QG_FULL_MASK, base, 0);
             if (hit) {
                 long long g = (long long)base + __popc(b & lt);
@@ -560,6 +572,82 @@ qg_status qg_join_hash_sort_async(qg_ctx *ctx, const int32_t *rkey, const int32_
     return in_b ? QG_ERR_INVALID : QG_OK;  // four passes end where they began
 }
 
+// ---------------------------------------------------------------------------
+// Reference layout: buildHashTable / probeHashTable
+// (kernel/hj_filter_sort/1/hj_filter_sort_op.cl:25-60 and 62-109).  The
+// reference's caller allocates the table (rHashTable, rHashCount) and may
+// probe it with several S tables; here the caller allocates
+// qg_hash_table_bytes(nR) bytes, qg_hash_build_ref fills them, and any number
+// of qg_hash_probe_ref calls read them.
+// ---------------------------------------------------------------------------
+static uint32_t ref_table_slots(long long nR) {
+    uint64_t c = 1024;
+    while (c < (uint64_t)nR * 2) c <<= 1;
+    return (uint32_t)c;
+}
+
+namespace {
+__global__ void k_ref_hash_hdr_init(RefHashHdr *hdr, uint32_t slots) {
+    if (threadIdx.x == 0) {
+        hdr->slots = slots;
+        hdr->magic = REF_HASH_MAGIC;
+    }
+}
+}  // namespace
+
+extern "C" QG_API int64_t qg_hash_table_bytes(int64_t nR) {
+    if (nR < 0 || nR >= (1LL << 30)) return -1;
+    return (int64_t)(REF_HASH_HDR + (size_t)ref_table_slots(nR) * 8);
+}
+
+extern "C" QG_API qg_status qg_hash_build_ref(qg_ctx *ctx, const uint32_t *r, int64_t nR, void *table,
+                                              int64_t table_bytes) {
+    if (!ctx || nR < 0 || !table || (nR > 0 && !r)) return QG_ERR_INVALID;
+    if ((((uintptr_t)r) & 7) || (((uintptr_t)table) & 255)) return QG_ERR_INVALID;
+    if (nR >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
+    if (table_bytes < qg_hash_table_bytes(nR)) return QG_ERR_CAPACITY;
+    const uint32_t slots = ref_table_slots(nR);
+    RefHashHdr *hdr = (RefHashHdr *)table;
+    unsigned long long *tab = (unsigned long long *)((char *)table + REF_HASH_HDR);
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(tab, 0xff, (size_t)slots * 8, ctx->stream), "memset table");
+    qg_pre_launch(ctx);
+    k_join_ctl_init<<<1, 256, 0, ctx->stream>>>(&hdr->jc);
+    QG_TRY(qg_check_launch(ctx, "k_join_ctl_init"));
+    qg_pre_launch(ctx);
+    k_ref_hash_hdr_init<<<1, 32, 0, ctx->stream>>>(hdr, slots);
+    QG_TRY(qg_check_launch(ctx, "k_ref_hash_hdr_init"));
+    if (nR > 0) {
+        int blocks = grid_cap(ctx, nR, 256, 8);
+        qg_pre_launch(ctx);
+        k_join_build<<<blocks, 256, 0, ctx->stream>>>((const int32_t *)r, (const int32_t *)r + 1, 2, nR, tab,
+                                                      slots - 1, &hdr->jc, ctx->ctl);
+        QG_TRY(qg_check_launch(ctx, "k_join_build"));
+    }
+    // a table that fills up (cannot happen at 2 slots per row) reports TABLE_FULL
+    return qg_ctx_check(ctx);
+}
+
+extern "C" QG_API qg_status qg_hash_probe_ref(qg_ctx *ctx, const void *table, const uint32_t *s, int64_t nS,
+                                              uint32_t *out, int64_t cap, int64_t *out_n) {
+    if (!ctx || !table || nS < 0 || cap < 0 || !out_n) return QG_ERR_INVALID;
+    if ((nS > 0 && !s) || (cap > 0 && !out)) return QG_ERR_INVALID;
+    if ((((uintptr_t)s) | ((uintptr_t)out)) & 7 || (((uintptr_t)table) & 255)) return QG_ERR_INVALID;
+    *out_n = 0;
+    if (nS == 0) return QG_OK;
+    const RefHashHdr *hdr = (const RefHashHdr *)table;
+    const unsigned long long *tab = (const unsigned long long *)((const char *)table + REF_HASH_HDR);
+    unsigned long long *cursor = &ctx->ctl->counter[0];
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(cursor, 0, 8, ctx->stream), "memset cursor");
+    int blocks = grid_cap(ctx, nS, 256, 8);
+    qg_pre_launch(ctx);
+    k_join_probe_ref<<<blocks, 256, 0, ctx->stream>>>(s, nS, tab, hdr, cursor, out, cap);
+    QG_TRY(qg_check_launch(ctx, "k_join_probe_ref"));
+    long long m = 0;
+    QG_TRY(qg_read_count(ctx, (const long long *)cursor, &m));
+    *out_n = m;
+    return m > cap ? QG_ERR_CAPACITY : QG_OK;
+}
+
 extern "C" QG_API qg_status qg_hash_join_ref(qg_ctx *ctx, const uint32_t *r, int64_t nR,
                                              const uint32_t *s, int64_t nS, uint32_t *out,
                                              int64_t cap, int64_t *out_n) {
@@ -568,18 +656,10 @@ extern "C" QG_API qg_status qg_hash_join_ref(qg_ctx *ctx, const uint32_t *r, int
     if ((((uintptr_t)r) | ((uintptr_t)s) | ((uintptr_t)out)) & 7) return QG_ERR_INVALID;
     *out_n = 0;
     if (nR == 0 || nS == 0) return QG_OK;
-    unsigned long long *tab;
-    uint32_t mask;
-    JoinCtl *jc;
-    char *tail;
-    QG_TRY(join_build(ctx, (const int32_t *)r, (const int32_t *)r + 1, 2, nR, 0, &tab, &mask, &jc,
-                      &tail));
-    int blocks = grid_cap(ctx, nS, 256, 8);
-    qg_pre_launch(ctx);
-    k_join_probe_ref<<<blocks, 256, 0, ctx->stream>>>(s, nS, tab, mask, jc, out, cap);
-    QG_TRY(qg_check_launch(ctx, "k_join_probe_ref"));
-    long long m = 0;
-    QG_TRY(qg_read_count(ctx, (const long long *)&jc->cursor, &m));
-    *out_n = m;
-    return m > cap ? QG_ERR_CAPACITY : QG_OK;
+    const int64_t tb = qg_hash_table_bytes(nR);
+    if (tb < 0) return QG_ERR_UNSUPPORTED;
+    char *aux;
+    QG_TRY(qg_aux(ctx, (size_t)tb, &aux));  // the aux arena is 256-byte aligned
+    QG_TRY(qg_hash_build_ref(ctx, r, nR, aux, tb));
+    return qg_hash_probe_ref(ctx, aux, s, nS, out, cap, out_n);
 }

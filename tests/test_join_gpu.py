@@ -105,3 +105,28 @@ def test_hash_join_ref(ctx, orc, nR, nS, keyspace):
     got = ctx.hash_join_ref(dev(r), dev(s)).cpu().numpy()
     exp = orc.hash_join_ref(r, s, cap=nS * 8)
     assert np.array_equal(np.sort(got.view(np.int64).ravel()), np.sort(exp.view(np.int64).ravel()))
+
+
+def test_hash_build_once_probe_three_batches(ctx, orc):
+    # buildHashTable once, probeHashTable with three S batches (as the
+    # reference's split kernels allow); each batch equals the oracle's join,
+    # including duplicate build keys and the all-ones (key -1, val -1) row.
+    rng = np.random.default_rng(77)
+    nR = 50000
+    r = np.stack([rng.integers(0, 30000, nR), rng.integers(0, 1 << 30, nR)], 1).astype(np.int32)
+    r[5] = (-1, -1)
+    table = ctx.hash_build_ref(dev(r))
+    assert table.numel() == ctx.lib.qg_hash_table_bytes(nR)
+    for b, nS in enumerate((1, 70001, 1 << 18)):
+        s = np.stack([rng.integers(-10, 33000, nS), rng.integers(0, 1 << 30, nS)], 1).astype(np.int32)
+        if nS > 10:
+            s[7, 0] = -1
+        got = ctx.hash_probe_ref(table, dev(s)).cpu().numpy()
+        exp = orc.hash_join_ref(r, s, cap=nS * 8)
+        assert np.array_equal(np.sort(got.view(np.int64).ravel()), np.sort(exp.view(np.int64).ravel())), b
+    # a table buffer smaller than qg_hash_table_bytes is refused
+    from ctypes import c_void_p
+
+    st = ctx.lib.qg_hash_build_ref(ctx.handle, c_void_p(dev(r).data_ptr()), nR, c_void_p(table.data_ptr()),
+                                   table.numel() - 8)
+    assert st == 3
