@@ -11,18 +11,18 @@
 //
 // Four launches, no host round trip until the caller's one read at the end:
 //  1. k_gbd_sample -- 2^18 keys (1024 runs of 256 consecutive rows spread over
-//                     the column, or every row of a smaller input) are counted,
-//                     per CTA in shared memory first, then in an L2 open-
-//                     addressing table; their smallest and largest key are
-//                     recorded.
-//  2. k_gbd_cands  -- every sampled key seen at least twice (every key when the
-//                     whole input was sampled) bids for the heavy-key slot its
-//                     hash selects with one 64-bit atomicMax of
-//                     (sample count << 32 | key): each of the 16384 slots ends
-//                     up holding its most frequent candidate.  The counting
-//                     table is cleared.  The key window [kbase, kbase + 2^22)
-//                     is centred on the sample's key range (no window when
-//                     that range spans more than 2^21 keys).
+//                     the column, or every row of a smaller input) are counted
+//                     per CTA in shared memory; each CTA adds its distinct
+//                     keys' counts to a two-row count-min sketch in L2 (fire-
+//                     and-forget reductions) and lists the keys.  The
+//                     smallest and largest sampled key are recorded.
+//  2. k_gbd_cands  -- every listed key whose sketch count is at least 2 (at
+//                     least 1 when the whole input was sampled) bids for the
+//                     heavy-key slot its hash selects with one 64-bit atomicMax
+//                     of (count << 32 | key): each of the 16384 slots ends up
+//                     holding its most frequent candidate.  The key window
+//                     [kbase, kbase + 2^22) is centred on the sample's key range
+//                     (no window when that range spans more than 2^21 keys).
 //  3. k_gbd_main   -- one 1024-thread CTA per SM over a contiguous slice.  The
 //                     slot image becomes a read-only direct-mapped table of
 //                     window offsets in shared memory, so a row's lookup is one
@@ -34,9 +34,10 @@
 //                     end the shared table is added to the dense table.
 //  4. k_gbd_emit   -- the touched index range of the dense table is read in
 //                     order, every non-empty entry becomes a group, and the
-//                     entries (and the slot image) are cleared.  Output
+//                     entries (and the slot image and sketch) are cleared.  Output
 //                     positions come from a decoupled look-back over 4096-entry
-//                     tiles; within a tile the writes are contiguous across
+//                     tiles (all warps of a tile read 256 predecessors per
+//                     round); within a tile the writes are contiguous across
 //                     each warp.
 //
 // The shared-memory pipeline (L1TEX) bounds the main pass: a row costs about
@@ -64,16 +65,15 @@ constexpr int GBD_WLOG2 = 22;
 constexpr uint32_t GBD_W = 1u << GBD_WLOG2;       // window keys (dense table entries)
 constexpr int GBD_SLOG2 = 14;
 constexpr int GBD_S = 1 << GBD_SLOG2;             // heavy-key slots (direct-mapped)
-constexpr int GBD_TLOG2 = 19;                     // sample counting table slots
+constexpr int GBD_TLOG2 = 19;                     // counters per row of the sample's count sketch
 constexpr uint32_t GBD_TMASK = (1u << GBD_TLOG2) - 1;
 constexpr int GBD_SAMPLE_RUNS = 1024;
 constexpr int GBD_RUN = 256;                      // consecutive rows per sample run
 constexpr int GBD_SAMPLE_CTAS = 256;              // runs b, b + 256, ... : at most 4 per CTA
 constexpr int GBD_RUNS_PER_CTA = GBD_SAMPLE_RUNS / GBD_SAMPLE_CTAS;
 constexpr int GBD_SSLOTS = 2048;                  // per-CTA sample table (<= 1024 keys)
+constexpr int GBD_LIST = GBD_RUNS_PER_CTA * GBD_RUN;  // distinct keys a sample CTA lists (at most)
 constexpr int GBD_CANDS_THREADS = 256;
-constexpr int GBD_CANDS_PER = 8;
-constexpr int GBD_CANDS_CTAS = (1 << GBD_TLOG2) / (GBD_CANDS_THREADS * GBD_CANDS_PER);
 constexpr int GBD_THREADS = 1024;
 constexpr int GBD_EMIT_THREADS = 256;
 constexpr int GBD_EMIT_PER = 16;                  // entries per emit thread
@@ -95,7 +95,8 @@ enum {
 };
 static_assert(G_WORDS <= 48, "gbd state words");
 static_assert(GBD_RUNS_PER_CTA * GBD_RUN * 2 <= GBD_SSLOTS, "sample table load <= 1/2");
-static_assert(GBD_CANDS_CTAS * GBD_CANDS_THREADS * GBD_CANDS_PER == (1 << GBD_TLOG2), "cands cover the table");
+static_assert(GBD_LIST % GBD_CANDS_THREADS == 0, "cands: whole list per CTA");
+static_assert(2 * (1 << GBD_TLOG2) % (GBD_EMIT_TILES * GBD_EMIT_THREADS * 4) == 0, "emit clears the sketch");
 static_assert(GBD_EMIT_PER * (GBD_EMIT_THREADS / 32) % 32 == 0, "emit cells per lane");
 static_assert(GBD_S % (16 * GBD_EMIT_THREADS) == 0, "emit clears the slot image in 16 tiles");
 
@@ -109,31 +110,32 @@ __device__ __forceinline__ void red_shared_u32(uint32_t *p, uint32_t v) {
     asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(qg_smem_u32(p)), "r"(v) : "memory");
 }
 
-// Count c more sightings of key k in the L2 table (entry key << 32 | count,
-// 0 = empty; load <= 1/2 with at most 2^18 distinct keys in 2^19 slots, so a
-// free or matching slot is always found).
-__device__ __forceinline__ void gbd_count_l2(unsigned long long *ct, uint32_t k, unsigned long long c) {
-    uint32_t h = qg_hash32(k) & GBD_TMASK;
-    for (uint32_t p = 0; p <= GBD_TMASK; p++, h = (h + 1) & GBD_TMASK) {
-        const unsigned long long old = atomicCAS(ct + h, 0ull, ((unsigned long long)k << 32) | c);
-        if (old == 0ull) return;
-        if ((uint32_t)(old >> 32) == k) {
-            atomicAdd(ct + h, c);
-            return;
-        }
-    }
-}
+// The two rows of the sample's count-min sketch: a key's count is the smaller
+// of its two counters, never below its true count.
+__device__ __forceinline__ uint32_t gbd_h1(uint32_t k) { return qg_hash32(k) & GBD_TMASK; }
+__device__ __forceinline__ uint32_t gbd_h2(uint32_t k) { return qg_hash32(k * 0x85EBCA77u + 0x27D4EB2Fu) & GBD_TMASK; }
 
 // 1. Sample.  Run r covers rows [start_r, start_r + 256); CTA b takes runs
 // b, b + 256, b + 512, b + 768.  Each thread loads its (up to) four keys
-// first, the CTA counts them in shared memory, and each distinct key's count
-// goes to the L2 table once: a heavy key costs one global atomic per CTA
-// instead of one per sampled row.
+// first, and the CTA counts them in a shared-memory table of 32-bit keys and
+// counts (64-bit shared atomics are several times slower).  Each distinct
+// key then adds its count to both rows of an L2 count sketch with
+// fire-and-forget reductions (no compare-and-swap round trips) and is listed
+// in the CTA's segment of `lst`.  The sketch only ranks candidates for the
+// heavy-key table, which decides where a row is added, never what it adds,
+// so a counter shared by two keys costs speed at most.  Key 0xffffffff is the
+// shared table's empty mark and is never a candidate (its rows take the dense
+// table like any other key's).
 __global__ void __launch_bounds__(GBD_RUN)
 k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_row,
-             unsigned long long *__restrict__ ct, uint32_t *__restrict__ st) {
-    __shared__ unsigned long long t[GBD_SSLOTS];  // key << 32 | count, 0 = empty
-    for (int i = threadIdx.x; i < GBD_SSLOTS; i += GBD_RUN) t[i] = 0ull;
+             uint32_t *__restrict__ sketch, uint32_t *__restrict__ lst, uint32_t *__restrict__ lcnt,
+             uint32_t *__restrict__ st) {
+    __shared__ uint32_t tkey[GBD_SSLOTS], tcnt[GBD_SSLOTS], s_n;
+    for (int i = threadIdx.x; i < GBD_SSLOTS; i += GBD_RUN) {
+        tkey[i] = GBD_EMPTY;
+        tcnt[i] = 0;
+    }
+    if (threadIdx.x == 0) s_n = 0;
     uint32_t k[GBD_RUNS_PER_CTA];
     bool have[GBD_RUNS_PER_CTA];
 #pragma unroll
@@ -151,21 +153,26 @@ k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_
         if (!have[j]) continue;
         lmin = min(lmin, k[j]);
         lmax = max(lmax, k[j]);
+        if (k[j] == GBD_EMPTY) continue;
         // load <= 1/2 (at most 1024 keys), so a free or matching slot exists
         uint32_t h = qg_hash32(k[j]) & (GBD_SSLOTS - 1);
         for (int p = 0; p < GBD_SSLOTS; p++, h = (h + 1) & (GBD_SSLOTS - 1)) {
-            const unsigned long long old = atomicCAS(&t[h], 0ull, ((unsigned long long)k[j] << 32) | 1ull);
-            if (old == 0ull) break;
-            if ((uint32_t)(old >> 32) == k[j]) {
-                atomicAdd(&t[h], 1ull);
+            const uint32_t old = atomicCAS(&tkey[h], GBD_EMPTY, k[j]);
+            if (old == GBD_EMPTY || old == k[j]) {
+                atomicAdd(&tcnt[h], 1u);
                 break;
             }
         }
     }
     __syncthreads();
-    for (int s = threadIdx.x; s < GBD_SSLOTS; s += GBD_RUN) {
-        const unsigned long long e = t[s];
-        if (e) gbd_count_l2(ct, (uint32_t)(e >> 32), e & 0xffffffffull);
+    uint32_t *mine = lst + (size_t)blockIdx.x * GBD_LIST;
+    for (int sl = threadIdx.x; sl < GBD_SSLOTS; sl += GBD_RUN) {
+        const uint32_t c = tcnt[sl];
+        if (!c) continue;
+        const uint32_t kk = tkey[sl];
+        atomicAdd(sketch + gbd_h1(kk), c);  // result unused: compiled as a reduction
+        atomicAdd(sketch + (1u << GBD_TLOG2) + gbd_h2(kk), c);
+        mine[atomicAdd(&s_n, 1u)] = kk;
     }
     lmin = __reduce_min_sync(QG_FULL_MASK, lmin);
     lmax = __reduce_max_sync(QG_FULL_MASK, lmax);
@@ -173,25 +180,30 @@ k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_
         atomicMax(&st[G_NSMIN], ~lmin);
         atomicMax(&st[G_SMAX], lmax);
     }
+    __syncthreads();
+    if (threadIdx.x == 0) lcnt[blockIdx.x] = s_n;
 }
 
-// 2. Candidates bid for their slots; the window.  Block b owns counting-table
-// slots [b*2048, (b+1)*2048).
+// 2. Candidates bid for their slots; the window.  CTA b reads sample CTA b's
+// list.  A key listed by several sample CTAs bids several times with the
+// same word, which atomicMax makes harmless.
 __global__ void __launch_bounds__(GBD_CANDS_THREADS)
-k_gbd_cands(unsigned long long *__restrict__ ct, unsigned long long *__restrict__ img, uint32_t min_count,
+k_gbd_cands(const uint32_t *__restrict__ sketch, const uint32_t *__restrict__ lst,
+            const uint32_t *__restrict__ lcnt, unsigned long long *__restrict__ img, uint32_t min_count,
             uint32_t *__restrict__ st) {
-    const uint32_t base = blockIdx.x * (GBD_CANDS_THREADS * GBD_CANDS_PER);
-    unsigned long long e[GBD_CANDS_PER];
+    const uint32_t m = lcnt[blockIdx.x];
+    const uint32_t *mine = lst + (size_t)blockIdx.x * GBD_LIST;
+    constexpr int PER = GBD_LIST / GBD_CANDS_THREADS;
+    uint32_t kk[PER], c[PER];
 #pragma unroll
-    for (int j = 0; j < GBD_CANDS_PER; j++) e[j] = ct[base + j * GBD_CANDS_THREADS + threadIdx.x];
-#pragma unroll
-    for (int j = 0; j < GBD_CANDS_PER; j++) {
-        if (!e[j]) continue;
-        ct[base + j * GBD_CANDS_THREADS + threadIdx.x] = 0ull;
-        const uint32_t c = (uint32_t)e[j], k = (uint32_t)(e[j] >> 32);
-        // the image word orders candidates by count, ties by key
-        if (c >= min_count) atomicMax(img + gbd_slot(k), ((unsigned long long)c << 32) | k);
+    for (int j = 0; j < PER; j++) {  // all lookups in flight before any bid
+        const uint32_t i = j * GBD_CANDS_THREADS + threadIdx.x;
+        kk[j] = i < m ? mine[i] : 0u;
+        c[j] = i < m ? min(sketch[gbd_h1(kk[j])], sketch[(1u << GBD_TLOG2) + gbd_h2(kk[j])]) : 0u;
     }
+#pragma unroll
+    for (int j = 0; j < PER; j++)  // the image word orders candidates by count, ties by key
+        if (c[j] >= min_count && c[j] > 0) atomicMax(img + gbd_slot(kk[j]), ((unsigned long long)c[j] << 32) | kk[j]);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const uint32_t smin = ~st[G_NSMIN], smax = st[G_SMAX];
         if (smin <= smax) {
@@ -328,14 +340,15 @@ k_gbd_main(const int32_t *__restrict__ key, const int32_t *__restrict__ val, con
 // tile, so the loads, the cleared entries and (after a per-round rank) the
 // groups written are contiguous across a warp.  Tiles past the touched range
 // leave at once; the last touched tile publishes the group count.  Tiles 0-15
-// also clear the slot image.
+// also clear the slot image, and every tile a share of the sample's sketch.
 __global__ void __launch_bounds__(GBD_EMIT_THREADS)
 k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra,
-           unsigned long long *__restrict__ img, const uint32_t *__restrict__ st, uint32_t shift,
+           unsigned long long *__restrict__ img, uint4 *__restrict__ sketch, const uint32_t *__restrict__ st,
+           uint32_t shift,
            int32_t *__restrict__ gkey, long long *__restrict__ gsum, long long *__restrict__ gcnt, long long cap,
            long long *__restrict__ d_num, qg_lookback lb) {
     constexpr int NW = GBD_EMIT_THREADS / 32;
-    __shared__ uint32_t s_tile, s_epoch, s_excl, s_off[GBD_EMIT_PER * NW];
+    __shared__ uint32_t s_tile, s_epoch, s_total, s_off[GBD_EMIT_PER * NW], s_tmp[2 * NW];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) {
         s_tile = atomicAdd(&lb.ctl->tile_ctr, 1u);
@@ -346,6 +359,10 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
     if (tile < 16) {
         constexpr int PER_TILE = GBD_S / 16;
         for (int i = tid; i < PER_TILE; i += GBD_EMIT_THREADS) img[tile * PER_TILE + i] = 0ull;
+    }
+    {  // every tile clears its share of the sample's count sketch
+        constexpr int PER_TILE = 2 * (1 << GBD_TLOG2) / 4 / GBD_EMIT_TILES;  // uint4 words
+        for (int i = tid; i < PER_TILE; i += GBD_EMIT_THREADS) sketch[(size_t)tile * PER_TILE + i] = make_uint4(0, 0, 0, 0);
     }
     const uint32_t umin = ~st[G_NUMIN], hi = st[G_UMAX];
     const bool any = st[G_OK] && umin <= hi;
@@ -368,8 +385,7 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
         if (lane == 0) s_off[r * NW + warp] = __popc(m);
     }
     __syncthreads();
-    // exclusive offsets of the (round, warp) cells in round-major order; warp 0
-    // then looks back for the tile's place
+    // exclusive offsets of the (round, warp) cells in round-major order
     if (warp == 0) {
         constexpr int CPL = GBD_EMIT_PER * NW / 32;  // cells per lane
         uint32_t c[CPL], sum = 0;
@@ -391,14 +407,14 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
             s_off[lane * CPL + k] = run;
             run += c[k];
         }
-        const uint32_t excl = qg_lb_warp_exclusive(lb, tile, epoch, total);
-        if (lane == 0) {
-            s_excl = excl;
-            if (tile == last) *d_num = (long long)excl + total;
-        }
+        if (lane == 0) s_total = total;
     }
     __syncthreads();
-    const long long tile_off = s_excl;
+    // the tile's place: all warps look back, 256 predecessors per round
+    const uint32_t total = s_total;
+    const uint32_t excl = qg_lb_wide_exclusive<NW>(lb, tile, epoch, total, s_tmp);
+    if (tid == 0 && tile == last) *d_num = (long long)excl + total;
+    const long long tile_off = excl;
 #pragma unroll
     for (int r = 0; r < GBD_EMIT_PER; r++) {
         const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
@@ -426,14 +442,19 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
                         int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt, int64_t cap,
                         long long *d_num) {
     // table arena (kept all-zero between calls):
-    //   dense [W] u64 | extra [W] i64 | sample counts [2^19] u64 | slot image [GBD_S] u64
-    const size_t dense_b = (size_t)GBD_W * 8, ct_b = ((size_t)1 << GBD_TLOG2) * 8, img_b = (size_t)GBD_S * 8;
+    //   dense [W] u64 | extra [W] i64 | sample sketch [2][2^19] u32 | slot image [GBD_S] u64
+    const size_t dense_b = (size_t)GBD_W * 8, sk_b = ((size_t)2 << GBD_TLOG2) * 4, img_b = (size_t)GBD_S * 8;
     char *tab;
-    QG_TRY(qg_table(ctx, 2 * dense_b + ct_b + img_b, &tab));
+    QG_TRY(qg_table(ctx, 2 * dense_b + sk_b + img_b, &tab));
     unsigned long long *dense = (unsigned long long *)tab;
     long long *extra = (long long *)(tab + dense_b);
-    unsigned long long *ct = (unsigned long long *)(tab + 2 * dense_b);
-    unsigned long long *img = (unsigned long long *)(tab + 2 * dense_b + ct_b);
+    uint32_t *sketch = (uint32_t *)(tab + 2 * dense_b);
+    unsigned long long *img = (unsigned long long *)(tab + 2 * dense_b + sk_b);
+    // scratch: the sample CTAs' key lists [GBD_SAMPLE_CTAS][GBD_LIST] | their lengths
+    const size_t lst_b = (size_t)GBD_SAMPLE_CTAS * GBD_LIST * 4;
+    char *scr;
+    QG_TRY(qg_scratch(ctx, lst_b + GBD_SAMPLE_CTAS * 4, &scr));
+    uint32_t *lst = (uint32_t *)scr, *lcnt = (uint32_t *)(scr + lst_b);
     qg_lookback lb;
     QG_TRY(qg_lb_make(ctx, GBD_EMIT_TILES, QG_SITE_GROUPBY, &lb));
     uint32_t *st = ctx->ctl->gbd;
@@ -462,14 +483,13 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
     const bool every_row = n <= (long long)GBD_SAMPLE_RUNS * GBD_RUN;
     const int runs = every_row ? (int)qg_ceil_div(n, GBD_RUN) : GBD_SAMPLE_RUNS;
     qg_status s = QG_OK;
-    if (runs > 0) {
-        qg_pre_launch(ctx);
-        k_gbd_sample<<<GBD_SAMPLE_CTAS, GBD_RUN, 0, ctx->stream>>>(key, n, runs, every_row, ct, st);
-        s = qg_check_launch(ctx, "k_gbd_sample");
-    }
+    qg_pre_launch(ctx);  // with runs == 0 (n == 0) every CTA lists nothing
+    k_gbd_sample<<<GBD_SAMPLE_CTAS, GBD_RUN, 0, ctx->stream>>>(key, n, runs, every_row, sketch, lst, lcnt, st);
+    s = qg_check_launch(ctx, "k_gbd_sample");
     if (s == QG_OK) {
         qg_pre_launch(ctx);
-        k_gbd_cands<<<GBD_CANDS_CTAS, GBD_CANDS_THREADS, 0, ctx->stream>>>(ct, img, every_row ? 1u : 2u, st);
+        k_gbd_cands<<<GBD_SAMPLE_CTAS, GBD_CANDS_THREADS, 0, ctx->stream>>>(sketch, lst, lcnt, img,
+                                                                            every_row ? 1u : 2u, st);
         s = qg_check_launch(ctx, "k_gbd_cands");
     }
     if (s == QG_OK && n > 0) {
@@ -481,7 +501,8 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
     if (s == QG_OK) {
         qg_pre_launch(ctx);
         k_gbd_emit<<<GBD_EMIT_TILES, GBD_EMIT_THREADS, 0, ctx->stream>>>(
-            dense, extra, img, st, shift, gkey, (long long *)gsum, (long long *)gcnt, cap, d_num, lb);
+            dense, extra, img, (uint4 *)sketch, st, shift, gkey, (long long *)gsum, (long long *)gcnt, cap, d_num,
+            lb);
         s = qg_check_launch(ctx, "k_gbd_emit");
     }
     if (s != QG_OK) ctx->table_dirty = true;  // the dense table may hold partial sums
