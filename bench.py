@@ -14,7 +14,8 @@ and results copied out every step.  Per-operator lines for the filter
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
 With --impl reference the CPU restatement of the reference operators runs on
-the host cores (all threads) on a bounded sample of the same workload.
+the host cores (all threads) over the same full step when the requested steps
+fit in about five minutes (a bounded sample of it otherwise).
 """
 from __future__ import annotations
 
@@ -139,7 +140,18 @@ def max_over_ranks(x, world):
 # ---------------------------------------------------------------------------
 # reference arm: the CPU restatement of the reference operators on host cores
 # ---------------------------------------------------------------------------
+def cpu_groupby_step(key, val, val2):
+    """One config-1 step (group-by + fused filter_aggregation) of the oracle port
+    of the reference operators on all host threads."""
+    from oracle import oracle as orc
+
+    orc.groupby_cols(key, val, None, -(2 ** 31), 499, cap=GROUPS * 2, mt=True)
+    orc.groupby_cols(key, val, val2, -(2 ** 31), 499, cap=GROUPS * 2, mt=True)
+
+
 def run_reference(args, rank, world):
+    """The full config-1 step (2 x 64M rows) when the requested steps fit in about
+    5 minutes at the rate of a first (warm-up) step, else a sample sized to fit."""
     if rank != 0:
         return
     import numpy as np
@@ -149,31 +161,37 @@ def run_reference(args, rank, world):
 
     orc.lib()
     threads = orc.threads()
-    sample = 1 << 23  # 8M rows per operator per step keeps a 13-step run to about a minute
-    d = datagen.config1_groupby(sample, GROUPS, seed=0)
+    d = datagen.config1_groupby(N_ROWS, GROUPS, seed=0)
     key, val, val2 = d["key"].numpy(), d["val"].numpy(), d["val2"].numpy()
-
-    def step():
-        orc.groupby_cols(key, val, None, d["lo2"], d["hi2"], cap=GROUPS * 2, mt=True)
-        orc.groupby_cols(key, val, val2, d["lo2"], d["hi2"], cap=GROUPS * 2, mt=True)
-
-    for _ in range(args.warmup):
-        step()
+    t0 = time.perf_counter()
+    cpu_groupby_step(key, val, val2)  # first warm-up step, also the rate estimate
+    t_full = time.perf_counter() - t0
+    budget_s = 300.0
+    sample = N_ROWS
+    while sample > (1 << 20) and t_full * sample / N_ROWS * (args.steps + args.warmup) > budget_s:
+        sample //= 2
+    if sample < N_ROWS:
+        key, val, val2 = (np.ascontiguousarray(x[:sample]) for x in (key, val, val2))
+    for _ in range(args.warmup - 1 if sample == N_ROWS else args.warmup):
+        cpu_groupby_step(key, val, val2)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        step()
+        cpu_groupby_step(key, val, val2)
     dt = (time.perf_counter() - t0) / args.steps
     value = 2 * sample / dt
+    full = sample == N_ROWS
+    wl = ("config1: groupby SUM(int64)+COUNT and fused filter_aggregation (value2<500), 64M rows, "
+          "key Zipf(1.0) over 1M groups, output in key order")
     line = {
         "impl": "reference", "metric": "rows_per_s", "value": value, "unit": "rows/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/int64",
-        "data": "synthetic (seeded; Zipf(1.0) keys over 1M groups, uniform values)",
-        "config": {"workload": "config1 groupby SUM+COUNT + fused filter_aggregation (value2<500), "
-                               "Zipf(1.0) 1M groups; bounded sample of 8M rows per operator per step",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32 in, int64 SUM/COUNT",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl if full else wl + f"; first {sample} rows per operator per step",
                    "rows_per_step": 2 * sample},
         "cpu_baseline": {"value": value, "unit": "rows/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} rows x 2 operators per step (the 64M-row batch, sampled)"},
+                         "sample": "the full step (2 x 64M rows)" if full else
+                         f"{sample} rows x 2 operators per step (the 64M-row batch, sampled to fit the run)"},
         "e2e": {"value": value, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference OpenCL CPU runtime unavailable on this box; oracle port of the reference "
                 "operators (oracle/qg_oracle.c, OpenMP) on all host threads",
@@ -230,25 +248,46 @@ def roofline(kern, name, bytes_per_launch, peak_gbs, traffic=None):
             "algorithmic_bytes_per_launch": bytes_per_launch}
 
 
-def cpu_baseline_groupby(d_host, sample):
+def cpu_baseline_groupby(d_host):
+    """The oracle port on all host threads over the full headline step (the same
+    work as the reference arm): one warm-up step, then two timed steps."""
     import numpy as np
 
     from oracle import oracle as orc
 
     orc.lib()
-    key, val, val2 = (d_host["key"][:sample], d_host["val"][:sample], d_host["val2"][:sample])
-    key, val, val2 = [np.ascontiguousarray(x) for x in (key, val, val2)]
+    key, val, val2 = (np.ascontiguousarray(d_host[k]) for k in ("key", "val", "val2"))
+    cpu_groupby_step(key, val, val2)
+    reps = 2
     t0 = time.perf_counter()
-    reps = 0
-    while True:
-        orc.groupby_cols(key, val, None, -(2 ** 31), 499, cap=GROUPS * 2, mt=True)
-        orc.groupby_cols(key, val, val2, -(2 ** 31), 499, cap=GROUPS * 2, mt=True)
-        reps += 1
-        if time.perf_counter() - t0 > 8.0 or reps >= 5:
-            break
+    for _ in range(reps):
+        cpu_groupby_step(key, val, val2)
     dt = (time.perf_counter() - t0) / reps
-    return {"value": 2 * sample / dt, "unit": "rows/s", "cores": orc.threads(), "kind": "port",
-            "sample": f"first {sample} rows of the batch, both operators, {reps} reps"}
+    return {"value": 2 * key.size / dt, "unit": "rows/s", "cores": orc.threads(), "kind": "port",
+            "sample": f"the full step ({key.size} rows x 2 operators), 1 warm-up + {reps} timed steps"}
+
+
+def pinned_copy_rates(hkey, hval, hval2, dev, copy_streams, reps=5):
+    """The link's plain host-to-device rate for the step's three input columns
+    from pinned memory (GB/s, best of reps): all three on one stream, and one
+    per copy stream at once (the e2e step's pattern)."""
+    import torch
+
+    host = (hkey, hval, hval2)
+    nbytes = sum(h.numel() * h.element_size() for h in host)
+    out = {}
+    for name, streams in (("one_stream", [copy_streams[0]] * 3), ("three_streams", copy_streams)):
+        best = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for cs, d, h in zip(streams, dev, host):
+                with torch.cuda.stream(cs):
+                    d.copy_(h, non_blocking=True)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        out[name] = nbytes / best / 1e9
+    return out
 
 
 def run_ours(args, rank, world, local):
@@ -287,9 +326,9 @@ def run_ours(args, rank, world, local):
     rows_per_step = 2 * N_ROWS
     value = rows_per_step * world / (ms * 1e-3)
 
-    # dominant kernel: the group-by pass 1 (plain or fused, whichever takes
-    # longer in total); its algorithmic bytes are the input columns it reads.
-    names = {"k_gb_part": N_ROWS * 8, "k_gb_part_fused": N_ROWS * 12}
+    # dominant kernel: the dense group-by's main pass (plain or fused, whichever
+    # takes longer in total); its algorithmic bytes are the input columns it reads.
+    names = {"k_gbd_main": N_ROWS * 8, "k_gbd_main_fused": N_ROWS * 12}
     dom = max(names, key=lambda n: kern.get(n, (0, 0.0))[1])
     roof = roofline(kern, dom, names[dom], peak)
     traffic_path = ROOT / "profiles" / "traffic.json"
@@ -353,6 +392,7 @@ def run_ours(args, rank, world, local):
     e2e_ms = max_over_ranks((time.perf_counter() - t0) / e2e_steps * 1e3, world)
     e2e = {"value": rows_per_step * world / (e2e_ms * 1e-3), "unit": "rows/s",
            "h2d_bytes_per_step": 3 * N_ROWS * 4, "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+           "h2d_pinned_gbs": pinned_copy_rates(hkey, hval, hval2, dev_in[0], copy_streams),
            "note": "inputs copied from pinned host memory on copy streams (one per column; the next step's "
                    "copies overlap this step's compute); results copied to pinned host memory"}
 
@@ -363,7 +403,7 @@ def run_ours(args, rank, world, local):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         host = {"key": hkey.numpy(), "val": hval.numpy(), "val2": hval2.numpy()}
-        cpu = cpu_baseline_groupby(host, 1 << 23)
+        cpu = cpu_baseline_groupby(host)
 
     if rank == 0:
         line = {
@@ -425,7 +465,7 @@ def operator_lines(ctx, args, peak, stream):
     out["groupby_config1_unordered"] = {"rows_per_s": N_ROWS / (ms * 1e-3), "ms_per_op": ms,
                                         "op_frac_of_peak": (N_ROWS * 8 + GROUPS * 20) / (ms * 1e-3) / 1e9 / peak,
                                         "path": ctx.groupby_stats()["path"],
-                                        "roofline": roofline(kern, "k_gb_part", N_ROWS * 8, peak)}
+                                        "roofline": roofline(kern, "k_gbd_main", N_ROWS * 8, peak)}
 
     def fgstep():
         ctx.groupby_cols(d["key"], d["val"], d["val2"], d["lo2"], d["hi2"], cap=GROUPS, order=QG_ORDER_NONE)
@@ -435,7 +475,7 @@ def operator_lines(ctx, args, peak, stream):
         "rows_per_s": N_ROWS / (ms * 1e-3), "ms_per_op": ms,
         "op_frac_of_peak": (N_ROWS * 12 + GROUPS * 20) / (ms * 1e-3) / 1e9 / peak,
         "path": ctx.groupby_stats()["path"],
-        "roofline": roofline(kern, "k_gb_part_fused", N_ROWS * 12, peak)}
+        "roofline": roofline(kern, "k_gbd_main_fused", N_ROWS * 12, peak)}
     del d
     torch.cuda.empty_cache()
     # config 2: join + filter + sort
