@@ -177,6 +177,9 @@ struct FpSmem {
     int32_t p[FP_STAGES][FP_TILE];
     unsigned long long bar[FP_STAGES];
     uint32_t tile_of[FP_STAGES];
+    uint32_t pending[FP_STAGES];  // a copy (or arrival) was issued into the stage and not yet seen to land
+    uint32_t phase[FP_STAGES];    // phases of the stage's barrier seen to complete
+    uint32_t broken;              // a wait gave up: no more copies, every later tile read from global
     uint32_t woff[FP_ROUNDS * FP_WARPS];
     uint32_t bal[FP_ROUNDS * FP_WARPS];
     uint32_t lbtmp[2 * FT_LB_WARPS + 1];
@@ -210,9 +213,12 @@ k_filter_cols_tma(const int32_t *__restrict__ key, const int32_t *__restrict__ p
         for (int s = 0; s < FP_STAGES; s++) qg_mbar_init(&S.bar[s], 1);
         qg_mbar_fence_init();
         S.epoch = *(volatile uint32_t *)&lb.ctl->epoch;
+        S.broken = 0;
         for (int s = 0; s < FP_STAGES; s++) {
             const uint32_t t = atomicAdd(&lb.ctl->tile_ctr, 1u);
             S.tile_of[s] = t;
+            S.phase[s] = 0;
+            S.pending[s] = t < num_tiles ? 1u : 0u;
             if (t < num_tiles) fp_issue(S, s, key, pay, n, t);
         }
     }
@@ -221,21 +227,39 @@ k_filter_cols_tma(const int32_t *__restrict__ key, const int32_t *__restrict__ p
         const int s = (int)(it % FP_STAGES);
         const uint32_t t = S.tile_of[s];
         if (t >= num_tiles) break;
-        const uint32_t parity = (it / FP_STAGES) & 1u;
-        uint32_t w = 0;
-        bool landed = true;
-        while (!qg_mbar_try_wait(&S.bar[s], parity)) {
-            if (++w >= lb.spin_limit) {
-                // The copy never landed: report, and read the tile from global.
+        // Bounded wait for the stage's copy.  The CTA uses the staged tile only
+        // when every thread saw it land; otherwise it reports QG_ERR_TIMEOUT,
+        // reads this and every later tile from global memory, issues no more
+        // copies, and never reads a stage whose copy it did not see land.
+        const bool waited = !S.broken && S.pending[s];
+        bool landed = false;
+        if (waited) {
+            const uint32_t parity = S.phase[s] & 1u;
+            uint32_t w = 0;
+            landed = true;
+            while (!qg_mbar_try_wait(&S.bar[s], parity)) {
+                if (++w >= lb.spin_limit) {
+                    landed = false;
+                    break;
+                }
+            }
+        }
+        const bool all = __syncthreads_and(landed) != 0;
+        const bool some = __syncthreads_or(landed) != 0;
+        if (waited && tid == 0) {
+            if (!all) {
                 qg_record_error(lb.ctl, QG_ERR_TIMEOUT, lb.site);
-                landed = false;
-                break;
+                S.broken = 1;
+            }
+            if (some) {  // the copy completed (a thread saw its phase end)
+                S.pending[s] = 0;
+                S.phase[s]++;
             }
         }
         const long long base = (long long)t * FP_TILE;
         long long rows_l = n - base;
         const int rows = rows_l > FP_TILE ? FP_TILE : (int)rows_l;
-        const int bulk_rows = landed ? (rows & ~3) : 0;
+        const int bulk_rows = (waited && all) ? (rows & ~3) : 0;
 #pragma unroll
         for (int r = 0; r < FP_ROUNDS; r++) {
             const int row = r * FP_THREADS + tid;
@@ -267,10 +291,26 @@ k_filter_cols_tma(const int32_t *__restrict__ key, const int32_t *__restrict__ p
         if (tid == 0) {
             const uint32_t t2 = atomicAdd(&lb.ctl->tile_ctr, 1u);
             S.tile_of[s] = t2;
-            if (t2 < num_tiles) fp_issue(S, s, key, pay, n, t2);
+            if (t2 < num_tiles && !S.broken && !S.pending[s]) {
+                fp_issue(S, s, key, pay, n, t2);
+                S.pending[s] = 1;
+            }
         }
         __syncthreads();
     }
+    // A copy still in flight into this CTA's shared memory must land before the
+    // CTA exits (only after a wait gave up): wait for it, again with a limit --
+    // its own, not the caller's poll limit, which may be 0 (a copy from valid
+    // memory lands within microseconds; the limit only bounds the loop).
+    if (tid == 0 && S.broken) {
+        constexpr uint32_t DRAIN_POLLS = 1u << 22;
+        for (int s = 0; s < FP_STAGES; s++) {
+            if (!S.pending[s]) continue;
+            for (uint32_t w = 0; w < DRAIN_POLLS && !qg_mbar_try_wait(&S.bar[s], S.phase[s] & 1u); w++) {
+            }
+        }
+    }
+    __syncthreads();
     qg_lb_end(lb);
 }
 

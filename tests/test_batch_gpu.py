@@ -2,6 +2,7 @@
 queries) against the plain per-query calls of the same operators."""
 import numpy as np
 import pytest
+import torch
 
 from query_on_opencl_fpga_gb300 import batch as qb
 
@@ -96,3 +97,31 @@ def test_batch_lanes_match_plain_calls(ctx, lanes):
     finally:
         lib.qg_batch_set_lanes(8)
     assert lib.qg_batch_set_lanes(0) != 0 and lib.qg_batch_set_lanes(17) != 0
+
+
+def test_batch_queries_match_oracle(ctx, orc):
+    # Every query of a batch holding all four operators, checked against the
+    # CPU oracle: the filter in input order, group-by and fused as groups by
+    # key, the join as a key-sorted multiset.
+    qs = qb.mixed_queries(16, seed=23, lo=4096, hi=1 << 17)
+    assert {q["op"] for q in qs} == {qb.OP_FILTER, qb.OP_GROUPBY, qb.OP_FUSED, qb.OP_JOIN}
+    b = qb.Batch(qs, autotune=False)
+    try:
+        b.run()
+        b.check()
+        for q, got in zip(qs, qb.batch_results(qs)):
+            i = [t.cpu().numpy() for t in q["inp"]]
+            if q["op"] == qb.OP_FILTER:
+                exp = orc.filter_cols(i[0], i[1], q["lo"], q["hi"])
+                assert np.array_equal(got.cpu().numpy(), exp)
+            elif q["op"] in (qb.OP_GROUPBY, qb.OP_FUSED):
+                v2 = i[2] if q["op"] == qb.OP_FUSED else None
+                ek, es, ec = orc.groupby_cols(i[0], i[1], v2, q["lo"], q["hi"])
+                gk, gs, gc = [t.cpu().numpy() for t in got]
+                o = np.argsort(gk.view(np.uint32), kind="stable")
+                assert np.array_equal(gk[o], ek) and np.array_equal(gs[o], es) and np.array_equal(gc[o], ec)
+            else:
+                exp = orc.join_filter_sort(i[0], i[1], i[2], i[3], q["lo"], q["hi"], cap=q["cap"])
+                _same(q["op"], got, tuple(torch.from_numpy(x) for x in exp))
+    finally:
+        b.close()

@@ -100,6 +100,31 @@ def test_lookback_timeout_reports_and_recovers(ctx, orc):
     assert np.array_equal(got, orc.filter_rec(rin, 0, 50))
 
 
+@pytest.mark.parametrize("variant", [0, 1])
+def test_filter_cols_timeout_reports_and_recovers(ctx, orc, variant):
+    # Poll limit 0 on the single-pass column filters: every wait (look-back,
+    # and for variant 1 the bulk-copy ring's barriers) gives up at once.  The
+    # call reports a timeout, the ring stops refilling and drains its copies,
+    # and the next call with the default limit is exact.
+    from query_on_opencl_fpga_gb300 import QGError
+
+    ctx.check(ctx.lib.qg_filter_set_variant(variant), "variant")
+    d = datagen.config0_filter(1 << 22, seed=41)
+    key, pay = d["key"].numpy(), d["payload"].numpy()
+    try:
+        ctx.set_spin_limit(0)
+        try:
+            with pytest.raises(QGError) as e:
+                ctx.filter_cols(dev(key), dev(pay), d["lo"], d["hi"])
+            assert e.value.status == 5
+        finally:
+            ctx.set_spin_limit(1 << 22)
+        got = ctx.filter_cols(dev(key), dev(pay), d["lo"], d["hi"]).cpu().numpy()
+        assert np.array_equal(got, orc.filter_cols(key, pay, d["lo"], d["hi"]))
+    finally:
+        ctx.lib.qg_filter_set_variant(2)
+
+
 @pytest.mark.parametrize("variant", [0, 1, 2])
 @pytest.mark.parametrize("n", [1, 4095, 4099, 300007, 1 << 22, 1048576 + 4096 * 300 + 5])
 def test_filter_cols_variants(ctx, orc, variant, n):

@@ -154,3 +154,43 @@ def test_part_radix_eval(ctx):
     keys = torch.tensor([5, 6, 1029, -1], dtype=torch.int32, device="cuda")
     b = ctx.part_eval(keys, None, kmin=5, shift=10).cpu().tolist()
     assert b == [0, 0, 1, (2 ** 32 - 1 - 5) >> 10]
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_join_config4_full_size(ctx, knobs, variant):
+    # The skewed config at the size the bench quotes (R 32M unique keys, S 256M
+    # keys from 8 Gaussians + 5 % Zipf(1.2) heavy hitters, S.payload < 300),
+    # radix (1) and learned (2) partitioning; both leave rows in oversize
+    # buckets, so the sort-merge and cross-product paths run.  Size-independent
+    # exact checks: the row count equals the filtered S rows whose key is in R,
+    # keys ascend (unsigned), every R.payload is R's payload for that key, and
+    # the multiset of (key, S.payload) equals the filtered, matching S rows'.
+    knobs(variant)
+    d = datagen.config4_skewed(1 << 25, 1 << 28, seed=0, device="cuda")
+    ok, orp, osp = ctx.join_filter_sort(d["rkey"], d["rpay"], d["skey"], d["spay"], d["slo"], d["shi"],
+                                        cap=120_000_000)
+    st = ctx.join_stats()
+    assert st["path"] == {1: "radix", 2: "learned"}[variant]
+    assert st["outside_rows"] > 0, st
+    ru = d["rkey"].long() & 0xFFFFFFFF
+    ru_sorted, order = torch.sort(ru)
+    rpay_sorted = d["rpay"][order]
+    del ru, order
+    m = d["spay"] <= 299
+    sk = d["skey"][m].long() & 0xFFFFFFFF
+    ss = d["spay"][m].long()
+    del m
+    pos = torch.searchsorted(ru_sorted, sk).clamp_(max=ru_sorted.numel() - 1)
+    hit = ru_sorted[pos] == sk
+    sk, ss = sk[hit], ss[hit]
+    del pos, hit
+    assert ok.numel() == sk.numel()
+    gu = ok.long() & 0xFFFFFFFF
+    assert bool((gu[1:] >= gu[:-1]).all())
+    gpos = torch.searchsorted(ru_sorted, gu)
+    assert torch.equal(orp, rpay_sorted[gpos])
+    del gpos
+    e = torch.sort(sk * 1024 + ss).values
+    del sk, ss
+    g = torch.sort(gu * 1024 + osp.long()).values
+    assert torch.equal(e, g)
