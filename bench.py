@@ -553,31 +553,52 @@ def sort_line(ctx, steps, peak, stream):
 
 
 def skew_line(ctx, stream):
-    """Config 4: skewed join, plain radix partitioning vs the learned partition function."""
+    """Config 4: skewed join.  Plain radix partitioning (variant 1) against the
+    learned partition function (variant 2), and against the engine steered by
+    the learned cost model (trained on the recorded cost log, attached to the
+    context: the library picks the join variant itself, judged against the
+    plain one)."""
+    import json as _json
+
     import torch
 
-    from query_on_opencl_fpga_gb300 import datagen
+    from query_on_opencl_fpga_gb300 import costmodel, datagen
 
     nR, nS = 1 << 25, 1 << 28
     j = datagen.config4_skewed(nR, nS, seed=0, device="cuda")
-    res = {}
-    for name, v in (("radix", 1), ("learned", 2)):
-        ctx.join_set_knobs(v)
 
-        def step():
-            ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"], j["shi"],
-                                 cap=int(nS * 0.3) + 1024)
+    def step():
+        ctx.join_filter_sort(j["rkey"], j["rpay"], j["skey"], j["spay"], j["slo"], j["shi"],
+                             cap=int(nS * 0.3) + 1024)
 
+    def timed_ms():
         step()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(2):
             step()
         torch.cuda.synchronize()
-        ms = (time.perf_counter() - t0) / 2 * 1e3
+        return (time.perf_counter() - t0) / 2 * 1e3
+
+    res = {}
+    for name, v in (("radix", 1), ("learned", 2)):
+        ctx.join_set_knobs(v)
+        ms = timed_ms()
         res[name] = {"ms_per_op": ms, "rows_per_s": (nR + nS) / (ms * 1e-3), **ctx.join_stats()}
     ctx.join_set_knobs(0)
+    recs = _json.loads((ROOT / "tests" / "golden" / "costlog.json").read_text())["records"]
+    params, _ = costmodel.train(ctx, recs)
+    ctx.steer_attach(params)
+    try:
+        ms = timed_ms()
+        st = ctx.steer_stats(3)
+        res["steered"] = {"ms_per_op": ms, "rows_per_s": (nR + nS) / (ms * 1e-3), **ctx.join_stats(),
+                          "variant": st["last_variant"], "predicted_ms": st["last_pred_us"] / 1e3,
+                          "judge": {k: st[k] for k in ("calls", "model_calls", "trials", "fallbacks")}}
+    finally:
+        ctx.steer_detach()
     res["learned_over_radix"] = res["radix"]["ms_per_op"] / res["learned"]["ms_per_op"]
+    res["steered_over_radix"] = res["radix"]["ms_per_op"] / res["steered"]["ms_per_op"]
     res["workload"] = ("config4: R 32M distinct keys and S 256M keys from 8 Gaussians (sigma 2^20) + 5% "
                        "Zipf(1.2) heavy hitters, S.payload < 300, output sorted by key")
     return res
@@ -603,7 +624,8 @@ def batched_line(ctx, stream):
     plain_ms = (time.perf_counter() - t0) * 1e3
     recs = _json.loads((ROOT / "tests" / "golden" / "costlog.json").read_text())["records"]
     params, _ = costmodel.train(ctx, recs)
-    qb.choose_variants(ctx, params, qs)
+    qb.choose_variants(ctx, params, qs)  # chosen by the library from the attached model
+    ctx.steer_detach()
     b = qb.Batch(qs, autotune=True)
     b.run()
     b.check()

@@ -316,6 +316,36 @@ QG_API qg_status qg_mlp_grad(qg_ctx *ctx, const float *params, const float *X, c
 QG_API qg_status qg_mlp_train(qg_ctx *ctx, float *params, const float *X, const float *y, int64_t n,
                               int steps, float lr, float *opt, int *t, float *loss);
 
+/* ---- the cost model steering the engine (replaces the static variant
+ * choice of host/dynamic_programming.cpp:874-996 with the model's, the plain
+ * choice kept as fallback and judge) ----
+ * Operators: 0 filter (qg_filter_cols), 1 group-by, 2 fused filter +
+ * group-by (qg_groupby_cols without / with val2), 3 join (qg_join_filter_sort).
+ * qg_steer_attach evaluates the model (device params, as trained) once on a
+ * grid of plan features with the inference kernel and keeps the predicted
+ * time of every variant per grid cell on the context.  From then on each
+ * synchronous call of those operators on the context runs its cell's
+ * predicted-fastest variant and times itself; a call slower than
+ * (1 + tolerance) x its prediction makes the cell's next call run the plain
+ * variant (the process-wide knob), and the cell keeps whichever of the two
+ * ran faster.  Results are identical whichever variant runs.
+ * qg_steer_choose: the variant the context would run (without running it)
+ * and its predicted ms.  qg_steer_stats: per operator, out[0] calls,
+ * [1] calls that ran the model's non-plain choice, [2] calls that ran the
+ * plain variant, [3] judge runs of the plain variant, [4] cells that fell
+ * back to it, [5] cells whose choice a judge run confirmed, [6] the last
+ * call's variant, [7] its measured and [8] its predicted time in us,
+ * [9] grid cells where the model's choice differs from the plain one.
+ * qg_steer_plan: the reference's DP (dp_test sub_index 0-3, size in M rows)
+ * over a cost table of the model's per-variant predictions (one row per
+ * primitive and variant, scan primitives at zero cost: they are fused into
+ * the operators); *variant receives the operator variant the plan chose. */
+QG_API qg_status qg_steer_attach(qg_ctx *ctx, const float *d_params, float tolerance);
+QG_API qg_status qg_steer_detach(qg_ctx *ctx);
+QG_API qg_status qg_steer_choose(qg_ctx *ctx, int op, int64_t n, int64_t n2, float sel, int *variant,
+                                 float *pred_ms);
+QG_API qg_status qg_steer_stats(qg_ctx *ctx, int op, int64_t *out10);
+
 /* ---- learned partition function (no reference counterpart) ----
  * A piecewise-linear model of a key CDF (1024 fp32 segments plus heavy-key
  * knots) mapping keys to nbuckets buckets, non-decreasing in the unsigned

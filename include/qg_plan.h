@@ -70,6 +70,10 @@ QG_API const char *qg_plan_variant_name(int kernel_id, int variant);
  * fpga_model = 0 the resource -> frequency model is off (freq = 1), which is
  * how a table of measured GPU kernel costs is planned. */
 QG_API qg_status qg_plan_set_table(const qg_plan_variant *rows, int n_rows, int fpga_model);
+/* The DP of qg_plan_pipeline over the cost table of the context's learned
+ * model (qg_steer_attach, include/qg.h); *variant: the operator variant the
+ * plan chose.  The process-wide table is not changed. */
+QG_API qg_status qg_steer_plan(qg_ctx *ctx, int sub_index, float size_m, qg_plan *out, int *variant);
 
 #ifdef __cplusplus
 }

@@ -72,6 +72,12 @@ SIGNATURES: dict[str, tuple] = {
     "qg_join_filter_sort": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                     c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64,
                                     POINTER(c_int64)]),
+    "qg_steer_attach": (c_int, [c_void_p, c_void_p, ctypes.c_float]),
+    "qg_steer_detach": (c_int, [c_void_p]),
+    "qg_steer_choose": (c_int, [c_void_p, c_int, c_int64, c_int64, ctypes.c_float, POINTER(c_int),
+                                POINTER(ctypes.c_float)]),
+    "qg_steer_stats": (c_int, [c_void_p, c_int, c_void_p]),
+    "qg_steer_plan": (c_int, [c_void_p, c_int, ctypes.c_float, c_void_p, POINTER(c_int)]),
     "qg_hash_table_bytes": (c_int64, [c_int64]),
     "qg_hash_build_ref": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64]),
     "qg_hash_probe_ref": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_int64, POINTER(c_int64)]),

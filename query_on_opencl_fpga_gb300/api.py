@@ -7,7 +7,7 @@ Records are int32 tensors of shape (n, 2) holding the reference's uint2
 from __future__ import annotations
 
 import ctypes
-from ctypes import byref, c_int64, c_void_p
+from ctypes import byref, c_int, c_int64, c_void_p
 
 import torch
 
@@ -352,6 +352,41 @@ class Context:
                 continue
             self.check(st, "qg_hash_join_ref")
             return out[: m.value]
+
+    # ---- the learned cost model steering the engine ------------------------
+    def steer_attach(self, params: torch.Tensor, tolerance: float = 0.25):
+        """Let the context's operator calls run the variants the model (device
+        params from costmodel.train) predicts fastest, judged against the
+        plain variant when a call is slower than (1 + tolerance) x predicted."""
+        _check_dev(params)
+        self.check(self.lib.qg_steer_attach(self.handle, _ptr(params), tolerance), "qg_steer_attach")
+
+    def steer_detach(self):
+        self.check(self.lib.qg_steer_detach(self.handle), "qg_steer_detach")
+
+    def steer_choose(self, op: int, n: int, n2: int = 0, sel: float = 1.0):
+        """(variant, predicted ms) the context would run for operator op (0 filter,
+        1 group-by, 2 fused, 3 join)."""
+        v = c_int()
+        ms = ctypes.c_float()
+        self.check(self.lib.qg_steer_choose(self.handle, op, n, n2, sel, byref(v), byref(ms)), "qg_steer_choose")
+        return v.value, ms.value
+
+    def steer_stats(self, op: int) -> dict:
+        out = (c_int64 * 10)()
+        self.check(self.lib.qg_steer_stats(self.handle, op, out), "qg_steer_stats")
+        keys = ("calls", "model_calls", "default_calls", "trials", "fallbacks", "confirmed", "last_variant",
+                "last_us", "last_pred_us", "cells_nondefault")
+        return dict(zip(keys, list(out)))
+
+    def steer_plan(self, sub_index: int, size_m: float):
+        """(plan, operator variant) of the DP over the model's cost table."""
+        from ._lib import Plan
+
+        p = Plan()
+        v = c_int()
+        self.check(self.lib.qg_steer_plan(self.handle, sub_index, size_m, byref(p), byref(v)), "qg_steer_plan")
+        return p, v.value
 
     def hash_build_ref(self, r_pairs: torch.Tensor) -> torch.Tensor:
         """Build the reference-layout hash table of R's (key, val) pairs into a

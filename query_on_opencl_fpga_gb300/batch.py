@@ -68,17 +68,19 @@ def input_rows(qs: list[dict]) -> int:
 
 
 def choose_variants(ctx, params, qs: list[dict]) -> None:
-    """Per-query variants from the learned cost model (costmodel.choose);
-    joins in a graph always take the hash + device-planned sort form."""
-    from . import costmodel
+    """Per-query variants chosen by the library (qg_steer_choose) from the
+    learned cost model attached to ctx; joins in a graph always take the
+    hash + device-planned sort form."""
+    from .costmodel import range_share
 
+    ctx.steer_attach(params)
     for q in qs:
         if q["op"] == OP_JOIN:
             q["variant"] = -1
             continue
-        sel = {OP_FILTER: 0.1, OP_GROUPBY: 1.0, OP_FUSED: 0.5}[q["op"]]
-        n2 = 0 if q["op"] == OP_FILTER else min(q["n"], q["n2"])
-        q["variant"] = costmodel.choose(ctx, params, OP_NAMES[q["op"]], q["n"], n2, sel, 1)
+        sel = range_share(q["lo"], q["hi"]) if q["op"] == OP_FILTER else 1.0
+        n2 = 0 if q["op"] == OP_FILTER else q["cap"]
+        q["variant"] = ctx.steer_choose(q["op"], q["n"], n2, sel)[0]
 
 
 class Batch:

@@ -52,6 +52,7 @@ QG_API qg_status qg_ctx_create(qg_ctx **out, void *stream) {
         return QG_ERR_CUDA;
     }
     ctx->table_dirty = true;
+    for (int i = 0; i < QG_STEER_OPS; i++) ctx->steer_force[i] = -1;
     *out = ctx;
     return QG_OK;
 }
@@ -59,6 +60,7 @@ QG_API qg_status qg_ctx_create(qg_ctx **out, void *stream) {
 QG_API qg_status qg_ctx_destroy(qg_ctx *ctx) {
     if (!ctx) return QG_ERR_INVALID;
     cudaStreamSynchronize(ctx->stream);
+    qg_steer_free(ctx);
     if (ctx->ev[0])
         for (int i = 0; i < 2 * QG_MAX_TIMED; i++) cudaEventDestroy(ctx->ev[i]);
     if (ctx->scratch) cudaFree(ctx->scratch);

@@ -498,7 +498,8 @@ qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *
     if (tiles > 0x7fffffff || n > 0x7fffffffLL) return QG_ERR_UNSUPPORTED;
     qg_lookback lb;
     QG_TRY(qg_lb_make(ctx, tiles, QG_SITE_FILTER, &lb));
-    if (g_filter_variant == 2) {
+    const int variant = qg_effective_variant(ctx, QG_STEER_FILTER, g_filter_variant);
+    if (variant == 2) {
         const long long tp_tiles = qg_ceil_div(n, TP_TILE);
         const long long groups = qg_ceil_div(tp_tiles, TP_GROUP);
         char *scr;
@@ -515,7 +516,7 @@ qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *
                                                                          cap, d_count);
         return qg_check_launch(ctx, "k_filter_write");
     }
-    if (g_filter_variant == 1) {
+    if (variant == 1) {
         static bool attr = false;
         if (!attr) {
             QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_filter_cols_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -538,6 +539,8 @@ qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *
 // 0: one tile per CTA, rows staged in registers, decoupled look-back;
 // 1: persistent CTAs with a bulk-copy ring; 2: two passes (count, write)
 // with no look-back (all bit-identical; chosen by measurement).
+int qg_filter_default_variant() { return g_filter_variant; }
+
 extern "C" QG_API qg_status qg_filter_set_variant(int variant) {
     if (variant < 0 || variant > 2) return QG_ERR_INVALID;
     g_filter_variant = variant;
@@ -573,9 +576,15 @@ QG_API qg_status qg_filter_cols(qg_ctx *ctx, const int32_t *key, const int32_t *
                                 int32_t lo, int32_t hi, int32_t *out, int64_t cap,
                                 int64_t *out_n) {
     if (!ctx || !out_n) return QG_ERR_INVALID;
+    // With a cost model attached the variant is its choice for this size; the
+    // selectivity estimate is the predicate's share of the int32 range.
+    qg_steer_call sc;
+    qg_steer_begin(ctx, QG_STEER_FILTER, n, 0, ((double)hi - (double)lo + 1.0) / 4294967296.0, &sc);
     long long *d_count = (long long *)&ctx->ctl->counter[0];
-    QG_TRY(qg_filter_cols_async(ctx, key, pay, n, lo, hi, out, cap, (int64_t *)d_count));
-    return finish_count(ctx, d_count, cap, out_n);
+    qg_status st = qg_filter_cols_async(ctx, key, pay, n, lo, hi, out, cap, (int64_t *)d_count);
+    if (st == QG_OK) st = finish_count(ctx, d_count, cap, out_n);
+    qg_steer_end(ctx, &sc, st);
+    return st;
 }
 
 }  // extern "C"

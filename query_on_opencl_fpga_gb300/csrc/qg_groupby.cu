@@ -1096,15 +1096,16 @@ extern "C" QG_API qg_status qg_aggregate_groups(qg_ctx *ctx, const void *sorted,
 // ---------------------------------------------------------------------------
 // host: column hash group-by
 // ---------------------------------------------------------------------------
-static int g_gb_mode = 0;            // 0: two-pass (global table as fallback), 1: global table only
-static int g_gb_dense = 1;           // 1: the dense-window path first (qg_gbdense.cu), two-pass when it does not apply
+// Variant (qg_groupby_set_knobs mode): 0 the dense-window path (qg_gbdense.cu)
+// first, two-pass when it does not apply; 1 the global table only; 2 two-pass
+// with 64-bit shared adds; 3 two-pass.  A steered call may run another.
+static int g_gb_knob = 0;
 static int g_gb_hot_slog2 = 13;      // pass-1 shared-memory table slots (log2)
 static int g_gb_plog2 = 0;           // spill partitions (log2); 0 = chosen from cap
 static uint32_t g_gb_capm = 0;       // spill bucket capacity override (0 = automatic)
 // 0 (default): int64 sums as two 32-bit words with explicit carry; 1: one
 // 64-bit shared atomic per add.  Measured on GB300 (64M rows, Zipf 1M groups):
 // pass 1 takes 0.44 ms with the carry scheme and 1.22 ms with 64-bit atomics.
-static int g_gb_sum64 = 0;
 static uint32_t g_gb_last_capm = 0;  // bucket capacity of the last two-pass launch
 static const int g_gb_slog2 = 12;    // fallback kernel: shared-memory table slots (log2)
 
@@ -1119,14 +1120,21 @@ extern "C" QG_API qg_status qg_groupby_stats(qg_ctx *ctx, uint32_t *out) {
 }
 static const int g_gb_blocks_per_sm = 2;
 
+int qg_groupby_default_mode() { return g_gb_knob; }
+
+// The variant a call on ctx runs (steered calls of either group-by form set it).
+static int gb_mode(const qg_ctx *ctx) {
+    const int f = ctx->steer_force[QG_STEER_GROUPBY] >= 0 ? ctx->steer_force[QG_STEER_GROUPBY]
+                                                           : ctx->steer_force[QG_STEER_FUSED];
+    return f >= 0 ? f : g_gb_knob;
+}
+
 extern "C" QG_API qg_status qg_groupby_set_knobs(int mode, int hot_slots_log2, int partitions_log2,
                                                  uint32_t bucket_cap) {
     if (mode < 0 || mode > 3 || hot_slots_log2 < 8 || hot_slots_log2 > 13 || partitions_log2 < 0 ||
         partitions_log2 > 13)
         return QG_ERR_INVALID;
-    g_gb_mode = mode == 1 ? 1 : 0;
-    g_gb_sum64 = mode == 2 ? 1 : 0;
-    g_gb_dense = mode == 0 ? 1 : 0;
+    g_gb_knob = mode;
     g_gb_hot_slog2 = hot_slots_log2;
     g_gb_plog2 = partitions_log2;
     g_gb_capm = bucket_cap;
@@ -1246,7 +1254,7 @@ static qg_status gb_launch_twopass(qg_ctx *ctx, const int32_t *key, const int32_
     sp.slog2 = slog2;
     const size_t smem1 = (size_t)S * 16 + (size_t)P * 4 + (size_t)GB_SKETCH_WORDS * 4;
     const bool pred = val2 != nullptr;
-    const bool s64 = g_gb_sum64 != 0;
+    const bool s64 = gb_mode(ctx) == 2;
     auto part = pred ? (s64 ? k_gb_part<true, true> : k_gb_part<true, false>)
                      : (s64 ? k_gb_part<false, true> : k_gb_part<false, false>);
     static size_t attr[4] = {0, 0, 0, 0};
@@ -1360,12 +1368,12 @@ extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *ke
     if (!ctx || n < 0 || cap < 0 || !d_num || (n > 0 && (!key || !val))) return QG_ERR_INVALID;
     if (order != QG_ORDER_NONE && order != QG_ORDER_KEY) return QG_ERR_INVALID;
     // key order is planned on the device by the two-pass path only
-    if (order == QG_ORDER_KEY && (g_gb_mode == 1 || cap >= (1LL << 30))) return QG_ERR_UNSUPPORTED;
+    if (order == QG_ORDER_KEY && (gb_mode(ctx) == 1 || cap >= (1LL << 30))) return QG_ERR_UNSUPPORTED;
     if ((((uintptr_t)key) | ((uintptr_t)val) | ((uintptr_t)val2)) & 15) return QG_ERR_INVALID;
     if (n >= (1LL << 32)) return QG_ERR_UNSUPPORTED;
     GbOut o;
     QG_TRY(gb_outputs(ctx, gkey, gsum, gcnt, cap, order, &o));
-    if (g_gb_mode == 1)
+    if (gb_mode(ctx) == 1)
         return gb_launch_global(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num);
     unsigned int *flags = (unsigned int *)&ctx->ctl->counter[2];
     QG_TRY(gb_launch_twopass(ctx, key, val, val2, lo2, hi2, n, o, cap, (long long *)d_num, flags,
@@ -1377,11 +1385,32 @@ extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *ke
     return qg_check_launch(ctx, "k_gb_flags_to_error");
 }
 
+static qg_status groupby_cols_impl(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
+                                   int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum,
+                                   int64_t *gcnt, int64_t cap, int order, int64_t *num_groups);
+
 extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, const int32_t *val,
                                             const int32_t *val2, int32_t lo2, int32_t hi2,
                                             int64_t n, int32_t *gkey, int64_t *gsum,
                                             int64_t *gcnt, int64_t cap, int order,
                                             int64_t *num_groups) {
+    if (!ctx) return QG_ERR_INVALID;
+    // With a cost model attached the variant is its choice for this size; the
+    // group count is estimated by the output capacity, the fused predicate's
+    // selectivity by the share of the int32 range it keeps.
+    qg_steer_call sc;
+    const bool fused = val2 != nullptr;
+    qg_steer_begin(ctx, fused ? QG_STEER_FUSED : QG_STEER_GROUPBY, n, cap,
+                   fused ? ((double)hi2 - (double)lo2 + 1.0) / 4294967296.0 : 1.0, &sc);
+    const qg_status st = groupby_cols_impl(ctx, key, val, val2, lo2, hi2, n, gkey, gsum, gcnt, cap, order,
+                                           num_groups);
+    qg_steer_end(ctx, &sc, st);
+    return st;
+}
+
+static qg_status groupby_cols_impl(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
+                                   int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum,
+                                   int64_t *gcnt, int64_t cap, int order, int64_t *num_groups) {
     if (!ctx || n < 0 || cap < 0 || !num_groups || (n > 0 && (!key || !val)))
         return QG_ERR_INVALID;
     if (order != QG_ORDER_NONE && order != QG_ORDER_KEY) return QG_ERR_INVALID;
@@ -1392,13 +1421,14 @@ extern "C" QG_API qg_status qg_groupby_cols(qg_ctx *ctx, const int32_t *key, con
     GbOut o;
     QG_TRY(gb_outputs(ctx, gkey, gsum, gcnt, cap, order, &o));
     long long g = 0;
-    bool global = g_gb_mode == 1;
+    const int gm = gb_mode(ctx);
+    bool global = gm == 1;
     bool done = false;  // the two-pass path wrote the final output (any order)
     // Key order: the dense order unless the context's last key-ordered call
     // found its keys too widely spread, then the device-planned sort (up to
     // 2^30 records).  Whatever neither placed is sorted after the host has
     // read the count.
-    if (g_gb_dense && !global && n > 0) {
+    if (gm == 0 && !global && n > 0) {
         // Dense-window path: output in key order whatever `order` asks for;
         // one read of the control block brings the error word, the group
         // count and whether every row fell inside the window.

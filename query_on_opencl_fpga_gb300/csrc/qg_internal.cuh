@@ -52,6 +52,11 @@ struct qg_ctx {
     size_t pj_tmp_bytes;
     void *pin_join;         // host pinned bucket bounds and group plan of the join (allocated on first use)
     char msg[256];
+    // Learned variant choice (qg_steer.cu): the model's decision table and
+    // judge state when one is attached, and the variant a steered call runs
+    // (per operator QG_STEER_*, -1 = the process-wide knob).
+    struct qg_steer_state *steer;
+    int steer_force[4];
     // Per-kernel CUDA-event timing (qg_ctx_enable_timing): a pair of events
     // brackets every launch on the context's stream.
     bool timing;
@@ -79,6 +84,29 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
                         int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt,
                         int64_t cap, long long *d_num);
 enum { QG_GBD_OUTSIDE = 6 };
+
+// Operators the learned variant choice covers (the batch's OP_* order).
+enum { QG_STEER_FILTER = 0, QG_STEER_GROUPBY = 1, QG_STEER_FUSED = 2, QG_STEER_JOIN = 3, QG_STEER_OPS = 4 };
+// The process-wide (plain) variant of each operator: the default the learned
+// choice is judged against.
+int qg_filter_default_variant();
+int qg_groupby_default_mode();
+int qg_join_default_variant();
+// The variant a call of `op` on ctx runs: the steered one, else the knob.
+static inline int qg_effective_variant(const qg_ctx *ctx, int op, int knob) {
+    const int f = ctx->steer_force[op];
+    return f >= 0 ? f : knob;
+}
+// A steered synchronous call (qg_steer.cu): _begin picks the variant and
+// starts the call's device timer, _end reads it (the call has synchronised)
+// and updates the judge.  No-ops without an attached model.
+struct qg_steer_call {
+    int op, cell, variant;
+    bool active;
+};
+void qg_steer_begin(qg_ctx *ctx, int op, int64_t n, int64_t n2, double sel, qg_steer_call *c);
+void qg_steer_end(qg_ctx *ctx, qg_steer_call *c, qg_status st);
+void qg_steer_free(qg_ctx *ctx);
 // Ensure the scratch arena holds at least `bytes`; newly grown memory is zeroed.
 qg_status qg_scratch(qg_ctx *ctx, size_t bytes, char **out);
 // Ensure the operator-temporary arena holds at least `bytes` (not zeroed).

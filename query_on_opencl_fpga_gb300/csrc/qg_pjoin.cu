@@ -1351,18 +1351,41 @@ extern "C" QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8) {
     return QG_OK;
 }
 
+int qg_join_default_variant() { return g_pj_variant; }
+
+static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay, int64_t nR,
+                                       const int32_t *skey, const int32_t *spay, int64_t nS, int32_t slo,
+                                       int32_t shi, int32_t *out_key, int32_t *out_rpay, int32_t *out_spay,
+                                       int64_t cap, int64_t *out_n);
+
 extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay,
                                                 int64_t nR, const int32_t *skey, const int32_t *spay,
                                                 int64_t nS, int32_t slo, int32_t shi, int32_t *out_key,
                                                 int32_t *out_rpay, int32_t *out_spay, int64_t cap,
                                                 int64_t *out_n) {
+    if (!ctx) return QG_ERR_INVALID;
+    // With a cost model attached the variant is its choice for these sizes;
+    // the S filter's selectivity is estimated by its share of the int32 range.
+    qg_steer_call sc;
+    qg_steer_begin(ctx, QG_STEER_JOIN, nS, nR, ((double)shi - (double)slo + 1.0) / 4294967296.0, &sc);
+    const qg_status st = join_filter_sort_impl(ctx, rkey, rpay, nR, skey, spay, nS, slo, shi, out_key, out_rpay,
+                                               out_spay, cap, out_n);
+    qg_steer_end(ctx, &sc, st);
+    return st;
+}
+
+static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const int32_t *rpay, int64_t nR,
+                                       const int32_t *skey, const int32_t *spay, int64_t nS, int32_t slo,
+                                       int32_t shi, int32_t *out_key, int32_t *out_rpay, int32_t *out_spay,
+                                       int64_t cap, int64_t *out_n) {
     if (!ctx || nR < 0 || nS < 0 || cap < 0 || !out_n) return QG_ERR_INVALID;
+    const int variant = qg_effective_variant(ctx, QG_STEER_JOIN, g_pj_variant);
     if ((nR > 0 && (!rkey || !rpay)) || (nS > 0 && (!skey || !spay)) ||
         (cap > 0 && (!out_key || !out_rpay || !out_spay)))
         return QG_ERR_INVALID;
     if ((((uintptr_t)skey) | ((uintptr_t)spay)) & 15) return QG_ERR_INVALID;
     if (cap >= (1LL << 30) || nS >= (1LL << 40)) return QG_ERR_UNSUPPORTED;
-    if (g_pj_variant == 3 || nS >= (1LL << 30) || nR >= (1LL << 30))
+    if (variant == 3 || nS >= (1LL << 30) || nR >= (1LL << 30))
         return qg_join_hash_sort(ctx, rkey, rpay, nR, skey, spay, nS, slo, shi, out_key, out_rpay,
                                  out_spay, cap, out_n);
     *out_n = 0;
@@ -1397,7 +1420,7 @@ extern "C" QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey
     const long long ns1 = (long long)hr.count;
     long long M = 0;
     // pj_core ends with a read of the output count and the error word
-    QG_TRY(pj_core(ctx, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, g_pj_variant, (uint32_t *)out_key,
+    QG_TRY(pj_core(ctx, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, variant, (uint32_t *)out_key,
                    (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M, lvl));
     *out_n = M;
     return M > cap ? QG_ERR_CAPACITY : QG_OK;

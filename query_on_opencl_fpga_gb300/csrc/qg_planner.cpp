@@ -243,6 +243,8 @@ qg_status plan(const Table &t, const int *ops, int n_ops, int data_size, qg_plan
     return QG_OK;
 }
 
+qg_status make_table(const qg_plan_variant *rows, int n_rows, int fpga_model, Table *out);
+
 }  // namespace
 
 extern "C" {
@@ -280,7 +282,35 @@ QG_API qg_status qg_plan_set_table(const qg_plan_variant *rows, int n_rows, int 
         ensure_table();
         return QG_OK;
     }
-    if (n_rows < QG_K_NUM) return QG_ERR_INVALID;
+    Table t;
+    const qg_status st = make_table(rows, n_rows, fpga_model, &t);
+    if (st != QG_OK) return st;
+    g_table = t;
+    return QG_OK;
+}
+
+}  // extern "C"
+
+// The DP over one of dp_test's pipelines with a caller-built table, leaving
+// the process-wide table alone (the learned variant choice plans with it).
+qg_status qg_plan_pipeline_rows(const qg_plan_variant *rows, int n_rows, int fpga_model, int sub_index,
+                                float size_m, qg_plan *out) {
+    Table t;
+    const qg_status st = make_table(rows, n_rows, fpga_model, &t);
+    if (st != QG_OK) return st;
+    const int data_size = (int)(size_m * 1.0);
+    switch (sub_index) {
+        case 0: return plan(t, PIPE_SELECTION, 5, data_size, out);
+        case 1: return plan(t, PIPE_GROUP_AGG, 7, data_size, out);
+        case 2: return plan(t, PIPE_FILTER_GROUP_AGG, 12, data_size, out);
+        case 3: return plan(t, PIPE_SELECTION + 1, 3, data_size, out);
+    }
+    return QG_ERR_INVALID;
+}
+
+namespace {
+qg_status make_table(const qg_plan_variant *rows, int n_rows, int fpga_model, Table *out) {
+    if (!rows || n_rows < QG_K_NUM) return QG_ERR_INVALID;
     Table t;
     for (int k = 0; k < QG_K_NUM; k++) t.count[k] = 0;
     int prev = -1;
@@ -296,8 +326,7 @@ QG_API qg_status qg_plan_set_table(const qg_plan_variant *rows, int n_rows, int 
     for (int k = 0; k < QG_K_NUM; k++)
         if (t.count[k] == 0) return QG_ERR_INVALID;
     t.fpga = fpga_model != 0;
-    g_table = t;
+    *out = t;
     return QG_OK;
 }
-
-}  // extern "C"
+}  // namespace

@@ -1,7 +1,10 @@
-"""The learned cost model (csrc/qg_mlp.cu, query_on_opencl_fpga_gb300/costmodel.py):
-GPU forward pass and gradients against the double-precision oracle, training
-by the library's own kernels, and what the trained model gains over the
-engine's default variants on timings recorded on a GB300."""
+"""The learned cost model (csrc/qg_mlp.cu, csrc/qg_steer.cu,
+query_on_opencl_fpga_gb300/costmodel.py): GPU forward pass and gradients
+against the double-precision oracle, training by the library's own kernels,
+what the trained model gains over the engine's default variants on timings
+recorded on a GB300, the library running the model's choices itself with the
+plain variant as the judge of mispredictions, and the DP planner over the
+model's cost table."""
 import json
 from pathlib import Path
 
@@ -60,32 +63,141 @@ def _log():
 
 def test_cost_model_beats_default_variants_on_held_out_workloads(ctx):
     # Timings recorded on a GB300 by `costmodel collect`; every fourth
-    # workload is held out.  The model trained on the rest must choose
-    # variants whose recorded total time is below that of the engine's
-    # default variants, i.e. the gain of the learned model over the method
-    # without it.
+    # workload is held out.  The model trained on the rest, with the
+    # library's judge in the loop (a choice slower than 1.25 x its prediction
+    # gets one run of the default variant, and the faster is kept), must reach
+    # a recorded total below that of the engine's default variants and close
+    # to the best one: the gain of the learned method over the method without
+    # it.  (The model's choices alone are reported by judged_regret too; an
+    # extrapolation to a size it was not trained at can cost more than the
+    # rest gains, which is what the judge is for.)
     recs = _log()
     train = [r for r in recs if r["id"] % 4 != 3]
     test = [r for r in recs if r["id"] % 4 == 3]
     params, loss = costmodel.train(ctx, train)
-    assert loss < 0.5
-    learned = costmodel.regret(ctx, params, test)
+    assert loss < 0.1
     plain = costmodel.regret(ctx, None, test)
     assert plain["chosen"] == pytest.approx(plain["default"])
-    assert learned["chosen"] < plain["chosen"]
-    assert learned["chosen"] <= learned["best"] * 1.5
+    learned = costmodel.judged_regret(ctx, params, test, tol=0.25)
+    assert learned["judged"] < 0.95 * learned["default"], learned
+    assert learned["judged"] <= learned["best"] * 1.15, learned
 
 
 def test_planner_takes_the_models_cost_table(ctx):
+    # The reference's DP over a table of the model's per-variant predictions
+    # picks the predicted-fastest variant (qg_steer_plan in the library and the
+    # same table built in Python agree), and its plan is not the reference
+    # FPGA table's plan.
     from query_on_opencl_fpga_gb300 import _lib
 
-    params, _ = costmodel.train(ctx, _log(), steps=500)
-    rows = costmodel.plan_table(ctx, params)
+    params, _ = costmodel.train(ctx, _log(), steps=800)
     lib = ctx.lib
-    assert lib.qg_plan_set_table(rows, 9, 0) == 0
+    ref = _lib.Plan()
+    assert lib.qg_plan_pipeline(1, 64, ref) == 0
+    rows, nrows = costmodel.plan_table(ctx, params, 64.0, "groupby")
+    assert lib.qg_plan_set_table(rows, nrows, 0) == 0
     try:
         p = _lib.Plan()
         assert lib.qg_plan_pipeline(1, 64, p) == 0
-        assert p.image_num >= 1 and p.exec_time > 0
     finally:
         assert lib.qg_plan_set_table(None, 0, 1) == 0
+    ctx.steer_attach(params)
+    try:
+        sp, v = ctx.steer_plan(1, 64.0)
+        want, pred = ctx.steer_choose(1, 64 << 20, 1 << 20, 1.0)
+        assert v == want
+        assert sp.exec_time == pytest.approx(p.exec_time, rel=1e-3)
+        assert sp.exec_time == pytest.approx(pred, rel=1e-3)
+        sig = lambda q: [(im.kernels[j].kernel_id, im.kernels[j].variant)  # noqa: E731
+                         for im in q.images[:q.image_num] for j in range(im.num_kernels)]
+        assert (sig(sp), round(sp.exec_time, 4)) != (sig(ref), round(ref.exec_time, 4))
+    finally:
+        ctx.steer_detach()
+
+
+def _held_out_nondefault(ctx, params, recs):
+    """Held-out workloads where the engine's own choice (its features) is not
+    the default variant and the recorded log shows it faster."""
+    by = {}
+    for r in recs:
+        by.setdefault(r["id"], {})[r["variant"]] = r
+    out = []
+    for wid, vs in by.items():
+        r0 = next(iter(vs.values()))
+        op = costmodel.STEER_OP[r0["op"]]
+        v, _ = ctx.steer_choose(op, r0["n"], r0["n2"], r0["fsel"])
+        d = costmodel.DEFAULT_VARIANT[r0["op"]]
+        if v != d and vs[v]["ms"] < vs[d]["ms"]:
+            out.append((r0, v, d, vs[v]["ms"], vs[d]["ms"]))
+    return out
+
+
+def test_engine_steers_variant_on_held_out_workload(ctx):
+    # The model trained on three quarters of the log, attached to a context:
+    # on held-out workloads the library itself picks non-default variants
+    # that the log records as faster, runs them (bit-identical output) and
+    # counts them as the model's calls.
+    recs = _log()
+    train = [r for r in recs if r["id"] % 4 != 3]
+    test = [r for r in recs if r["id"] % 4 == 3]
+    params, _ = costmodel.train(ctx, train)
+    ctx.steer_attach(params)
+    try:
+        cands = _held_out_nondefault(ctx, params, test)
+        assert cands, "the model never beats the default on the held-out workloads"
+        gain = sum(d - c for _, _, _, c, d in cands)
+        assert gain > 0
+        r0, v, dflt, _, _ = min(cands, key=lambda c: c[0]["n"])  # the smallest such workload
+        fn = costmodel.make_op(ctx, {**r0, "id": r0["id"]})
+        op = costmodel.STEER_OP[r0["op"]]
+        before = ctx.steer_stats(op)
+        got = fn()
+        st = ctx.steer_stats(op)
+        assert st["calls"] == before["calls"] + 1
+        assert st["last_variant"] == v and st["model_calls"] >= before["model_calls"] + 1, st
+    finally:
+        ctx.steer_detach()
+    plain = fn()  # no model: the default variant
+    g = got if isinstance(got, tuple) else (got,)
+    p = plain if isinstance(plain, tuple) else (plain,)
+    if r0["op"] in ("groupby", "fused"):  # unordered output: compare in key order
+        og = torch.argsort(g[0].long() & 0xFFFFFFFF)
+        op_ = torch.argsort(p[0].long() & 0xFFFFFFFF)
+        g, p = tuple(t[og] for t in g), tuple(t[op_] for t in p)
+    for a, b in zip(g, p):
+        assert torch.equal(a, b)
+
+
+def test_judge_falls_back_when_the_model_mispredicts(ctx):
+    # A model trained on made-up timings that call the two-pass group-by with
+    # 64-bit shared adds (variant 2) nearly free: the library runs it, sees it
+    # take far longer than predicted, runs the plain variant on the next call,
+    # finds it faster and keeps it from then on.  Output is exact throughout.
+    from query_on_opencl_fpga_gb300 import datagen
+
+    n, groups = 1 << 24, 1 << 18
+    cap = 2 * groups + 1024
+    fake = []
+    for lg in (20, 22, 24):
+        for v in costmodel.VARIANTS["groupby"]:
+            fake.append({"op": "groupby", "n": 1 << lg, "n2": cap, "fsel": 1.0, "skew": 0, "variant": v,
+                         "ms": 0.001 if v == 2 else 50.0})
+    params, _ = costmodel.train(ctx, fake, steps=1500)
+    ctx.steer_attach(params, 0.5)
+    try:
+        assert ctx.steer_choose(1, n, cap, 1.0)[0] == 2
+        d = datagen.config1_groupby(n, groups, seed=5, device="cuda")
+        ref = None
+        for call in range(3):
+            out = ctx.groupby_cols(d["key"], d["val"], None, d["lo2"], d["hi2"], cap=cap)
+            st = ctx.steer_stats(1)
+            assert st["last_variant"] == (2 if call == 0 else 0), (call, st)
+            host = [t.cpu() for t in out]
+            if ref is None:
+                ref = host
+            else:
+                assert all(torch.equal(a, b) for a, b in zip(host, ref))
+        assert st["trials"] == 1 and st["fallbacks"] == 1 and st["confirmed"] == 0, st
+        assert ctx.steer_choose(1, n, cap, 1.0)[0] == 0
+    finally:
+        ctx.steer_detach()
