@@ -295,6 +295,18 @@ QG_API qg_status qg_batch_destroy(qg_batch *b);
  * 8): the queries are spread over that many streams, each with a private
  * context, and the graph runs the lanes side by side. */
 QG_API qg_status qg_batch_set_lanes(int lanes);
+/* Form of the batches created after this call (process-wide): 1
+ * persistent -- every filter, group-by and fused query runs inside one
+ * persistent kernel launch whose CTAs take (query, tile) work items from a
+ * device queue (filter tiles with a per-query look-back, group-by tiles into
+ * a per-query table, emit tiles after the query's tiles; the kernel's table
+ * and tile sizes are the autotuner's group tile of 2^13 or 2^14 rows), the
+ * joins as their own launches on the other lanes beside it; 0 (default)
+ * lanes -- every query as its operator's launches (faster on mixed queries
+ * with high-cardinality group-bys, whose per-query tables the persistent
+ * kernel touches at about one random sector per group).  In the persistent
+ * form a filter or group-by query's `variant` is not used. */
+QG_API qg_status qg_batch_set_persistent(int on);
 
 /* ---- learned cost model (no reference counterpart; it stands beside the
  * static unit-cost table of host/dynamic_programming.cpp:152-167) ----

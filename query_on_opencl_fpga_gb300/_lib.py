@@ -151,6 +151,7 @@ SIGNATURES.update({
     "qg_batch_info": (c_int, [c_void_p, c_void_p]),
     "qg_batch_destroy": (c_int, [c_void_p]),
     "qg_batch_set_lanes": (c_int, [c_int]),
+    "qg_batch_set_persistent": (c_int, [c_int]),
 })
 
 PLAN_MAX_OPS = 16

@@ -1,6 +1,8 @@
 """Batched mixed queries: many filter / group-by / fused / join+sort queries
-of uneven sizes as one captured CUDA graph (include/qg.h qg_batch_*), next to
-the plain form that calls the operators one by one.
+of uneven sizes as one captured CUDA graph (include/qg.h qg_batch_*) -- the
+filter and group-by queries inside one persistent kernel launch, or every
+query as its operator's launches spread over lanes -- next to the plain form
+that calls the operators one by one.
 
 The mixed workload draws each query's operator uniformly from {filter,
 group-by, filter_aggregation, join+sort} and its row count log-uniformly in
@@ -86,7 +88,10 @@ def choose_variants(ctx, params, qs: list[dict]) -> None:
 class Batch:
     """A captured batch (qg_batch).  Inputs and outputs must outlive it."""
 
-    def __init__(self, queries: list[dict], autotune: bool = True):
+    def __init__(self, queries: list[dict], autotune: bool = True, persistent: bool = False):
+        """persistent: filter / group-by / fused queries in one persistent kernel
+        launch (joins beside it); False (default): every query as its
+        operator's launches, spread over lanes."""
         self.lib = _lib.load()
         self.queries = queries
         arr = (_lib.Query * len(queries))()
@@ -101,7 +106,11 @@ class Batch:
             a.cap = q["cap"]
             a.d_count = q["count"].data_ptr()
         h = c_void_p()
-        st = self.lib.qg_batch_create(arr, len(queries), int(autotune), byref(h))
+        self.lib.qg_batch_set_persistent(int(persistent))
+        try:
+            st = self.lib.qg_batch_create(arr, len(queries), int(autotune), byref(h))
+        finally:
+            self.lib.qg_batch_set_persistent(0)
         if st != 0:
             raise QGError(st, "qg_batch_create")
         self.handle = h

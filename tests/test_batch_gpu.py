@@ -30,11 +30,12 @@ def _same(op, got, exp):
     assert np.array_equal(gs, es)
 
 
+@pytest.mark.parametrize("persistent", [True, False])
 @pytest.mark.parametrize("autotune", [False, True])
-def test_batch_matches_plain_calls(ctx, autotune):
+def test_batch_matches_plain_calls(ctx, autotune, persistent):
     qs = qb.mixed_queries(24, seed=7, lo=4096, hi=1 << 18)
     plain = qb.run_plain(ctx, qs)
-    b = qb.Batch(qs, autotune=autotune)
+    b = qb.Batch(qs, autotune=autotune, persistent=persistent)
     try:
         for _ in range(2):  # replays give the same results
             for q in qs:
@@ -44,8 +45,12 @@ def test_batch_matches_plain_calls(ctx, autotune):
             for q, got, exp in zip(qs, qb.batch_results(qs), plain):
                 _same(q["op"], got, exp)
         info = b.info()
-        assert info["graph_nodes"] > len(qs) and info["replay_us"] > 0
-        assert info["hot_slots_log2"] in (12, 13) and info["join_table_factor"] in (2, 4)
+        assert info["replay_us"] > 0
+        if persistent:  # one persistent launch for the filters and group-bys; the joins beside it
+            assert info["hot_slots_log2"] in (13, 14) and info["graph_nodes"] < len(qs) * 5
+        else:
+            assert info["graph_nodes"] > len(qs) and info["hot_slots_log2"] in (12, 13)
+        assert info["join_table_factor"] in (2, 4)
     finally:
         b.close()
 
@@ -55,7 +60,7 @@ def test_batch_variants_are_bit_identical(ctx):
     plain = qb.run_plain(ctx, qs)
     for q in qs:
         q["variant"] = 1  # filter: bulk-copy ring; group-by: global table
-    b = qb.Batch(qs, autotune=False)
+    b = qb.Batch(qs, autotune=False, persistent=False)  # variants are the lanes form's
     try:
         b.run()
         b.check()
@@ -77,16 +82,18 @@ def test_batch_join_over_capacity_reports_error(ctx):
     ctx.check(ctx.lib.qg_ctx_check(ctx.handle), "qg_ctx_check")
 
 
+@pytest.mark.parametrize("persistent", [True, False])
 @pytest.mark.parametrize("lanes", [1, 3, 16])
-def test_batch_lanes_match_plain_calls(ctx, lanes):
+def test_batch_lanes_match_plain_calls(ctx, lanes, persistent):
     # The queries spread over `lanes` streams, each with a private context, in
-    # one fork/join graph: the same results whatever the number of lanes.
+    # one fork/join graph (persistent form: lane 0 runs the persistent kernel,
+    # the joins the others): the same results whatever the number of lanes.
     qs = qb.mixed_queries(20, seed=13, lo=4096, hi=1 << 18)
     plain = qb.run_plain(ctx, qs)
     lib = ctx.lib
     assert lib.qg_batch_set_lanes(lanes) == 0
     try:
-        b = qb.Batch(qs, autotune=False)
+        b = qb.Batch(qs, autotune=False, persistent=persistent)
         try:
             b.run()
             b.check()
@@ -105,7 +112,12 @@ def test_batch_queries_match_oracle(ctx, orc):
     # key, the join as a key-sorted multiset.
     qs = qb.mixed_queries(16, seed=23, lo=4096, hi=1 << 17)
     assert {q["op"] for q in qs} == {qb.OP_FILTER, qb.OP_GROUPBY, qb.OP_FUSED, qb.OP_JOIN}
-    b = qb.Batch(qs, autotune=False)
+    for persistent in (False, True):
+        _check_batch_against_oracle(qs, orc, persistent)
+
+
+def _check_batch_against_oracle(qs, orc, persistent):
+    b = qb.Batch(qs, autotune=False, persistent=persistent)
     try:
         b.run()
         b.check()
@@ -125,3 +137,81 @@ def test_batch_queries_match_oracle(ctx, orc):
                 _same(q["op"], got, tuple(torch.from_numpy(x) for x in exp))
     finally:
         b.close()
+
+
+def _query(op, key, val, val2=None, lo=0, hi=0, cap=None):
+    n = key.size
+    q = {"op": op, "n": n, "variant": -1, "lo": lo, "hi": hi, "count": torch.zeros(1, dtype=torch.int64, device="cuda")}
+    if op == qb.OP_FILTER:
+        q.update(inp=[torch.from_numpy(key).cuda(), torch.from_numpy(val).cuda()], n2=0, cap=n if cap is None else cap)
+        q["out"] = [torch.empty((max(q["cap"], 1), 2), dtype=torch.int32, device="cuda")]
+    else:
+        w = val2 if val2 is not None else np.zeros_like(key)
+        q.update(inp=[torch.from_numpy(key).cuda(), torch.from_numpy(val).cuda(), torch.from_numpy(w).cuda()],
+                 n2=0, cap=n if cap is None else cap)
+        q["out"] = [torch.empty(max(q["cap"], 1), dtype=t, device="cuda") for t in (torch.int32, torch.int64,
+                                                                                      torch.int64)]
+    return q
+
+
+def test_batch_persistent_edge_cases(ctx, orc):
+    # The persistent kernel's tiles and tails: 1 to 5 rows, a ragged last
+    # tile, key -1 (the shared table's empty mark, which goes to the L2 table)
+    # and INT_MIN, INT_MIN/INT_MAX values (int64 sums with carries), the fused
+    # predicate, a group count above the capacity (count reported, cap rows
+    # written), and filters at the range bounds; two replays.
+    rng = np.random.default_rng(99)
+    qs = []
+    for n in (1, 3, 5, 4097, 70001):
+        k = rng.choice(np.array([-1, 0, 7, -(2 ** 31), 2 ** 31 - 1], np.int64), n)
+        k = np.where(rng.random(n) < 0.5, k, rng.integers(0, 3000, n)).astype(np.int32)
+        v = rng.choice(np.array([-(2 ** 31), 2 ** 31 - 1, -1, 0, 999], np.int64), n).astype(np.int32)
+        w = rng.integers(0, 1000, n).astype(np.int32)
+        qs.append(_query(qb.OP_GROUPBY, k, v))
+        qs.append(_query(qb.OP_FUSED, k, v, w, -(2 ** 31), 499))
+        fk = rng.integers(-(2 ** 31), 2 ** 31, n, dtype=np.int64).astype(np.int32)
+        fk[0] = 100
+        qs.append(_query(qb.OP_FILTER, fk, rng.integers(0, 1000, n).astype(np.int32), lo=-5, hi=2 ** 30))
+    kk = np.arange(1500, dtype=np.int32)
+    qs.append(_query(qb.OP_GROUPBY, kk, kk, cap=1000))  # 1500 groups, room for 1000 (table of 2048)
+    b = qb.Batch(qs, autotune=False, persistent=True)
+    try:
+        for _ in range(2):
+            for q in qs:
+                q["count"].fill_(-1)
+            b.run()
+            b.check()
+            for q in qs:
+                i = [t.cpu().numpy() for t in q["inp"]]
+                m = int(q["count"].item())
+                if q["op"] == qb.OP_FILTER:
+                    exp = orc.filter_cols(i[0], i[1], q["lo"], q["hi"])
+                    assert m == exp.shape[0]
+                    assert np.array_equal(q["out"][0][:m].cpu().numpy(), exp)
+                    continue
+                v2 = i[2] if q["op"] == qb.OP_FUSED else None
+                ek, es, ec = orc.groupby_cols(i[0], i[1], v2, q["lo"], q["hi"])
+                assert m == ek.size
+                w = min(m, q["cap"])
+                gk, gs, gc = [t[:w].cpu().numpy() for t in q["out"]]
+                if w == m:
+                    o = np.argsort(gk.view(np.uint32), kind="stable")
+                    assert np.array_equal(gk[o], ek) and np.array_equal(gs[o], es) and np.array_equal(gc[o], ec)
+                else:  # the first cap groups written are genuine groups
+                    pos = np.searchsorted(ek.view(np.uint32), gk.view(np.uint32))
+                    assert np.array_equal(ek[pos], gk) and np.array_equal(es[pos], gs) and np.array_equal(ec[pos], gc)
+    finally:
+        b.close()
+
+
+def test_batch_persistent_table_overflow_reports_error(ctx):
+    # More groups than the query's table holds (2 x cap rounded up to a power
+    # of two): the persistent kernel records QG_ERR_TABLE_FULL, seen by the
+    # batch's eager run; ordinary calls are unaffected.
+    from query_on_opencl_fpga_gb300.api import QGError
+
+    kk = np.arange(20000, dtype=np.int32)
+    with pytest.raises(QGError) as e:
+        qb.Batch([_query(qb.OP_GROUPBY, kk, kk, cap=1000)], autotune=False, persistent=True)
+    assert e.value.status == 4
+    ctx.check(ctx.lib.qg_ctx_check(ctx.handle), "qg_ctx_check")
