@@ -248,26 +248,23 @@ def roofline(kern, name, bytes_per_launch, peak_gbs, traffic=None):
             "algorithmic_bytes_per_launch": bytes_per_launch}
 
 
-def cpu_baseline_groupby(d_host):
-    """The oracle port on all host threads over the full headline step (the same
-    work as the reference arm): two warm-up steps, then two timed steps.  The
-    columns are copied out of the pinned host buffers of the e2e run into
-    ordinary memory first, as the reference arm's inputs are."""
-    import numpy as np
-
-    from oracle import oracle as orc
-
-    orc.lib()
-    key, val, val2 = (np.array(d_host[k], copy=True) for k in ("key", "val", "val2"))
-    for _ in range(2):
-        cpu_groupby_step(key, val, val2)
-    reps = 2
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        cpu_groupby_step(key, val, val2)
-    dt = (time.perf_counter() - t0) / reps
-    return {"value": 2 * key.size / dt, "unit": "rows/s", "cores": orc.threads(), "kind": "port",
-            "sample": f"the full step ({key.size} rows x 2 operators), 2 warm-up + {reps} timed steps"}
+def cpu_baseline_groupby(reps=2):
+    """The oracle port on all host threads over the full headline step: the
+    reference arm's own code (`--impl reference`, 3 warm-up + `reps` timed steps)
+    in a fresh process, so that both CPU figures are taken the same way.  Run
+    inside this process, beside the GPU run's threads and pinned buffers, the
+    same steps measured about half the rate."""
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    out = subprocess.run([sys.executable, str(Path(__file__).resolve()), "--impl", "reference",
+                          "--steps", str(reps), "--warmup", "3"], capture_output=True, text=True, env=env,
+                         timeout=900)
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    if out.returncode != 0 or not lines:
+        raise RuntimeError(f"cpu baseline run failed (rc {out.returncode}): {out.stderr[-500:]}")
+    ref = json.loads(lines[-1])
+    cb = dict(ref["cpu_baseline"])
+    cb["sample"] = cb["sample"] + f", 3 warm-up + {reps} timed steps (a separate process running --impl reference)"
+    return cb
 
 
 def pinned_copy_rates(hkey, hval, hval2, dev, copy_streams, reps=5):
@@ -405,8 +402,7 @@ def run_ours(args, rank, world, local):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        host = {"key": hkey.numpy(), "val": hval.numpy(), "val2": hval2.numpy()}
-        cpu = cpu_baseline_groupby(host)
+        cpu = cpu_baseline_groupby()
 
     if rank == 0:
         line = {

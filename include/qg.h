@@ -179,11 +179,15 @@ QG_API qg_status qg_scatter_rec(qg_ctx *ctx, const void *R, int64_t rLen, const 
  * filter_aggregation pipeline, kernel/filter_aggregation/
  * filter_aggregation_cu_op_dp.cl).  Outputs hold `cap` groups; order is
  * QG_ORDER_KEY (ascending unsigned key, the reference's sorted order) or
- * QG_ORDER_NONE.  `cap` also sizes the spill partitions (about 1024 groups
- * each), so a cap near the true group count is fastest.  For key order the
- * context remembers the key range of its previous call and ranks keys in a
- * bitmap window placed there; results never depend on it, only the path
- * does (keys outside the window are sorted after the count).
+ * QG_ORDER_NONE.  By default the keys are first aggregated in a direct-indexed
+ * window of 2^22 keys placed on a sample's key range (output in key order
+ * either way); when the sample spans more than 2^21 keys or any row's key
+ * falls outside the window, the call runs the two-pass hash path instead.
+ * There `cap` also sizes the spill partitions (about 1024 groups each), so a
+ * cap near the true group count is fastest, and for key order the context
+ * remembers the key range of its previous call and ranks keys in a bitmap
+ * window placed there; results never depend on either, only the path does
+ * (keys outside the bitmap window are sorted after the count).
  * qg_groupby_cols_async is the same without a host round trip: the group
  * count goes to device memory (*d_num_groups); key order is sorted on the
  * device (two-pass path, cap < 2^30); a spill overflow is reported by
@@ -197,19 +201,23 @@ QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key, const in
                                        int32_t *gkey, int64_t *gsum, int64_t *gcount, int64_t cap,
                                        int order, int64_t *d_num_groups);
 
-/* Tuning of qg_groupby_cols (process-wide).  mode 0: two-pass shared-memory
- * aggregation with the global-table kernel as automatic fallback; mode 1:
- * global-table kernel only; mode 2: as 0 but the int64 sums use 64-bit shared
- * atomics instead of two 32-bit words with explicit carry (slower on GB300,
- * kept for comparison).  hot_slots_log2: per-SM shared-memory table
- * (8..13); partitions_log2: spill partitions (0 = chosen from cap, else
- * 1..13); bucket_cap: spill bucket capacity (0 = automatic; a small value
- * forces the fallback, for testing). */
+/* Tuning of qg_groupby_cols (process-wide).  mode 0 (default): the
+ * dense-window path, else two-pass shared-memory aggregation, with the
+ * global-table kernel as automatic fallback of the two-pass path; mode 1:
+ * global-table kernel only; mode 2: two-pass with the int64 sums as 64-bit
+ * shared atomics instead of two 32-bit words with explicit carry (slower on
+ * GB300, kept for comparison); mode 3: two-pass (no dense-window attempt).
+ * A context with a cost model attached (qg_steer_attach) may run another
+ * mode per call.  hot_slots_log2: the two-pass path's per-SM shared-memory
+ * table (8..13); partitions_log2: spill partitions (0 = chosen from cap,
+ * else 1..13); bucket_cap: spill bucket capacity (0 = automatic; a small
+ * value forces the fallback, for testing). */
 QG_API qg_status qg_groupby_set_knobs(int mode, int hot_slots_log2, int partitions_log2,
                                       uint32_t bucket_cap);
 /* Diagnostics of the context's last qg_groupby_cols call: out[0] = path
- * (0 two-pass, 1 global table), out[1] = overflow flags (bit 0 spill bucket,
- * bit 1 pass-2 table), out[2] = fullest spill bucket, out[3] = bucket capacity. */
+ * (0 two-pass, 1 global table, 2 dense window), out[1] = overflow flags
+ * (bit 0 spill bucket, bit 1 pass-2 table), out[2] = fullest spill bucket,
+ * out[3] = bucket capacity (the last three 0 on the dense-window path). */
 QG_API qg_status qg_groupby_stats(qg_ctx *ctx, uint32_t *out4);
 
 /* ---- hash join + filter + sort (config 2; kernel/hj_filter_sort/1/hj_filter_sort_op.cl)

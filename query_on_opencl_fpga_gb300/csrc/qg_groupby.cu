@@ -16,15 +16,17 @@
 //    predicate on a second column (configs 1 / 1-fused; the fused
 //    filter_aggregation image, kernel/filter_aggregation/
 //    filter_aggregation_cu_op_dp.cl).  Instead of sort -> label -> scan ->
-//    aggregate, rows are hashed: the default path is two passes (k_gb_part,
-//    k_gb_merge, section 2' below) -- per-SM shared-memory tables absorb the
-//    heavy hitters, the remaining rows are spilled into hash partitions and
-//    each partition is summed by one CTA in shared memory.  The single-pass
-//    global-table kernel (k_groupby_hash: shared-memory table + global
-//    open-addressing table of 32-byte {tag, sum, count} slots updated with
-//    atomicCAS / 64-bit atomicAdd) is the fallback for inputs that overflow
-//    the spill buckets.  QG_ORDER_KEY then sorts the groups by key (unsigned,
-//    the order groupByImpl's sorted array gives).
+//    aggregate, rows are aggregated in tables: the default path is the
+//    dense-window kernels of qg_gbdense.cu (keys within a 2^22-key window,
+//    emitted in key order).  Keys that do not fit a window take two passes
+//    (k_gb_part, k_gb_merge, section 2' below) -- per-SM shared-memory tables
+//    absorb the heavy hitters, the remaining rows are spilled into hash
+//    partitions and each partition is summed by one CTA in shared memory.
+//    The single-pass global-table kernel (k_groupby_hash: shared-memory table
+//    + global open-addressing table of 32-byte {tag, sum, count} slots
+//    updated with atomicCAS / 64-bit atomicAdd) is the fallback for inputs
+//    that overflow the spill buckets.  QG_ORDER_KEY then ranks or sorts the
+//    groups by key (unsigned, the order groupByImpl's sorted array gives).
 #include "qg_internal.cuh"
 #include "qg_sort.cuh"
 
@@ -350,7 +352,7 @@ __global__ void k_groupby_gather(const unsigned long long *__restrict__ rec, lon
 }
 
 // ---------------------------------------------------------------------------
-// 2'. two-pass column group-by (default path)
+// 2'. two-pass column group-by (keys that do not fit the dense window)
 //
 // Pass 1 (k_gb_part): one CTA per SM reads a contiguous slice of the rows.
 // Keys that find a place in the CTA's shared-memory table (the heavy
