@@ -82,88 +82,130 @@ constexpr int SF_THREADS = 256;
 constexpr int SF_WARPS = SF_THREADS / 32;
 constexpr int SF_ROUNDS = 4;  // int4 of keys + int4 of payloads per round: 4096 rows per tile
 
+// Radix partition function of the join over R's key range [kmin, kmax] with
+// up to 2^lb2 buckets: bucket = (k - kmin) >> shift.  The host and the
+// kernels that read the range from device memory derive it the same way.
+struct PjRadix {
+    int shift;
+    uint32_t nb;  // buckets in use: (kmax - kmin) >> shift, plus one
+};
+__host__ __device__ inline PjRadix pj_radix(uint32_t kmin, uint32_t kmax, int lb2) {
+    const uint32_t range = kmax - kmin;
+    int bits = 0;
+    while (bits < 32 && (range >> bits) != 0u) bits++;
+    const int shift = bits > lb2 ? bits - lb2 : 0;
+    return PjRadix{shift, (uint32_t)(((unsigned long long)range >> shift) + 1)};
+}
+
 // S-filter without input order: S' is repartitioned by key right after, and
 // the join leaves the order among equal keys unspecified, so a tile takes
 // its output range with one atomic on the S' counter instead of a look-back
 // over earlier tiles.  R's key range is read from device memory (no host
-// round trip before the launch).
+// round trip before the launch).  Persistent CTAs walk the tiles.  A tile's
+// selected rows are compacted into shared memory and written from there
+// with consecutive addresses; on the way out each is counted by the two
+// 8-bit digits of its radix bucket id in shared memory (the partition
+// passes' digit histograms, so S' is not read again to count them), added to
+// hist[0..512) once at the end.
 __global__ void __launch_bounds__(SF_THREADS, 4)
 k_pj_sfilter(const int32_t *__restrict__ skey, const int32_t *__restrict__ spay, long long n,
                int32_t slo, int32_t shi, const PjRange *__restrict__ range,
                unsigned long long *__restrict__ out, unsigned long long *__restrict__ cursor,
-               qg_control *ctl) {
+               qg_control *ctl, int lb2, uint32_t *__restrict__ hist) {
     constexpr int TILE = SF_THREADS * SF_ROUNDS * 4;
     __shared__ uint32_t s_woff[SF_ROUNDS * SF_WARPS];
     __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_cnt;
+    __shared__ uint32_t s_h[2][256];
+    __shared__ unsigned long long s_out[TILE];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const long long base = (long long)blockIdx.x * TILE;
     const uint32_t lt = qg_lanemask_lt();
-    int4 kv[SF_ROUNDS], pv[SF_ROUNDS];
-#pragma unroll
-    for (int r = 0; r < SF_ROUNDS; r++) {
-        const long long idx = base + (long long)(r * SF_THREADS + tid) * 4;
-        if (idx + 3 < n) {
-            kv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(skey + idx));
-            pv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(spay + idx));
-        } else {
-            int t[4] = {0, 0, 0, 0}, p[4] = {0, 0, 0, 0};
-            for (int j = 0; j < 4; j++)
-                if (idx + j < n) { t[j] = skey[idx + j]; p[j] = spay[idx + j]; }
-            kv[r] = make_int4(t[0], t[1], t[2], t[3]);
-            pv[r] = make_int4(p[0], p[1], p[2], p[3]);
-        }
-    }
+    for (int i = tid; i < 512; i += SF_THREADS) (&s_h[0][0])[i] = 0;
     const uint32_t kmin = range->kmin, kmax = range->kmax;
-    uint32_t fl = 0, lpre[SF_ROUNDS];
+    const PjRadix rp = pj_radix(kmin, kmax, lb2);
+    const bool two = rp.nb > 256u;  // the high digit is 0 for every row otherwise
+    const long long ntiles = (n + TILE - 1) / TILE;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long base = t * TILE;
+        int4 kv[SF_ROUNDS], pv[SF_ROUNDS];
 #pragma unroll
-    for (int r = 0; r < SF_ROUNDS; r++) {
-        const long long idx = base + (long long)(r * SF_THREADS + tid) * 4;
-        const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
-        const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
-        uint32_t f = 0;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const uint32_t u = (uint32_t)kk[j];
-            f |= (uint32_t)((idx + j < n) & (pp[j] >= slo) & (pp[j] <= shi) & (u >= kmin) & (u <= kmax)) << j;
-        }
-        uint32_t c = 0, tot = 0;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const uint32_t b = __ballot_sync(QG_FULL_MASK, (f >> j) & 1u);
-            c += __popc(b & lt);
-            tot += __popc(b);
-        }
-        lpre[r] = c;
-        if (lane == 0) s_woff[r * SF_WARPS + warp] = tot;
-        fl |= f << (4 * r);
-    }
-    __syncthreads();
-    if (warp == 0) {  // exclusive offsets of the tile's (round, warp) pieces; one atomic for the tile
-        const uint32_t x = s_woff[lane];  // SF_ROUNDS * SF_WARPS == 32
-        uint32_t inc = x;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t y = __shfl_up_sync(QG_FULL_MASK, inc, d);
-            if (lane >= d) inc += y;
-        }
-        s_woff[lane] = inc - x;
-        if (lane == 31) s_base = inc ? atomicAdd(cursor, (unsigned long long)inc) : 0ull;
-    }
-    __syncthreads();
-    const unsigned long long tb = s_base;
-#pragma unroll
-    for (int r = 0; r < SF_ROUNDS; r++) {
-        unsigned long long pos = tb + s_woff[r * SF_WARPS + warp] + lpre[r];
-        const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
-        const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-            if ((fl >> (4 * r + j)) & 1u) {
-                if (pos < (unsigned long long)n) out[pos] = ((unsigned long long)(uint32_t)kk[j] << 32) | (uint32_t)pp[j];
-                else qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_FILTER);
-                pos++;
+        for (int r = 0; r < SF_ROUNDS; r++) {
+            const long long idx = base + (long long)(r * SF_THREADS + tid) * 4;
+            if (idx + 3 < n) {
+                kv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(skey + idx));
+                pv[r] = qg_ldg_stream(reinterpret_cast<const int4 *>(spay + idx));
+            } else {
+                int tk[4] = {0, 0, 0, 0}, tp[4] = {0, 0, 0, 0};
+                for (int j = 0; j < 4; j++)
+                    if (idx + j < n) { tk[j] = skey[idx + j]; tp[j] = spay[idx + j]; }
+                kv[r] = make_int4(tk[0], tk[1], tk[2], tk[3]);
+                pv[r] = make_int4(tp[0], tp[1], tp[2], tp[3]);
             }
+        }
+        uint32_t fl = 0, lpre[SF_ROUNDS];
+#pragma unroll
+        for (int r = 0; r < SF_ROUNDS; r++) {
+            const long long idx = base + (long long)(r * SF_THREADS + tid) * 4;
+            const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
+            const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
+            uint32_t f = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint32_t u = (uint32_t)kk[j];
+                f |= (uint32_t)((idx + j < n) & (pp[j] >= slo) & (pp[j] <= shi) & (u >= kmin) & (u <= kmax)) << j;
+            }
+            uint32_t c = 0, tot = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const uint32_t bl = __ballot_sync(QG_FULL_MASK, (f >> j) & 1u);
+                c += __popc(bl & lt);
+                tot += __popc(bl);
+            }
+            lpre[r] = c;
+            if (lane == 0) s_woff[r * SF_WARPS + warp] = tot;
+            fl |= f << (4 * r);
+        }
+        __syncthreads();
+        if (warp == 0) {  // exclusive offsets of the tile's (round, warp) pieces; one atomic for the tile
+            const uint32_t x = s_woff[lane];  // SF_ROUNDS * SF_WARPS == 32
+            uint32_t inc = x;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(QG_FULL_MASK, inc, d);
+                if (lane >= d) inc += y;
+            }
+            s_woff[lane] = inc - x;
+            if (lane == 31) {
+                s_cnt = inc;
+                s_base = inc ? atomicAdd(cursor, (unsigned long long)inc) : 0ull;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < SF_ROUNDS; r++) {
+            uint32_t pos = s_woff[r * SF_WARPS + warp] + lpre[r];
+            const int32_t kk[4] = {kv[r].x, kv[r].y, kv[r].z, kv[r].w};
+            const int32_t pp[4] = {pv[r].x, pv[r].y, pv[r].z, pv[r].w};
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if ((fl >> (4 * r + j)) & 1u) s_out[pos++] = ((unsigned long long)(uint32_t)kk[j] << 32) | (uint32_t)pp[j];
+        }
+        __syncthreads();
+        const unsigned long long tb = s_base;
+        const uint32_t cnt = s_cnt;
+        for (uint32_t i = tid; i < cnt; i += SF_THREADS) {
+            const unsigned long long v = s_out[i];
+            if (tb + i < (unsigned long long)n) out[tb + i] = v;
+            else qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_FILTER);
+            const uint32_t bk = (uint32_t)((unsigned long long)((uint32_t)(v >> 32) - kmin) >> rp.shift);
+            atomicAdd(&s_h[0][bk & 255u], 1u);
+            if (two) atomicAdd(&s_h[1][(bk >> 8) & 255u], 1u);
+        }
+        __syncthreads();  // s_woff, s_base, s_cnt and s_out are rewritten by the next tile
     }
+    __syncthreads();
+    for (int i = tid; i < 512; i += SF_THREADS)
+        if ((&s_h[0][0])[i]) atomicAdd(&hist[i], (&s_h[0][0])[i]);
 }
 static_assert(SF_ROUNDS * SF_WARPS == 32, "one warp scans the tile's pieces");
 
@@ -174,12 +216,19 @@ static_assert(SF_ROUNDS * SF_WARPS == 32, "one warp scans the tile's pieces");
 constexpr int PJ_MAX_BUCKETS = 1 << 16;  // two 8-bit partition passes
 
 // Histograms of the two 8-bit digits of each row's bucket (shared-memory
-// privatised), for the partition passes' digit bases.
+// privatised), for the partition passes' digit bases.  With drange set (radix
+// only) the function comes from R's key range in device memory and lb2.
 template <bool LEARNED>
 __global__ void __launch_bounds__(256)
 k_pj_dhist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn pf, uint32_t nb,
-           uint32_t *__restrict__ hist, qg_control *ctl, uint16_t *__restrict__ bid) {
+           uint32_t *__restrict__ hist, qg_control *ctl, uint16_t *__restrict__ bid,
+           const PjRange *__restrict__ drange, int lb2) {
     __shared__ uint32_t h[2][256];
+    if (!LEARNED && drange) {
+        const PjRadix rp = pj_radix(drange->kmin, drange->kmax, lb2);
+        pf = qg_part_fn{0, drange->kmin, rp.shift, nullptr};
+        nb = rp.nb;
+    }
     // A learned function is evaluated from a shared-memory copy of the model.
     __shared__ __align__(16) unsigned char sm_model[LEARNED ? sizeof(qg_cdf_model) : 16];
     for (int i = threadIdx.x; i < 512; i += blockDim.x) (&h[0][0])[i] = 0;
@@ -702,6 +751,204 @@ struct PjMj {  // a bucket with several keys, joined by the sort-merge path
     uint32_t roff, soff;         // its rows in the gathered arrays
 };
 
+// Join groups from the fine bucket bounds, on the device.  Thread t of CTA c
+// packs the buckets of its segment (seg consecutive buckets) greedily:
+// consecutive buckets join the open group while it holds at most rmax R rows
+// and smax S' rows; a bucket above either limit is a group of its own,
+// handled outside the bucket kernel (big = 1) and listed in `over` (b = its
+// group) when both sides have rows.  A segment starts a new group, so no
+// group spans two segments.  The greedy walk runs twice: once to count each
+// segment's groups and listed buckets, then -- after the CTA's exclusive scan
+// of the counts -- to write them into the CTA's staging region (span =
+// PK_THREADS * seg entries per CTA); k_pj_place then moves every CTA's groups
+// to their final places.  Bounds are read 8 buckets at a time with 16-byte
+// loads, the next 8 in flight while these are walked (seg is a multiple of 8;
+// rbk and sbk hold at least nb + 16 entries).  Several CTAs share the
+// scattered reads, which bound this kernel on one SM.
+struct PjPackOut {
+    uint32_t groups, over;
+    unsigned long long over_rows;
+    uint32_t most, pad;
+};
+struct PjPackCta {  // one pack CTA's totals
+    uint32_t groups, over, most, pad;
+    unsigned long long over_rows;
+};
+constexpr int PK_THREADS = 128;
+constexpr int PK_SEG = 64;  // buckets per thread at most
+
+struct PkWalk {
+    uint32_t rmax, smax;
+    bool open = false;
+    uint32_t r0 = 0, s0 = 0, ng = 0, no = 0, most = 0;
+    unsigned long long orows = 0;
+    // write targets (null in the counting walk)
+    uint32_t *gr = nullptr, *gs = nullptr, *big = nullptr;
+    PjCross *over = nullptr;
+    uint32_t gb = 0, ob = 0;
+
+    __device__ void group(uint32_t re, uint32_t se, uint32_t b) {
+        if (gr) {
+            gr[gb + ng] = re;
+            gs[gb + ng] = se;
+            big[gb + ng] = b;
+        }
+        ng++;
+    }
+    __device__ void step(uint32_t rb, uint32_t re, uint32_t sb, uint32_t se) {
+        if (re - rb > rmax || se - sb > smax) {
+            if (open) { group(rb, sb, 0u); open = false; }
+            if (re > rb && se > sb) {
+                if (over) over[ob + no] = PjCross{ng, rb, re - rb, sb, se - sb};  // b: the CTA-local group
+                no++;
+                orows += (unsigned long long)(re - rb) + (se - sb);
+                most = max(most, max(re - rb, se - sb));
+            }
+            group(re, se, 1u);
+            return;
+        }
+        if (open && (re - r0 > rmax || se - s0 > smax)) { group(rb, sb, 0u); open = false; }
+        if (!open) { r0 = rb; s0 = sb; open = true; }
+    }
+};
+
+__device__ __forceinline__ void pk_load8(const uint32_t *p, uint32_t *v) {
+    const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(p));
+    const uint4 b = __ldcg(reinterpret_cast<const uint4 *>(p + 4));
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+__device__ void pk_walk(const uint32_t *__restrict__ rbk, const uint32_t *__restrict__ sbk, uint32_t b0,
+                        uint32_t b1, PkWalk &w) {
+    if (b0 >= b1) return;
+    uint32_t rv[8], sv[8];
+    pk_load8(rbk + b0, rv);
+    pk_load8(sbk + b0, sv);
+    for (uint32_t c = b0; c < b1; c += 8) {
+        uint32_t rn[8], sn[8];  // the next 8 starts (the first is this chunk's last end)
+        pk_load8(rbk + c + 8, rn);
+        pk_load8(sbk + c + 8, sn);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            if (c + j >= b1) break;
+            const uint32_t re = j < 7 ? rv[j + 1] : rn[0], se = j < 7 ? sv[j + 1] : sn[0];
+            w.step(rv[j], re, sv[j], se);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) { rv[j] = rn[j]; sv[j] = sn[j]; }
+    }
+    if (w.open) { w.group(rbk[b1], sbk[b1], 0u); w.open = false; }
+}
+
+__global__ void __launch_bounds__(PK_THREADS)
+k_pj_pack(const uint32_t *__restrict__ rbk, const uint32_t *__restrict__ sbk, uint32_t nb, uint32_t seg,
+          uint32_t rmax, uint32_t smax, uint32_t *__restrict__ tgr, uint32_t *__restrict__ tgs,
+          uint32_t *__restrict__ tbig, PjCross *__restrict__ tover, PjPackCta *__restrict__ cta) {
+    constexpr int W = PK_THREADS / 32;
+    __shared__ uint32_t s_g[W], s_o[W], s_m[W];
+    __shared__ unsigned long long s_r[W];
+    const uint32_t t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint32_t span = PK_THREADS * seg, cbase = blockIdx.x * span;
+    const uint32_t b0 = min(nb, cbase + t * seg), b1 = min(nb, b0 + seg);
+    PkWalk w;
+    w.rmax = rmax;
+    w.smax = smax;
+    pk_walk(rbk, sbk, b0, b1, w);
+    const uint32_t ng = w.ng, no = w.no;
+    uint32_t ig = ng, io = no;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t xg = __shfl_up_sync(QG_FULL_MASK, ig, d), xo = __shfl_up_sync(QG_FULL_MASK, io, d);
+        if (lane >= d) { ig += xg; io += xo; }
+    }
+    unsigned long long wr = w.orows;
+    uint32_t wm = w.most;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        wr += __shfl_xor_sync(QG_FULL_MASK, wr, d);
+        wm = max(wm, __shfl_xor_sync(QG_FULL_MASK, wm, d));
+    }
+    if (lane == 31) { s_g[warp] = ig; s_o[warp] = io; }
+    if (lane == 0) { s_r[warp] = wr; s_m[warp] = wm; }
+    __syncthreads();
+    uint32_t gw = 0, ow = 0;  // exclusive offsets of this warp
+    if (t == 0) {
+        uint32_t G = 0, O = 0, M = 0;
+        unsigned long long Rw = 0;
+        for (int i = 0; i < W; i++) {
+            G += s_g[i];
+            O += s_o[i];
+            M = max(M, s_m[i]);
+            Rw += s_r[i];
+        }
+        cta[blockIdx.x] = PjPackCta{G, O, M, 0u, Rw};
+    }
+    for (uint32_t i = 0; i < warp; i++) { gw += s_g[i]; ow += s_o[i]; }
+    PkWalk v;
+    v.rmax = rmax;
+    v.smax = smax;
+    v.gr = tgr;
+    v.gs = tgs;
+    v.big = tbig;
+    v.over = tover;
+    v.gb = cbase + gw + ig - ng;
+    v.ob = cbase + ow + io - no;
+    const uint32_t lg = gw + ig - ng;  // CTA-local index of this segment's first group
+    pk_walk(rbk, sbk, b0, b1, v);
+    // the listed buckets' group indices are segment-local so far: make them CTA-local
+    for (uint32_t j = 0; j < no; j++) tover[v.ob + j].b += lg;
+}
+
+// Moves each pack CTA's staged groups and listed buckets to their final
+// places (CTA c of this grid moves pack CTA c's): gr/gs[0 .. G] bound the
+// groups, big/bigcnt[0 .. G) describe them (bigcnt zeroed), `over` lists the
+// buckets handled outside, and *out gets the totals.
+__global__ void __launch_bounds__(256)
+k_pj_place(const uint32_t *__restrict__ rbk, const uint32_t *__restrict__ sbk, uint32_t nb, uint32_t span,
+           const uint32_t *__restrict__ tgr, const uint32_t *__restrict__ tgs, const uint32_t *__restrict__ tbig,
+           const PjCross *__restrict__ tover, const PjPackCta *__restrict__ cta, uint32_t *__restrict__ gr,
+           uint32_t *__restrict__ gs, uint32_t *__restrict__ big, unsigned long long *__restrict__ bigcnt,
+           PjCross *__restrict__ over, PjPackOut *__restrict__ out) {
+    const uint32_t c = blockIdx.x;
+    uint32_t gb = 0, ob = 0;
+    for (uint32_t i = 0; i < c; i++) { gb += cta[i].groups; ob += cta[i].over; }
+    const uint32_t ng = cta[c].groups, no = cta[c].over;
+    const uint32_t src = c * span;
+    for (uint32_t i = threadIdx.x; i < ng; i += blockDim.x) {
+        gr[gb + i + 1] = tgr[src + i];
+        gs[gb + i + 1] = tgs[src + i];
+        big[gb + i] = tbig[src + i];
+        bigcnt[gb + i] = 0ull;
+    }
+    for (uint32_t i = threadIdx.x; i < no; i += blockDim.x) {
+        PjCross e = tover[src + i];
+        e.b += gb;
+        over[ob + i] = e;
+    }
+    if (c == gridDim.x - 1 && threadIdx.x == 0) {
+        uint32_t most = 0;
+        unsigned long long rows = 0;
+        for (uint32_t i = 0; i < gridDim.x; i++) {
+            most = max(most, cta[i].most);
+            rows += cta[i].over_rows;
+        }
+        out->groups = gb + ng;
+        out->over = ob + no;
+        out->over_rows = rows;
+        out->most = most;
+        gr[0] = nb ? rbk[0] : 0u;
+        gs[0] = nb ? sbk[0] : 0u;
+    }
+}
+
+// Output rows of the cross-product buckets, for the bucket kernel's look-back.
+__global__ void k_pj_cross_cnt(const PjCross *__restrict__ list, uint32_t nlist,
+                               unsigned long long *__restrict__ bigcnt) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nlist; i += gridDim.x * blockDim.x)
+        bigcnt[list[i].b] = (unsigned long long)list[i].rn * list[i].sn;
+}
+
 // blockIdx.y walks the list (nlist entries) with stride gridDim.y.
 __global__ void k_pj_cross(const PjCross *__restrict__ list, uint32_t nlist, const unsigned long long *__restrict__ R,
                            const unsigned long long *__restrict__ S, const unsigned long long *__restrict__ off,
@@ -871,7 +1118,7 @@ constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit (and assess) t
 struct PjLevel {
     PjRange *range;
     uint32_t *dh;          // [side R, S'][digit 0, 1][256]
-    uint32_t *rbk, *sbk;   // [nb + 1] first row of each fine bucket
+    uint32_t *rbk, *sbk;   // [nb + 1] first row of each fine bucket (room for nb + 16)
     uint32_t *gr, *gs;     // [nb + 1] first row of each join group
     uint32_t *big, *mm;    // [nb] group handled outside the bucket kernel; [2 nb] key ranges
     uint32_t *scnt;        // [2 nb] sample counts under radix, learned
@@ -879,6 +1126,10 @@ struct PjLevel {
     PjCross *cross;
     PjMj *mj;
     unsigned long long *mjtot;  // matches of the sort-merge buckets
+    PjPackOut *pk;              // the packing's counts
+    PjPackCta *pkc;             // [nb / (PK_THREADS * 8) + 1] the pack CTAs' totals
+    uint32_t *tg;               // [3][nb + PK_THREADS * PK_SEG] the packing's staging (group ends, flags)
+    PjCross *tover;             // [nb + PK_THREADS * PK_SEG] the packing's staging (listed buckets)
     qg_cdf_model *model;             // learned model (top level only)
     uint32_t *heavy;                 // [1 + QG_CDF_MAX_HEAVY] heavy keys of the sample
     unsigned long long *smp, *smp2;  // key sample (top level only)
@@ -889,7 +1140,7 @@ size_t pj_level_bytes(uint32_t nb, bool learned) {
     auto add = [&](size_t x) { b += qg_align_up(x, 256); };
     add(sizeof(PjRange));
     add(4 * 256 * 4);
-    for (int i = 0; i < 4; i++) add((size_t)(nb + 1) * 4);
+    for (int i = 0; i < 4; i++) add((size_t)(nb + 16) * 4);  // the packing reads bounds 8 ahead
     add((size_t)nb * 4);
     add((size_t)2 * nb * 4);
     add((size_t)2 * nb * 4);
@@ -899,6 +1150,10 @@ size_t pj_level_bytes(uint32_t nb, bool learned) {
     add((size_t)nb * sizeof(PjCross));
     add((size_t)nb * sizeof(PjMj));
     add(8);
+    add(sizeof(PjPackOut));
+    add(((size_t)nb / (PK_THREADS * 8) + 1) * sizeof(PjPackCta));
+    add((size_t)3 * (nb + PK_THREADS * PK_SEG) * 4);
+    add((size_t)(nb + PK_THREADS * PK_SEG) * sizeof(PjCross));
     if (learned) {
         add(sizeof(qg_cdf_model));
         add((size_t)(1 + QG_CDF_MAX_HEAVY) * 4);
@@ -912,10 +1167,10 @@ void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     auto take = [&](size_t x) { char *q = p; p += qg_align_up(x, 256); return q; };
     L->range = (PjRange *)take(sizeof(PjRange));
     L->dh = (uint32_t *)take(4 * 256 * 4);
-    L->rbk = (uint32_t *)take((size_t)(nb + 1) * 4);
-    L->sbk = (uint32_t *)take((size_t)(nb + 1) * 4);
-    L->gr = (uint32_t *)take((size_t)(nb + 1) * 4);
-    L->gs = (uint32_t *)take((size_t)(nb + 1) * 4);
+    L->rbk = (uint32_t *)take((size_t)(nb + 16) * 4);
+    L->sbk = (uint32_t *)take((size_t)(nb + 16) * 4);
+    L->gr = (uint32_t *)take((size_t)(nb + 16) * 4);
+    L->gs = (uint32_t *)take((size_t)(nb + 16) * 4);
     L->big = (uint32_t *)take((size_t)nb * 4);
     L->mm = (uint32_t *)take((size_t)2 * nb * 4);
     L->scnt = (uint32_t *)take((size_t)2 * nb * 4);
@@ -925,6 +1180,10 @@ void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     L->cross = (PjCross *)take((size_t)nb * sizeof(PjCross));
     L->mj = (PjMj *)take((size_t)nb * sizeof(PjMj));
     L->mjtot = (unsigned long long *)take(8);
+    L->pk = (PjPackOut *)take(sizeof(PjPackOut));
+    L->pkc = (PjPackCta *)take(((size_t)nb / (PK_THREADS * 8) + 1) * sizeof(PjPackCta));
+    L->tg = (uint32_t *)take((size_t)3 * (nb + PK_THREADS * PK_SEG) * 4);
+    L->tover = (PjCross *)take((size_t)(nb + PK_THREADS * PK_SEG) * sizeof(PjCross));
     L->model = nullptr;
     L->heavy = nullptr;
     L->smp = L->smp2 = nullptr;
@@ -980,10 +1239,10 @@ qg_status pj_dhist(qg_ctx *ctx, const PjLevel &L, const qg_part_fn &pf, uint32_t
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 4 * 256 * 4, ctx->stream), "memset dhist");
     qg_pre_launch(ctx);
     auto kern = pf.learned ? k_pj_dhist<true> : k_pj_dhist<false>;
-    kern<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, pf, nb, L.dh, ctx->ctl, bid_r);
+    kern<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, pf, nb, L.dh, ctx->ctl, bid_r, nullptr, 0);
     QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     qg_pre_launch(ctx);
-    kern<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl, bid_s);
+    kern<<<pj_grid(ctx, nS, 256, 8), 256, 0, ctx->stream>>>(s, nS, pf, nb, L.dh + 512, ctx->ctl, bid_s, nullptr, 0);
     QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
     return qg_collect_error(ctx);  // synchronises: h is filled
@@ -1043,73 +1302,64 @@ qg_status pj_compare(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot,
     return QG_OK;
 }
 
-// Pinned host staging of one join's bucket bounds and group plan (grow-once:
-// sized for the largest bucket count).  The call ends with a stream sync, so
-// the next call may overwrite it.
-struct PjPlan {
-    uint32_t *rbk, *sbk;             // [nb + 1] first row of each fine bucket
-    uint32_t *gr, *gs;               // [G + 1] first row of each join group
-    uint32_t *big;                   // [G] 1: handled outside the bucket kernel
-    unsigned long long *bigcnt;      // [G] output rows of outside groups
+// Pinned host staging of one join's reads (grow-once, sized for the largest
+// bucket count): the digit histograms, the packing's counts, the list of
+// oversize buckets and their key ranges.  Every call ends with a stream sync,
+// so the next call may overwrite it.
+struct PjPin {
+    uint32_t h[1024];                 // [side R, S'][digit 0, 1][256]
+    PjPackOut pk;
+    PjCross over[PJ_MAX_BUCKETS];
+    uint32_t mm[2 * PJ_MAX_BUCKETS];  // [mins][maxes] of the listed buckets
 };
 
-qg_status pj_plan_host(qg_ctx *ctx, PjPlan *p) {
-    const size_t n = (size_t)PJ_MAX_BUCKETS + 2;
+qg_status pj_pin(qg_ctx *ctx, PjPin **out) {
     if (!ctx->pin_join) {
-        if (cudaMallocHost(&ctx->pin_join, n * (8 + 5 * 4)) != cudaSuccess) {
+        if (cudaMallocHost(&ctx->pin_join, sizeof(PjPin)) != cudaSuccess) {
             cudaGetLastError();
             ctx->pin_join = nullptr;
             return QG_ERR_OOM;
         }
     }
-    char *q = (char *)ctx->pin_join;
-    p->bigcnt = (unsigned long long *)q;
-    q += n * 8;
-    p->rbk = (uint32_t *)q;
-    p->sbk = p->rbk + n;
-    p->gr = p->sbk + n;
-    p->gs = p->gr + n;
-    p->big = p->gs + n;
+    *out = (PjPin *)ctx->pin_join;
     return QG_OK;
 }
 
-// Partition, join groups, outside buckets.  mem: the level's arrays
-// (pj_level_bytes), carved here.
-qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, long long nR,
-                  unsigned long long *s, unsigned long long *ssp, long long nS, uint32_t kmin,
-                  uint32_t kmax, int variant, uint32_t *ok, uint32_t *oa, uint32_t *ob, long long cap,
-                  long long *M_out, char *mem) {
+// Fine bucket count (a power of two, at most 2^16) for nR build rows and at
+// most nS probe rows: buckets of about a quarter of the bucket kernel's
+// capacity, which the packing then joins into groups.  It is taken from the
+// S row count before the filter, so that the filter can count the partition
+// digits of the rows it keeps.
+uint32_t pj_bucket_count(long long nR, long long nS) {
+    if (g_pj_blog2 > 0) return 1u << g_pj_blog2;
+    const long long ntot = nR + nS;
+    uint32_t nb = 1u;
+    while (nb < (uint32_t)PJ_MAX_BUCKETS &&
+           ((long long)nb * 1024 < ntot || (long long)nb * (g_pj_smax / 4) < nS || (long long)nb * (g_pj_rmax / 4) < nR))
+        nb <<= 1;
+    return nb;
+}
+
+// Partition, join groups, outside buckets.  L: the level's arrays (carved for
+// nb = 2^lb2 buckets); h: both sides' radix digit histograms, read with the
+// S' count.
+qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb2, unsigned long long *r,
+                  unsigned long long *rsp, long long nR, unsigned long long *s, unsigned long long *ssp,
+                  long long nS, uint32_t kmin, uint32_t kmax, int variant, uint32_t *ok, uint32_t *oa,
+                  uint32_t *ob, long long cap, long long *M_out) {
     *M_out = 0;
     if (nR == 0 || nS == 0) return QG_OK;
     QG_TRY(pj_attrs(ctx));
     const long long ntot = nR + nS;
-    // fine buckets of about a quarter of the bucket kernel's capacity (join
-    // groups pack several of them)
-    uint32_t nb = 1u;
-    if (g_pj_blog2 > 0) {
-        nb = 1u << g_pj_blog2;
-    } else {
-        while (nb < (uint32_t)PJ_MAX_BUCKETS &&
-               ((long long)nb * 1024 < ntot || (long long)nb * (g_pj_smax / 4) < nS ||
-                (long long)nb * (g_pj_rmax / 4) < nR))
-            nb <<= 1;
-    }
-    int lb2 = 0;
-    while ((1u << lb2) < nb) lb2++;
-    const uint32_t range = kmax - kmin;
-    const int bits = range ? 32 - __builtin_clz(range) : 0;
-    const int shift = bits > lb2 ? bits - lb2 : 0;
-    const uint32_t nb_radix = (uint32_t)(((unsigned long long)range >> shift) + 1);
+    const PjRadix rp = pj_radix(kmin, kmax, lb2);
+    const uint32_t nb_radix = rp.nb;
     const bool may_learn = variant != 1;
-    PjLevel L;
-    pj_level_carve(mem, nb, may_learn, &L);
-    const qg_part_fn radix{0, kmin, shift, nullptr};
+    const qg_part_fn radix{0, kmin, rp.shift, nullptr};
     const qg_part_fn learned{1, 0u, 0, L.model};
 
-    // radix digit histograms; a lopsided high digit means skew, and then a
-    // key sample decides whether the learned function spreads the rows better
-    uint32_t h[1024];
-    QG_TRY(pj_dhist(ctx, L, radix, nb_radix, r, nR, s, nS, h));
+    // A lopsided high digit of the radix histograms means skew, and then a key
+    // sample decides whether the learned function spreads the rows better.
+    uint32_t *h = pin->h;
     bool use_learned = may_learn && variant == 2;
     bool compared = false;
     if (may_learn && variant == 0 && ntot >= (1 << 16)) {
@@ -1161,89 +1411,66 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
                                   &in_b));
         if (in_b) std::swap(s, ssp);
     }
-    // fine bucket bounds
+    // fine bucket bounds, then the join groups packed on the device
     qg_pre_launch(ctx);
     k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(r, nR, pf, nbu, L.rbk);
     QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
     qg_pre_launch(ctx);
     k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(s, nS, pf, nbu, L.sbk);
     QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
-    PjPlan P;
-    QG_TRY(pj_plan_host(ctx, &P));
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(P.rbk, L.rbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "rbk d2h");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(P.sbk, L.sbk, (size_t)(nbu + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream), "sbk d2h");
+    // pack CTAs of PK_THREADS segments of seg buckets (seg <= PK_SEG, a multiple of 8)
+    const uint32_t nctas = (nbu + PK_THREADS * PK_SEG - 1) / (PK_THREADS * PK_SEG);
+    const uint32_t seg = ((nbu + PK_THREADS * nctas - 1) / (PK_THREADS * nctas) + 7) & ~7u;
+    const size_t tgn = (size_t)nb + PK_THREADS * PK_SEG;
+    qg_pre_launch(ctx);
+    k_pj_pack<<<nctas, PK_THREADS, 0, ctx->stream>>>(L.rbk, L.sbk, nbu, seg, g_pj_rmax, g_pj_smax, L.tg, L.tg + tgn,
+                                                     L.tg + 2 * tgn, L.tover, L.pkc);
+    QG_TRY(qg_check_launch(ctx, "k_pj_pack"));
+    qg_pre_launch(ctx);
+    k_pj_place<<<nctas, 256, 0, ctx->stream>>>(L.rbk, L.sbk, nbu, PK_THREADS * seg, L.tg, L.tg + tgn, L.tg + 2 * tgn,
+                                               L.tover, L.pkc, L.gr, L.gs, L.big, L.bigcnt, L.cross, L.pk);
+    QG_TRY(qg_check_launch(ctx, "k_pj_place"));
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(&pin->pk, L.pk, sizeof(PjPackOut), cudaMemcpyDeviceToHost, ctx->stream), "pack d2h");
     QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-
-    // Pack consecutive fine buckets into join groups up to the bucket
-    // kernel's capacity.  A bucket above it is a group of its own, handled
-    // outside the kernel (flag 1): listed in `over` when both sides have rows,
-    // an empty group otherwise.  The plan is written straight into pinned
-    // memory (one pass, no per-group allocation).
-    std::vector<PjCross> over;
-    uint32_t G = 0;
-    {
-        const uint32_t *R = P.rbk, *S = P.sbk;
-        const uint32_t rmax = g_pj_rmax, smax = g_pj_smax;
-        uint32_t r0 = 0, s0 = 0;  // first rows of the open group
-        bool open = false;
-        P.gr[0] = R[0];
-        P.gs[0] = S[0];
-        for (uint32_t b = 0; b < nbu; b++) {
-            const uint32_t rb = R[b], sb = S[b], re = R[b + 1], se = S[b + 1];
-            if (re - rb > rmax || se - sb > smax) {
-                if (open) {
-                    P.gr[G + 1] = rb; P.gs[G + 1] = sb; P.big[G] = 0; P.bigcnt[G] = 0; G++;
-                    open = false;
-                }
-                if (re > rb && se > sb) over.push_back(PjCross{G, rb, re - rb, sb, se - sb});
-                P.gr[G + 1] = re; P.gs[G + 1] = se; P.big[G] = 1; P.bigcnt[G] = 0; G++;
-                continue;
-            }
-            if (open && (re - r0 > rmax || se - s0 > smax)) {
-                P.gr[G + 1] = rb; P.gs[G + 1] = sb; P.big[G] = 0; P.bigcnt[G] = 0; G++;
-                open = false;
-            }
-            if (!open) { r0 = rb; s0 = sb; open = true; }
-        }
-        if (open) { P.gr[G + 1] = R[nbu]; P.gs[G + 1] = S[nbu]; P.big[G] = 0; P.bigcnt[G] = 0; G++; }
-    }
-    unsigned long long *bigcnt = P.bigcnt;
+    const PjPackOut pk = pin->pk;
+    const uint32_t G = pk.groups;
+    const uint32_t no = pk.over;
+    if (G == 0 || G > nbu || no > G) return QG_ERR_INVALID;  // cannot happen: G <= buckets
 
     // Outside groups: a bucket with one key is a cross product (k_pj_cross);
     // the others all go through the sort-merge path together (k_pj_mj_*).
     std::vector<PjCross> cross;
     std::vector<PjMj> mj;
     long long nrb = 0, nsb = 0;
-    if (!over.empty()) {
-        const size_t no = over.size();
-        std::vector<uint32_t> mm(2 * no);  // [mins][maxes]
-        uint32_t most = 0;
-        for (auto &e : over) most = max(most, max(e.rn, e.sn));
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, over.data(), no * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "list h2d");
-        QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mm, 0xff, no * 4, ctx->stream), "memset mins");
-        QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mm + no, 0, no * 4, ctx->stream), "memset maxes");
+    unsigned long long cross_rows = 0;  // output rows of the cross products
+    if (no > 0) {
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mm, 0xff, (size_t)no * 4, ctx->stream), "memset mins");
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mm + no, 0, (size_t)no * 4, ctx->stream), "memset maxes");
         qg_pre_launch(ctx);
-        k_pj_minmax<<<dim3((unsigned)pj_grid(ctx, (most + 3) / 4, 256, 4), (unsigned)std::min<size_t>(no, 65535)), 256, 0,
-                      ctx->stream>>>(L.cross, (uint32_t)no, r, s, L.mm, L.mm + no);
+        k_pj_minmax<<<dim3((unsigned)pj_grid(ctx, ((long long)pk.most + 3) / 4, 256, 4), (unsigned)std::min<uint32_t>(no, 65535)),
+                      256, 0, ctx->stream>>>(L.cross, no, r, s, L.mm, L.mm + no);
         QG_TRY(qg_check_launch(ctx, "k_pj_minmax"));
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(mm.data(), L.mm, mm.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "mm d2h");
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->over, L.cross, (size_t)no * sizeof(PjCross), cudaMemcpyDeviceToHost, ctx->stream), "list d2h");
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->mm, L.mm, (size_t)2 * no * 4, cudaMemcpyDeviceToHost, ctx->stream), "mm d2h");
         QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-        for (size_t i = 0; i < no; i++) {
-            const PjCross &e = over[i];
-            if (mm[i] == mm[no + i]) {
-                bigcnt[e.b] = (unsigned long long)e.rn * e.sn;
+        for (uint32_t i = 0; i < no; i++) {
+            const PjCross &e = pin->over[i];
+            if (pin->mm[i] == pin->mm[no + i]) {
                 cross.push_back(e);
+                cross_rows += (unsigned long long)e.rn * e.sn;
             } else {
                 mj.push_back(PjMj{e.b, e.rb, e.rn, e.sb, e.sn, (uint32_t)nrb, (uint32_t)nsb});
                 nrb += e.rn;
                 nsb += e.sn;
             }
         }
+        if (!cross.empty()) {  // their output counts, for the bucket kernel's look-back
+            QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, cross.data(), cross.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "cross h2d");
+            qg_pre_launch(ctx);
+            k_pj_cross_cnt<<<(unsigned)((cross.size() + 255) / 256), 256, 0, ctx->stream>>>(L.cross, (uint32_t)cross.size(), L.bigcnt);
+            QG_TRY(qg_check_launch(ctx, "k_pj_cross_cnt"));
+        }
     }
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gr, P.gr, (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gr h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.gs, P.gs, (size_t)(G + 1) * 4, cudaMemcpyHostToDevice, ctx->stream), "gs h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.big, P.big, (size_t)G * 4, cudaMemcpyHostToDevice, ctx->stream), "big h2d");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.bigcnt, P.bigcnt, (size_t)G * 8, cudaMemcpyHostToDevice, ctx->stream), "bigcnt h2d");
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.mjtot, 0, 8, ctx->stream), "memset mjtot");
 
     // sort-merge buckets: gather, sort by key, count each S row's matches
@@ -1287,7 +1514,6 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     k_pj_join<<<G, PB_THREADS, sizeof(PbSmem), ctx->stream>>>(args, lb);
     QG_TRY(qg_check_launch(ctx, "k_pj_join"));
     if (!cross.empty()) {
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(L.cross, cross.data(), cross.size() * sizeof(PjCross), cudaMemcpyHostToDevice, ctx->stream), "cross h2d");
         qg_pre_launch(ctx);
         k_pj_cross<<<dim3((unsigned)pj_grid(ctx, 1LL << 24, 256, 4), (unsigned)std::min<size_t>(cross.size(), 65535)),
                      256, 0, ctx->stream>>>(L.cross, (uint32_t)cross.size(), r, s, L.off, ok, oa, ob, cap);
@@ -1310,16 +1536,13 @@ qg_status pj_core(qg_ctx *ctx, unsigned long long *r, unsigned long long *rsp, l
     // when they alone could wrap it (a capacity error follows).
     *M_out = (long long)total;
     {
-        unsigned long long outside = (unsigned long long)ctx->pinned[1];
-        for (uint32_t g = 0; g < G; g++) outside += bigcnt[g];
+        const unsigned long long outside = (unsigned long long)ctx->pinned[1] + cross_rows;
         if (outside >= (1ull << 32)) *M_out = (long long)outside;
     }
     ctx->pj_stats[0] = use_learned ? 2 : 1;
     ctx->pj_stats[1] = nbu;
-    ctx->pj_stats[2] = (uint32_t)over.size();
-    long long orows = 0;
-    for (auto &e : over) orows += (long long)e.rn + e.sn;
-    ctx->pj_stats[3] = orows > 0xffffffffLL ? 0xffffffffu : (uint32_t)orows;
+    ctx->pj_stats[2] = no;
+    ctx->pj_stats[3] = pk.over_rows > 0xffffffffull ? 0xffffffffu : (uint32_t)pk.over_rows;
     ctx->pj_stats[4] = (uint32_t)mj.size();
     ctx->pj_stats[5] = 0;
     ctx->pj_stats[6] = 0;
@@ -1395,33 +1618,45 @@ static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const i
     const size_t rb = qg_align_up((size_t)nR * 8, 256), sb = qg_align_up((size_t)nS * 8, 256);
     char *aux;
     QG_TRY(qg_aux(ctx, 2 * rb + 2 * sb + pj_level_bytes(PJ_MAX_BUCKETS, true), &aux));
+    PjPin *pin;
+    QG_TRY(pj_pin(ctx, &pin));
     unsigned long long *R = (unsigned long long *)aux, *Rsp = (unsigned long long *)(aux + rb);
     unsigned long long *S = (unsigned long long *)(aux + 2 * rb), *Ssp = (unsigned long long *)(aux + 2 * rb + sb);
-    char *lvl = aux + 2 * rb + 2 * sb;
-    PjRange *range = (PjRange *)lvl;  // first member of the level-0 arrays
+    const uint32_t nb = pj_bucket_count(nR, nS);
+    int lb2 = 0;
+    while ((1u << lb2) < nb) lb2++;
+    PjLevel L;
+    pj_level_carve(aux + 2 * rb + 2 * sb, nb, variant != 1, &L);
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 4 * 256 * 4, ctx->stream), "memset dhist");
     qg_pre_launch(ctx);
-    k_pj_range_init<<<1, 1, 0, ctx->stream>>>(range);
+    k_pj_range_init<<<1, 1, 0, ctx->stream>>>(L.range);
     QG_TRY(qg_check_launch(ctx, "k_pj_range_init"));
     qg_pre_launch(ctx);
-    k_pj_rrec<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, R, range);
+    k_pj_rrec<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, R, L.range);
     QG_TRY(qg_check_launch(ctx, "k_pj_rrec"));
+    // S filter with the S' digit histograms of the radix function, then R's
     constexpr int SF_TILE = SF_THREADS * SF_ROUNDS * 4;
     const long long tiles = (nS + SF_TILE - 1) / SF_TILE;
     qg_pre_launch(ctx);
-    k_pj_sfilter<<<(unsigned)tiles, SF_THREADS, 0, ctx->stream>>>(skey, spay, nS, slo, shi, range, S,
-                                                                   &range->count, ctx->ctl);
+    k_pj_sfilter<<<(unsigned)std::min<long long>(tiles, (long long)ctx->sm_count * 4), SF_THREADS, 0, ctx->stream>>>(
+        skey, spay, nS, slo, shi, L.range, S, &L.range->count, ctx->ctl, lb2, L.dh + 512);
     QG_TRY(qg_check_launch(ctx, "k_pj_sfilter"));
-    // one read brings R's key range, the S' count and the error word
+    qg_pre_launch(ctx);
+    k_pj_dhist<false><<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(R, nR, qg_part_fn{0, 0u, 0, nullptr}, 0u,
+                                                                        L.dh, ctx->ctl, nullptr, L.range, lb2);
+    QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
+    // one read brings R's key range, the S' count, both sides' histograms and the error word
     static_assert(sizeof(PjRange) <= 2 * sizeof(long long), "two pinned slots");
     PjRange *hp = reinterpret_cast<PjRange *>(ctx->pinned + 4);
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(hp, range, sizeof(PjRange), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(hp, L.range, sizeof(PjRange), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
     QG_TRY(qg_collect_error(ctx));
     const PjRange hr = *hp;
     const long long ns1 = (long long)hr.count;
     long long M = 0;
     // pj_core ends with a read of the output count and the error word
-    QG_TRY(pj_core(ctx, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, variant, (uint32_t *)out_key,
-                   (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M, lvl));
+    QG_TRY(pj_core(ctx, L, pin, nb, lb2, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, variant, (uint32_t *)out_key,
+                   (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M));
     *out_n = M;
     return M > cap ? QG_ERR_CAPACITY : QG_OK;
 }
