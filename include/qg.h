@@ -242,8 +242,16 @@ QG_API qg_status qg_join_filter_sort(qg_ctx *ctx, const int32_t *rkey, const int
  * the reference has a single join kernel pair. */
 QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uint32_t bucket_s_max,
                                    uint32_t bucket_r_max);
+/* Dense build side (process-wide, on by default): when R's keys are unique
+ * and spread over at most 2 nR values, a presence bitmap and a payload table
+ * indexed by key - min(key) stand for R, so only S is partitioned (radix
+ * partitioning; an S bucket above the bucket kernel's capacity, or the learned
+ * function, takes the general path instead).  enable = 0 always takes the
+ * general path.  Results are identical. */
+QG_API qg_status qg_join_set_dense(int enable);
 /* Diagnostics of the context's last qg_join_filter_sort: out[0] path
- * (1 radix, 2 learned, 3 hash join + sort, 0 nothing to join), out[1]
+ * (1 radix, 2 learned, 3 hash join + sort, 4 radix with the dense build side,
+ * 0 nothing to join), out[1]
  * buckets, out[2] buckets handled outside the bucket kernel, out[3] their
  * rows, out[4] those of them with several keys (joined together by the
  * sort-merge path; the others are single-key cross products), out[5] knots

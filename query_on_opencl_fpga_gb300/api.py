@@ -310,11 +310,15 @@ class Context:
         self.check(self.lib.qg_join_set_knobs(variant, buckets_log2, bucket_s_max, bucket_r_max),
                    "qg_join_set_knobs")
 
+    def join_set_dense(self, enable: bool = True):
+        """Dense build side (unique R keys over a dense span) on or off; results are identical."""
+        self.check(self.lib.qg_join_set_dense(1 if enable else 0), "qg_join_set_dense")
+
     def join_stats(self) -> dict:
         """Path and partition diagnostics of the last join_filter_sort call."""
         out = (ctypes.c_uint32 * 8)()
         self.check(self.lib.qg_join_stats(self.handle, out), "qg_join_stats")
-        names = {0: "none", 1: "radix", 2: "learned", 3: "hash_sort"}
+        names = {0: "none", 1: "radix", 2: "learned", 3: "hash_sort", 4: "dense"}
         return {"path": names.get(out[0], str(out[0])), "buckets": out[1], "outside_buckets": out[2],
                 "outside_rows": out[3], "merge_buckets": out[4], "knots": out[5], "heavy_keys": out[6],
                 "auto_switched": out[7]}

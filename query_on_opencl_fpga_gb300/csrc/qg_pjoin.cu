@@ -49,6 +49,31 @@ struct PjRange {
     unsigned long long count;  // S' rows (step 2)
 };
 
+// Radix partition function of the join over R's key range [kmin, kmax] with
+// up to 2^lb2 buckets: bucket = (k - kmin) >> shift.  The host and the
+// kernels that read the range from device memory derive it the same way.
+struct PjRadix {
+    int shift;
+    uint32_t nb;  // buckets in use: (kmax - kmin) >> shift, plus one
+};
+__host__ __device__ inline PjRadix pj_radix(uint32_t kmin, uint32_t kmax, int lb2) {
+    const uint32_t range = kmax - kmin;
+    int bits = 0;
+    while (bits < 32 && (range >> bits) != 0u) bits++;
+    const int shift = bits > lb2 ? bits - lb2 : 0;
+    return PjRadix{shift, (uint32_t)(((unsigned long long)range >> shift) + 1)};
+}
+
+// Dense build side: R's keys unique and spread over at most 2 nR values,
+// with buckets of at most PJ_DENSE_BSPAN keys.  Then a presence bitmap and a
+// payload table indexed by key - kmin stand for R in key order, and R needs
+// no partitioning at all.
+constexpr uint32_t PJ_DENSE_BSPAN = 8192;
+__host__ __device__ inline bool pj_dense_span(uint32_t kmin, uint32_t kmax, int lb2, long long nR) {
+    const unsigned long long w = (unsigned long long)(kmax - kmin) + 1ull;
+    return w <= 2ull * (unsigned long long)nR && (1ull << pj_radix(kmin, kmax, lb2).shift) <= PJ_DENSE_BSPAN;
+}
+
 __global__ void k_pj_range_init(PjRange *r) {
     r->kmin = 0xffffffffu;
     r->kmax = 0;
@@ -75,6 +100,64 @@ k_pj_rrec(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
     }
 }
 
+// R's key range from the key column alone.
+__global__ void __launch_bounds__(256)
+k_pj_rrange(const int32_t *__restrict__ rkey, long long nR, PjRange *range) {
+    uint32_t lmin = 0xffffffffu, lmax = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += stride) {
+        const uint32_t k = (uint32_t)__ldg(rkey + i);
+        lmin = min(lmin, k);
+        lmax = max(lmax, k);
+    }
+    lmin = __reduce_min_sync(QG_FULL_MASK, lmin);
+    lmax = __reduce_max_sync(QG_FULL_MASK, lmax);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&range->kmin, lmin);
+        atomicMax(&range->kmax, lmax);
+    }
+}
+
+// R after its key range is known.  Dense span (pj_dense_span): the presence
+// bit of every key offset is set with atomicOr -- a bit found set already
+// means a duplicate key (flags[0] = 1) -- and T[offset] = payload; flags[1] =
+// 1.  Otherwise: R records (key << 32 | payload) and the two 8-bit digit
+// histograms of their radix bucket ids into hist[0 .. 512).
+__global__ void __launch_bounds__(256)
+k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, long long nR,
+          const PjRange *__restrict__ range, int lb2, uint32_t *__restrict__ bitmap, uint32_t *__restrict__ T,
+          uint32_t *__restrict__ flags, unsigned long long *__restrict__ rec, uint32_t *__restrict__ hist) {
+    __shared__ uint32_t h[2][256];
+    const uint32_t kmin = range->kmin, kmax = range->kmax;
+    const bool dense = pj_dense_span(kmin, kmax, lb2, nR);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    if (dense) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) flags[1] = 1u;
+        bool dup = false;
+        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += stride) {
+            const uint32_t off = (uint32_t)__ldg(rkey + i) - kmin;
+            const uint32_t bit = 1u << (off & 31u);
+            dup |= (atomicOr(&bitmap[off >> 5], bit) & bit) != 0u;
+            T[off] = (uint32_t)__ldg(rpay + i);
+        }
+        if (__any_sync(QG_FULL_MASK, dup) && (threadIdx.x & 31) == 0) flags[0] = 1u;
+        return;
+    }
+    for (int i = threadIdx.x; i < 512; i += blockDim.x) (&h[0][0])[i] = 0;
+    __syncthreads();
+    const PjRadix rp = pj_radix(kmin, kmax, lb2);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += stride) {
+        const uint32_t k = (uint32_t)__ldg(rkey + i);
+        rec[i] = ((unsigned long long)k << 32) | (uint32_t)__ldg(rpay + i);
+        const uint32_t bk = (uint32_t)((unsigned long long)(k - kmin) >> rp.shift);
+        atomicAdd(&h[0][bk & 255u], 1u);
+        atomicAdd(&h[1][(bk >> 8) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 512; i += blockDim.x)
+        if ((&h[0][0])[i]) atomicAdd(&hist[i], (&h[0][0])[i]);
+}
+
 // ---------------------------------------------------------------------------
 // 2. S filter + range test, compacted into S' records
 // ---------------------------------------------------------------------------
@@ -82,20 +165,6 @@ constexpr int SF_THREADS = 256;
 constexpr int SF_WARPS = SF_THREADS / 32;
 constexpr int SF_ROUNDS = 4;  // int4 of keys + int4 of payloads per round: 4096 rows per tile
 
-// Radix partition function of the join over R's key range [kmin, kmax] with
-// up to 2^lb2 buckets: bucket = (k - kmin) >> shift.  The host and the
-// kernels that read the range from device memory derive it the same way.
-struct PjRadix {
-    int shift;
-    uint32_t nb;  // buckets in use: (kmax - kmin) >> shift, plus one
-};
-__host__ __device__ inline PjRadix pj_radix(uint32_t kmin, uint32_t kmax, int lb2) {
-    const uint32_t range = kmax - kmin;
-    int bits = 0;
-    while (bits < 32 && (range >> bits) != 0u) bits++;
-    const int shift = bits > lb2 ? bits - lb2 : 0;
-    return PjRadix{shift, (uint32_t)(((unsigned long long)range >> shift) + 1)};
-}
 
 // S-filter without input order: S' is repartitioned by key right after, and
 // the join leaves the order among equal keys unspecified, so a tile takes
@@ -497,6 +566,7 @@ constexpr int PB_RMAX = 2048;  // R rows of a bucket
 constexpr int PB_HEADS_LOG2 = 12;
 constexpr int PB_HEADS = 1 << PB_HEADS_LOG2;
 constexpr int PB_CSPAN = 8192;  // widest key span that is counting-sorted
+static_assert(PB_CSPAN == (int)PJ_DENSE_BSPAN, "a dense group is counting-sorted");
 constexpr int PB_IPT = PB_SMAX / PB_THREADS;
 constexpr int PB_WSEG = PB_SMAX / PB_WARPS;  // sorted S' rows probed by one warp
 
@@ -738,6 +808,145 @@ k_pj_join(PbArgs a, qg_lookback lb) {
         }
     }
     qg_lb_finish(lb, b, gridDim.x - 1, S.epoch);
+}
+
+// Dense build side (pj_dense_span, unique keys): one CTA per join group,
+// tickets in group order.  A group is a key range [kmin + gk[g], kmin +
+// gk[g + 1]) of at most PB_CSPAN keys with its S' rows [gs[g], gs[g + 1]).
+// The S' rows are counting-sorted by key in shared memory; a row matches when
+// its key's presence bit is set, and then produces exactly one output row
+// (key, T[key - kmin], S.payload).  The group's match count is published and
+// its output offset found by decoupled look-back, as in k_pj_join; each warp
+// writes its rows' matches at consecutive output rows.
+struct PdSmem {
+    unsigned long long s[PB_SMAX];
+    uint32_t cnt[PB_CSPAN];
+    uint32_t wsum[PB_WARPS];
+    uint32_t tile, epoch, excl, pad;
+};
+
+struct PdArgs {
+    const unsigned long long *S;  // bucket-ordered S' records
+    const uint32_t *gk, *gs;      // [G + 1] first key offset and first S' row of each group
+    const uint32_t *bitmap;       // presence of each key offset
+    const uint32_t *T;            // R payload of each present key offset
+    uint32_t kmin;
+    unsigned long long *total;    // output rows (written by the last group)
+    uint32_t *out_k, *out_a, *out_b;
+    long long cap;
+};
+
+__global__ void __launch_bounds__(PB_THREADS, 2)
+k_pj_join_dense(PdArgs a, qg_lookback lb) {
+    extern __shared__ __align__(16) unsigned char pd_raw[];
+    PdSmem &S = *reinterpret_cast<PdSmem *>(pd_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    qg_lb_begin(lb, &S.tile, &S.epoch);
+    const uint32_t g = S.tile;
+    const uint32_t sb = a.gs[g], sn = a.gs[g + 1] - sb;
+    const uint32_t k0 = a.gk[g], span = a.gk[g + 1] - k0;
+    bool work = sn > 0 && span > 0;
+    if (work && (sn > (uint32_t)PB_SMAX || span > (uint32_t)PB_CSPAN)) {  // the packing keeps groups within both
+        if (tid == 0) qg_record_error(lb.ctl, QG_ERR_INVALID, QG_SITE_PJ_BUCKET);
+        work = false;
+    }
+    uint32_t my_cnt = 0;
+    uint32_t q = 0, r0 = 0;  // this warp's segment of sorted rows
+    if (work) {
+        const uint32_t base = a.kmin + k0;
+        unsigned long long it[PB_IPT];
+        uint32_t rk[PB_IPT];
+        for (uint32_t i = tid; i < span; i += PB_THREADS) S.cnt[i] = 0;
+#pragma unroll
+        for (int j = 0; j < PB_IPT; j++) {
+            const uint32_t i = j * PB_THREADS + tid;
+            it[j] = i < sn ? __ldg(a.S + sb + i) : 0ull;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PB_IPT; j++) {
+            const uint32_t i = j * PB_THREADS + tid;
+            if (i < sn) rk[j] = atomicAdd(&S.cnt[(uint32_t)(it[j] >> 32) - base], 1u);
+        }
+        __syncthreads();
+        constexpr int PER = PB_CSPAN / PB_THREADS;
+        const uint32_t c0 = tid * PER;
+        uint32_t loc[PER], sum = 0;
+#pragma unroll
+        for (int e = 0; e < PER; e++) {
+            loc[e] = (c0 + e < span) ? S.cnt[c0 + e] : 0u;
+            sum += loc[e];
+        }
+        uint32_t tot;
+        uint32_t run = pb_excl(sum, S.wsum, &tot);
+#pragma unroll
+        for (int e = 0; e < PER; e++) {
+            if (c0 + e < span) S.cnt[c0 + e] = run;
+            run += loc[e];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < PB_IPT; j++) {
+            const uint32_t i = j * PB_THREADS + tid;
+            if (i < sn) S.s[S.cnt[(uint32_t)(it[j] >> 32) - base] + rk[j]] = it[j];
+        }
+        __syncthreads();
+        r0 = min(sn, (uint32_t)warp * PB_WSEG);
+        q = min(sn, r0 + PB_WSEG) - r0;
+        for (uint32_t r = r0 + lane; r < r0 + q; r += 32) {
+            const uint32_t off = (uint32_t)(S.s[r] >> 32) - a.kmin;
+            my_cnt += (__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u;
+        }
+    }
+    // warp totals -> warp offsets within the group (pb_excl: every thread, uniformly)
+    const uint32_t wcnt = __reduce_add_sync(QG_FULL_MASK, my_cnt);
+    uint32_t total;
+    const uint32_t my_off = pb_excl(lane == 0 ? wcnt : 0u, S.wsum, &total);
+    const uint32_t warp_off = __shfl_sync(QG_FULL_MASK, my_off, 0);
+    if (warp == 0) {
+        const uint32_t excl = qg_lb_warp_exclusive(lb, g, S.epoch, total);
+        if (lane == 0) {
+            S.excl = excl;
+            if (g == gridDim.x - 1) *a.total = (unsigned long long)excl + total;
+        }
+    }
+    __syncthreads();
+    if (work && wcnt) {  // warp-uniform
+        long long o = (long long)S.excl + warp_off;
+        const uint32_t lt = qg_lanemask_lt();
+        for (uint32_t s0 = r0; s0 < r0 + q; s0 += 32) {
+            const uint32_t r = s0 + lane;
+            unsigned long long v = 0;
+            uint32_t off = 0;
+            bool hit = false;
+            if (r < r0 + q) {
+                v = S.s[r];
+                off = (uint32_t)(v >> 32) - a.kmin;
+                hit = ((__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u) != 0u;
+            }
+            const uint32_t bal = __ballot_sync(QG_FULL_MASK, hit);
+            if (hit) {
+                const long long oo = o + __popc(bal & lt);
+                if (oo < a.cap) {
+                    a.out_k[oo] = (uint32_t)(v >> 32);
+                    a.out_a[oo] = __ldg(a.T + off);
+                    a.out_b[oo] = (uint32_t)v;
+                }
+            }
+            o += __popc(bal);
+        }
+    }
+    qg_lb_finish(lb, g, gridDim.x - 1, S.epoch);
+}
+
+// Group bounds of the dense build side in key offsets: the buckets' first key
+// offsets min(b << shift, w) for b in [0, nb], where the packing reads an R
+// "row count" (its key span) per bucket.
+__global__ void k_pj_vbounds(uint32_t *__restrict__ rbk, uint32_t nb, int shift, unsigned long long w) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > nb) return;
+    const unsigned long long x = (unsigned long long)b << shift;
+    rbk[b] = (uint32_t)(x < w ? x : w);
 }
 
 // ---------------------------------------------------------------------------
@@ -1113,6 +1322,7 @@ namespace {
 int g_pj_variant = 0;  // 0 auto (radix; learned when a key sample shows that it spreads the rows better), 1 radix, 2 learned, 3 hash join + sort
 int g_pj_blog2 = 0;    // 0: fine bucket count from the input size
 uint32_t g_pj_smax = PB_SMAX, g_pj_rmax = PB_RMAX;
+bool g_pj_dense = true;  // the dense build side where it applies (unique R keys over a dense span)
 constexpr long long CDF_SAMPLE = 1 << 20;  // keys sampled to fit (and assess) the learned model
 
 struct PjLevel {
@@ -1127,6 +1337,7 @@ struct PjLevel {
     PjMj *mj;
     unsigned long long *mjtot;  // matches of the sort-merge buckets
     PjPackOut *pk;              // the packing's counts
+    uint32_t *dflags;           // [4] dense build side: [0] duplicate key seen, [1] dense span
     PjPackCta *pkc;             // [nb / (PK_THREADS * 8) + 1] the pack CTAs' totals
     uint32_t *tg;               // [3][nb + PK_THREADS * PK_SEG] the packing's staging (group ends, flags)
     PjCross *tover;             // [nb + PK_THREADS * PK_SEG] the packing's staging (listed buckets)
@@ -1151,6 +1362,7 @@ size_t pj_level_bytes(uint32_t nb, bool learned) {
     add((size_t)nb * sizeof(PjMj));
     add(8);
     add(sizeof(PjPackOut));
+    add(16);
     add(((size_t)nb / (PK_THREADS * 8) + 1) * sizeof(PjPackCta));
     add((size_t)3 * (nb + PK_THREADS * PK_SEG) * 4);
     add((size_t)(nb + PK_THREADS * PK_SEG) * sizeof(PjCross));
@@ -1181,6 +1393,7 @@ void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     L->mj = (PjMj *)take((size_t)nb * sizeof(PjMj));
     L->mjtot = (unsigned long long *)take(8);
     L->pk = (PjPackOut *)take(sizeof(PjPackOut));
+    L->dflags = (uint32_t *)take(16);
     L->pkc = (PjPackCta *)take(((size_t)nb / (PK_THREADS * 8) + 1) * sizeof(PjPackCta));
     L->tg = (uint32_t *)take((size_t)3 * (nb + PK_THREADS * PK_SEG) * 4);
     L->tover = (PjCross *)take((size_t)(nb + PK_THREADS * PK_SEG) * sizeof(PjCross));
@@ -1218,6 +1431,7 @@ qg_status pj_attrs(qg_ctx *ctx) {
     static bool done = false;
     if (!done) {
         QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PbSmem)), "attr join");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PdSmem)), "attr join dense");
         done = true;
     }
     return QG_OK;
@@ -1308,6 +1522,7 @@ qg_status pj_compare(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot,
 // so the next call may overwrite it.
 struct PjPin {
     uint32_t h[1024];                 // [side R, S'][digit 0, 1][256]
+    uint32_t dflags[4];
     PjPackOut pk;
     PjCross over[PJ_MAX_BUCKETS];
     uint32_t mm[2 * PJ_MAX_BUCKETS];  // [mins][maxes] of the listed buckets
@@ -1340,13 +1555,22 @@ uint32_t pj_bucket_count(long long nR, long long nS) {
     return nb;
 }
 
+// R's build side when R was not turned into records before the first read
+// (dense span): its records and radix digit histograms now (one more read).
+struct PjRSide {
+    const int32_t *rkey, *rpay;
+    bool rec_ready;       // R records (and h[0 .. 512)) exist
+    bool dense_ok;        // dense span, no duplicate key: bitmap and T describe R
+    const uint32_t *bitmap, *T;
+};
+
 // Partition, join groups, outside buckets.  L: the level's arrays (carved for
-// nb = 2^lb2 buckets); h: both sides' radix digit histograms, read with the
-// S' count.
-qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb2, unsigned long long *r,
-                  unsigned long long *rsp, long long nR, unsigned long long *s, unsigned long long *ssp,
-                  long long nS, uint32_t kmin, uint32_t kmax, int variant, uint32_t *ok, uint32_t *oa,
-                  uint32_t *ob, long long cap, long long *M_out) {
+// nb = 2^lb2 buckets); pin->h: the radix digit histograms of both sides (R's
+// only when R's records exist), read with the S' count.
+qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb2, PjRSide &rs,
+                  unsigned long long *r, unsigned long long *rsp, long long nR, unsigned long long *s,
+                  unsigned long long *ssp, long long nS, uint32_t kmin, uint32_t kmax, int variant, uint32_t *ok,
+                  uint32_t *oa, uint32_t *ob, long long cap, long long *M_out) {
     *M_out = 0;
     if (nR == 0 || nS == 0) return QG_OK;
     QG_TRY(pj_attrs(ctx));
@@ -1356,10 +1580,25 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
     const bool may_learn = variant != 1;
     const qg_part_fn radix{0, kmin, rp.shift, nullptr};
     const qg_part_fn learned{1, 0u, 0, L.model};
+    uint32_t *h = pin->h;
+    auto ensure_rrec = [&]() -> qg_status {
+        if (rs.rec_ready) return QG_OK;
+        QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 512 * 4, ctx->stream), "memset dhist");
+        qg_pre_launch(ctx);
+        k_pj_rrec<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rs.rkey, rs.rpay, nR, r, L.range);
+        QG_TRY(qg_check_launch(ctx, "k_pj_rrec"));
+        qg_pre_launch(ctx);
+        k_pj_dhist<false><<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(r, nR, radix, nb_radix, L.dh, ctx->ctl,
+                                                                            nullptr, nullptr, 0);
+        QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(h, L.dh, 512 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
+        QG_TRY(qg_collect_error(ctx));
+        rs.rec_ready = true;
+        return QG_OK;
+    };
 
     // A lopsided high digit of the radix histograms means skew, and then a key
     // sample decides whether the learned function spreads the rows better.
-    uint32_t *h = pin->h;
     bool use_learned = may_learn && variant == 2;
     bool compared = false;
     if (may_learn && variant == 0 && ntot >= (1 << 16)) {
@@ -1370,12 +1609,18 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
         if ((double)mx > 4.0 * (double)nS / (double)nbin) compared = true;
     }
     long long m = 0;
-    if (use_learned || compared) QG_TRY(pj_train(ctx, L, nb, r, nR, s, nS, &m));
+    if (use_learned || compared) {
+        QG_TRY(ensure_rrec());
+        QG_TRY(pj_train(ctx, L, nb, r, nR, s, nS, &m));
+    }
     if (compared) {
         double orad = 0, olrn = 0;
         QG_TRY(pj_compare(ctx, L, m, ntot, radix, nb_radix, learned, nb, &orad, &olrn));
         use_learned = olrn < 0.5 * orad;
     }
+    // Dense build side: only S' is partitioned, by the radix function.
+    bool dense = rs.dense_ok && !use_learned;
+    if (!dense) QG_TRY(ensure_rrec());
     // The learned function is evaluated once per row: its bucket ids go to a
     // sidecar that the partition passes carry along (ping-pong per side).
     uint16_t *bidr[2] = {nullptr, nullptr}, *bids[2] = {nullptr, nullptr};
@@ -1392,50 +1637,90 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
     const qg_part_fn &pf = use_learned ? learned : radix;
     const uint32_t nbu = use_learned ? nb : nb_radix;
 
-    // partition both sides by bucket (one or two stable 8-bit passes)
+    // partition a side by bucket (one or two stable 8-bit passes)
     const int npos = nbu > 256 ? 2 : (nbu > 1 ? 1 : 0);
-    if (npos > 0) {
+    auto partition = [&](bool side_r) -> qg_status {
+        if (npos == 0) return QG_OK;
         uint32_t hist[4 * QG_RADIX] = {0}, bases[4 * QG_RADIX];
-        int passes[4], np;
+        int passes[4];
         bool in_b = false;
-        memcpy(hist, h, 512 * 4);
-        np = qg_sort_plan(hist, npos, nR, passes, bases);
-        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{r, nullptr, nullptr, nullptr, bidr[0]},
-                                  qg_sort_bufs{rsp, nullptr, nullptr, nullptr, bidr[1]}, nR, pf, passes, np, bases,
+        memcpy(hist, h + (side_r ? 0 : 512), 512 * 4);
+        const long long n = side_r ? nR : nS;
+        const int np = qg_sort_plan(hist, npos, n, passes, bases);
+        unsigned long long *&a = side_r ? r : s, *&bb = side_r ? rsp : ssp;
+        uint16_t **bid = side_r ? bidr : bids;
+        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{a, nullptr, nullptr, nullptr, bid[0]},
+                                  qg_sort_bufs{bb, nullptr, nullptr, nullptr, bid[1]}, n, pf, passes, np, bases,
                                   &in_b));
-        if (in_b) std::swap(r, rsp);
-        memcpy(hist, h + 512, 512 * 4);
-        np = qg_sort_plan(hist, npos, nS, passes, bases);
-        QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{s, nullptr, nullptr, nullptr, bids[0]},
-                                  qg_sort_bufs{ssp, nullptr, nullptr, nullptr, bids[1]}, nS, pf, passes, np, bases,
-                                  &in_b));
-        if (in_b) std::swap(s, ssp);
-    }
-    // fine bucket bounds, then the join groups packed on the device
-    qg_pre_launch(ctx);
-    k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(r, nR, pf, nbu, L.rbk);
-    QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
+        if (in_b) std::swap(a, bb);
+        return QG_OK;
+    };
+    // fine bucket bounds, then the join groups packed on the device (one read of the counts)
+    auto pack = [&](uint32_t rmax, PjPackOut *pk) -> qg_status {
+        const uint32_t nctas = (nbu + PK_THREADS * PK_SEG - 1) / (PK_THREADS * PK_SEG);
+        const uint32_t seg = ((nbu + PK_THREADS * nctas - 1) / (PK_THREADS * nctas) + 7) & ~7u;
+        const size_t tgn = (size_t)nb + PK_THREADS * PK_SEG;
+        qg_pre_launch(ctx);
+        k_pj_pack<<<nctas, PK_THREADS, 0, ctx->stream>>>(L.rbk, L.sbk, nbu, seg, rmax, g_pj_smax, L.tg, L.tg + tgn,
+                                                         L.tg + 2 * tgn, L.tover, L.pkc);
+        QG_TRY(qg_check_launch(ctx, "k_pj_pack"));
+        qg_pre_launch(ctx);
+        k_pj_place<<<nctas, 256, 0, ctx->stream>>>(L.rbk, L.sbk, nbu, PK_THREADS * seg, L.tg, L.tg + tgn,
+                                                   L.tg + 2 * tgn, L.tover, L.pkc, L.gr, L.gs, L.big, L.bigcnt,
+                                                   L.cross, L.pk);
+        QG_TRY(qg_check_launch(ctx, "k_pj_place"));
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(&pin->pk, L.pk, sizeof(PjPackOut), cudaMemcpyDeviceToHost, ctx->stream), "pack d2h");
+        QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+        *pk = pin->pk;
+        if (pk->groups == 0 || pk->groups > nbu || pk->over > pk->groups) return QG_ERR_INVALID;  // G <= buckets
+        return QG_OK;
+    };
+    auto r_bounds = [&]() -> qg_status {
+        qg_pre_launch(ctx);
+        k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(r, nR, pf, nbu, L.rbk);
+        return qg_check_launch(ctx, "k_pj_bounds");
+    };
+    QG_TRY(partition(false));
+    if (!dense) QG_TRY(partition(true));
     qg_pre_launch(ctx);
     k_pj_bounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(s, nS, pf, nbu, L.sbk);
     QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
-    // pack CTAs of PK_THREADS segments of seg buckets (seg <= PK_SEG, a multiple of 8)
-    const uint32_t nctas = (nbu + PK_THREADS * PK_SEG - 1) / (PK_THREADS * PK_SEG);
-    const uint32_t seg = ((nbu + PK_THREADS * nctas - 1) / (PK_THREADS * nctas) + 7) & ~7u;
-    const size_t tgn = (size_t)nb + PK_THREADS * PK_SEG;
-    qg_pre_launch(ctx);
-    k_pj_pack<<<nctas, PK_THREADS, 0, ctx->stream>>>(L.rbk, L.sbk, nbu, seg, g_pj_rmax, g_pj_smax, L.tg, L.tg + tgn,
-                                                     L.tg + 2 * tgn, L.tover, L.pkc);
-    QG_TRY(qg_check_launch(ctx, "k_pj_pack"));
-    qg_pre_launch(ctx);
-    k_pj_place<<<nctas, 256, 0, ctx->stream>>>(L.rbk, L.sbk, nbu, PK_THREADS * seg, L.tg, L.tg + tgn, L.tg + 2 * tgn,
-                                               L.tover, L.pkc, L.gr, L.gs, L.big, L.bigcnt, L.cross, L.pk);
-    QG_TRY(qg_check_launch(ctx, "k_pj_place"));
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(&pin->pk, L.pk, sizeof(PjPackOut), cudaMemcpyDeviceToHost, ctx->stream), "pack d2h");
-    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
-    const PjPackOut pk = pin->pk;
+    PjPackOut pk;
+    if (dense) {
+        // a group's "R rows" are its key span, at most a counting sort's
+        qg_pre_launch(ctx);
+        k_pj_vbounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(L.rbk, nbu, rp.shift,
+                                                                (unsigned long long)(kmax - kmin) + 1ull);
+        QG_TRY(qg_check_launch(ctx, "k_pj_vbounds"));
+        QG_TRY(pack(PJ_DENSE_BSPAN, &pk));
+        if (pk.over > 0) {  // an S' bucket above the bucket kernel's capacity: R's records after all
+            dense = false;
+            QG_TRY(ensure_rrec());
+            QG_TRY(partition(true));
+            QG_TRY(r_bounds());
+            QG_TRY(pack(g_pj_rmax, &pk));
+        }
+    } else {
+        QG_TRY(r_bounds());
+        QG_TRY(pack(g_pj_rmax, &pk));
+    }
     const uint32_t G = pk.groups;
     const uint32_t no = pk.over;
-    if (G == 0 || G > nbu || no > G) return QG_ERR_INVALID;  // cannot happen: G <= buckets
+    if (dense) {
+        qg_lookback lb;
+        QG_TRY(qg_lb_make(ctx, G, QG_SITE_JOIN_PROBE, &lb));
+        PdArgs da{s, L.gr, L.gs, rs.bitmap, rs.T, kmin, L.total, ok, oa, ob, cap};
+        qg_pre_launch(ctx);
+        k_pj_join_dense<<<G, PB_THREADS, sizeof(PdSmem), ctx->stream>>>(da, lb);
+        QG_TRY(qg_check_launch(ctx, "k_pj_join_dense"));
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
+        QG_TRY(qg_collect_error(ctx));
+        *M_out = ctx->pinned[0];
+        ctx->pj_stats[0] = 4;
+        ctx->pj_stats[1] = nbu;
+        for (int i = 2; i < 8; i++) ctx->pj_stats[i] = 0;
+        return QG_OK;
+    }
 
     // Outside groups: a bucket with one key is a cross product (k_pj_cross);
     // the others all go through the sort-merge path together (k_pj_mj_*).
@@ -1568,6 +1853,12 @@ extern "C" QG_API qg_status qg_join_set_knobs(int variant, int buckets_log2, uin
     return QG_OK;
 }
 
+extern "C" QG_API qg_status qg_join_set_dense(int enable) {
+    if (enable != 0 && enable != 1) return QG_ERR_INVALID;
+    g_pj_dense = enable != 0;
+    return QG_OK;
+}
+
 extern "C" QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8) {
     if (!ctx || !out8) return QG_ERR_INVALID;
     memcpy(out8, ctx->pj_stats, sizeof(ctx->pj_stats));
@@ -1614,49 +1905,58 @@ static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const i
     *out_n = 0;
     memset(ctx->pj_stats, 0, sizeof(ctx->pj_stats));
     if (nR == 0 || nS == 0) return QG_OK;
-    // aux: R records + spare, S' records + spare, level-0 arrays
+    // aux: R records + spare (the spare doubles as the dense build side's
+    // payload table), S' records + spare, the presence bitmap, level-0 arrays
     const size_t rb = qg_align_up((size_t)nR * 8, 256), sb = qg_align_up((size_t)nS * 8, 256);
+    const size_t bmb = qg_align_up(((size_t)2 * nR + 63) / 32 * 4, 256);
     char *aux;
-    QG_TRY(qg_aux(ctx, 2 * rb + 2 * sb + pj_level_bytes(PJ_MAX_BUCKETS, true), &aux));
+    QG_TRY(qg_aux(ctx, 2 * rb + 2 * sb + bmb + pj_level_bytes(PJ_MAX_BUCKETS, true), &aux));
     PjPin *pin;
     QG_TRY(pj_pin(ctx, &pin));
     unsigned long long *R = (unsigned long long *)aux, *Rsp = (unsigned long long *)(aux + rb);
     unsigned long long *S = (unsigned long long *)(aux + 2 * rb), *Ssp = (unsigned long long *)(aux + 2 * rb + sb);
+    uint32_t *bitmap = (uint32_t *)(aux + 2 * rb + 2 * sb);
     const uint32_t nb = pj_bucket_count(nR, nS);
     int lb2 = 0;
     while ((1u << lb2) < nb) lb2++;
     PjLevel L;
-    pj_level_carve(aux + 2 * rb + 2 * sb, nb, variant != 1, &L);
+    pj_level_carve(aux + 2 * rb + 2 * sb + bmb, nb, variant != 1, &L);
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 4 * 256 * 4, ctx->stream), "memset dhist");
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dflags, 0, 16, ctx->stream), "memset flags");
+    QG_TRY_CUDA(ctx, cudaMemsetAsync(bitmap, 0, bmb, ctx->stream), "memset bitmap");
     qg_pre_launch(ctx);
     k_pj_range_init<<<1, 1, 0, ctx->stream>>>(L.range);
     QG_TRY(qg_check_launch(ctx, "k_pj_range_init"));
     qg_pre_launch(ctx);
-    k_pj_rrec<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, R, L.range);
-    QG_TRY(qg_check_launch(ctx, "k_pj_rrec"));
-    // S filter with the S' digit histograms of the radix function, then R's
+    k_pj_rrange<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, nR, L.range);
+    QG_TRY(qg_check_launch(ctx, "k_pj_rrange"));
+    // R: presence bitmap + payload table (dense span), else records + digit histograms
+    qg_pre_launch(ctx);
+    k_pj_rtab<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, L.range, lb2, bitmap,
+                                                                 (uint32_t *)Rsp, L.dflags, R, L.dh);
+    QG_TRY(qg_check_launch(ctx, "k_pj_rtab"));
+    // S filter with the S' digit histograms of the radix function
     constexpr int SF_TILE = SF_THREADS * SF_ROUNDS * 4;
     const long long tiles = (nS + SF_TILE - 1) / SF_TILE;
     qg_pre_launch(ctx);
     k_pj_sfilter<<<(unsigned)std::min<long long>(tiles, (long long)ctx->sm_count * 4), SF_THREADS, 0, ctx->stream>>>(
         skey, spay, nS, slo, shi, L.range, S, &L.range->count, ctx->ctl, lb2, L.dh + 512);
     QG_TRY(qg_check_launch(ctx, "k_pj_sfilter"));
-    qg_pre_launch(ctx);
-    k_pj_dhist<false><<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(R, nR, qg_part_fn{0, 0u, 0, nullptr}, 0u,
-                                                                        L.dh, ctx->ctl, nullptr, L.range, lb2);
-    QG_TRY(qg_check_launch(ctx, "k_pj_dhist"));
-    // one read brings R's key range, the S' count, both sides' histograms and the error word
+    // one read brings R's key range, the S' count, the histograms, the dense flags and the error word
     static_assert(sizeof(PjRange) <= 2 * sizeof(long long), "two pinned slots");
     PjRange *hp = reinterpret_cast<PjRange *>(ctx->pinned + 4);
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(hp, L.range, sizeof(PjRange), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->dflags, L.dflags, 16, cudaMemcpyDeviceToHost, ctx->stream), "flags d2h");
     QG_TRY(qg_collect_error(ctx));
     const PjRange hr = *hp;
     const long long ns1 = (long long)hr.count;
+    PjRSide rs{rkey, rpay, pin->dflags[1] == 0u, pin->dflags[1] != 0u && pin->dflags[0] == 0u && g_pj_dense,
+               bitmap, (const uint32_t *)Rsp};
     long long M = 0;
     // pj_core ends with a read of the output count and the error word
-    QG_TRY(pj_core(ctx, L, pin, nb, lb2, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, variant, (uint32_t *)out_key,
-                   (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M));
+    QG_TRY(pj_core(ctx, L, pin, nb, lb2, rs, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, variant,
+                   (uint32_t *)out_key, (uint32_t *)out_rpay, (uint32_t *)out_spay, cap, &M));
     *out_n = M;
     return M > cap ? QG_ERR_CAPACITY : QG_OK;
 }

@@ -66,6 +66,7 @@ def test_join_config2_full_size(ctx):
     d = datagen.config2_join(1 << 24, 1 << 28, seed=0, device="cuda")
     ok, orp, osp = ctx.join_filter_sort(d["rkey"], d["rpay"], d["skey"], d["spay"], d["slo"], d["shi"],
                                         cap=70_000_000)
+    assert ctx.join_stats()["path"] == "dense"  # R's keys are a permutation of [0, 2^24)
     m = (d["spay"] <= 299) & (d["skey"] < (1 << 24))
     assert ok.numel() == int(m.sum())
     assert bool((ok[1:] >= ok[:-1]).all())

@@ -194,3 +194,73 @@ def test_join_config4_full_size(ctx, knobs, variant):
     del sk, ss
     g = torch.sort(gu * 1024 + osp.long()).values
     assert torch.equal(e, g)
+
+
+@pytest.fixture
+def dense_knob(ctx):
+    yield ctx.join_set_dense
+    ctx.join_set_dense(True)
+
+
+@pytest.mark.parametrize("nR,nS,gap,base", [
+    (1, 5, 1, 7),
+    (1000, 50000, 1, 0),
+    (1 << 16, 1 << 20, 1, 1000),
+    (1 << 16, 1 << 20, 2, -(1 << 20)),      # every other key, all negative (one unsigned span)
+    (50000, 3 << 20, 1, (1 << 31) - 25000),  # keys across 0x7fffffff / 0x80000000 (unsigned order)
+])
+def test_join_dense_build_side(ctx, orc, knobs, dense_knob, nR, nS, gap, base):
+    # Unique R keys over a dense span: R becomes a presence bitmap and a payload
+    # table indexed by key - min, and only S is partitioned.  Equal to the
+    # oracle, to the general path (dense build side off) and to the learned
+    # partitioning (which takes the general path).
+    rng = np.random.default_rng(nR + nS + gap)
+    rk = (rng.permutation(nR).astype(np.int64) * gap + base)
+    rkey = ((rk + (1 << 31)) % (1 << 32) - (1 << 31)).astype(np.int32)
+    rpay = rng.integers(-1000, 1000, nR).astype(np.int32)
+    sk = rng.integers(base - 300, base + nR * gap + 300, nS)
+    skey = ((sk + (1 << 31)) % (1 << 32) - (1 << 31)).astype(np.int32)
+    spay = rng.integers(0, 1000, nS).astype(np.int32)
+    skey[0], spay[0] = rkey[0], 0  # at least one S row passes the filters
+    exp = orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 299, cap=nS + 16, mt=True)
+    args = [dev(a) for a in (rkey, rpay, skey, spay)]
+    check_join(ctx.join_filter_sort(*args, -(2 ** 31), 299), exp)
+    assert ctx.join_stats()["path"] == "dense"
+    dense_knob(False)
+    check_join(ctx.join_filter_sort(*args, -(2 ** 31), 299), exp)
+    assert ctx.join_stats()["path"] == "radix"
+    dense_knob(True)
+    knobs(2)
+    check_join(ctx.join_filter_sort(*args, -(2 ** 31), 299), exp)
+    assert ctx.join_stats()["path"] == "learned"
+
+
+def test_join_dense_span_duplicate_key_takes_general_path(ctx, orc):
+    # A dense span with one key twice: the bitmap sees the duplicate, and the
+    # general path (R records after all) joins both build rows.
+    rng = np.random.default_rng(21)
+    rkey = rng.permutation(20000).astype(np.int32)
+    rkey[5] = rkey[6]
+    rpay = rng.integers(0, 1000, rkey.size).astype(np.int32)
+    skey = rng.integers(-10, 20010, 300000).astype(np.int32)
+    spay = rng.integers(0, 1000, skey.size).astype(np.int32)
+    got = ctx.join_filter_sort(dev(rkey), dev(rpay), dev(skey), dev(spay), -(2 ** 31), 299)
+    assert ctx.join_stats()["path"] == "radix"
+    check_join(got, orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 299, cap=skey.size * 2, mt=True))
+
+
+def test_join_dense_oversize_bucket_falls_back(ctx, orc):
+    # Unique R keys over a dense span, but one S key holds 200K rows: its
+    # bucket exceeds the bucket kernel, so R's records are made after all and
+    # the general path (with its outside buckets) finishes the join.
+    rng = np.random.default_rng(22)
+    nR = 1 << 16
+    rkey = rng.permutation(nR).astype(np.int32)
+    rpay = rng.integers(0, 1000, nR).astype(np.int32)
+    skey = np.concatenate([rng.integers(0, nR, 1 << 20), np.full(200000, 4321)]).astype(np.int32)
+    rng.shuffle(skey)
+    spay = rng.integers(0, 1000, skey.size).astype(np.int32)
+    got = ctx.join_filter_sort(dev(rkey), dev(rpay), dev(skey), dev(spay), -(2 ** 31), 299)
+    st = ctx.join_stats()
+    assert st["path"] == "radix" and st["outside_buckets"] > 0, st
+    check_join(got, orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 299, cap=skey.size + 16, mt=True))
