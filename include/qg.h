@@ -255,7 +255,7 @@ QG_API qg_status qg_join_set_dense(int enable);
  * buckets, out[2] buckets handled outside the bucket kernel, out[3] their
  * rows, out[4] those of them with several keys (joined together by the
  * sort-merge path; the others are single-key cross products), out[5] knots
- * of the learned model,
+ * of the learned model (path 4: the dense bucket kernel's CTAs per SM),
  * out[6] heavy keys among them, out[7] 1 when the automatic choice moved
  * from radix to the learned function. */
 QG_API qg_status qg_join_stats(qg_ctx *ctx, uint32_t *out8);

@@ -294,6 +294,52 @@ __device__ __forceinline__ uint32_t qg_lb_warp_exclusive(const qg_lookback &lb, 
     return excl;
 }
 
+// qg_lb_warp_exclusive split in two, so that a tile can publish its aggregate
+// as soon as it is known and look back later (successors then wait less):
+// qg_lb_publish_agg by one thread, then qg_lb_warp_lookback by warp 0.
+__device__ __forceinline__ void qg_lb_publish_agg(const qg_lookback &lb, uint32_t tile, uint32_t epoch,
+                                                  uint32_t aggregate) {
+    qg_st_relaxed_u64(&lb.status[tile], qg_lb_word(epoch, tile == 0 ? QG_LB_PREFIX : QG_LB_AGG, aggregate));
+}
+__device__ __forceinline__ uint32_t qg_lb_warp_lookback(const qg_lookback &lb, uint32_t tile, uint32_t epoch,
+                                                        uint32_t aggregate) {
+    const int lane = threadIdx.x & 31;
+    if (tile == 0) return 0;
+    uint32_t excl = 0;
+    long long pred = (long long)tile - 1;
+    while (true) {
+        long long j = pred - lane;
+        unsigned long long flag = QG_LB_PREFIX;
+        uint32_t value = 0;
+        if (j >= 0) {
+            uint32_t spins = 0;
+            unsigned long long w;
+            while (true) {
+                if (spins >= lb.spin_limit) {
+                    qg_record_error(lb.ctl, QG_ERR_TIMEOUT, lb.site);
+                    w = qg_lb_word(epoch, QG_LB_PREFIX, 0);
+                    break;
+                }
+                w = qg_ld_relaxed_u64(&lb.status[j]);
+                if ((uint32_t)(w >> 34) == (epoch & 0x3fffffffu) && ((w >> 32) & 3ull) != 0) break;
+                spins++;
+                __nanosleep(32);
+            }
+            flag = (w >> 32) & 3ull;
+            value = (uint32_t)w;
+        }
+        uint32_t pmask = __ballot_sync(QG_FULL_MASK, flag == QG_LB_PREFIX);
+        int stop = pmask ? (__ffs(pmask) - 1) : 31;
+        uint32_t contrib = (lane <= stop) ? value : 0u;
+        excl += __reduce_add_sync(QG_FULL_MASK, contrib);
+        if (pmask) break;
+        pred -= 32;
+    }
+    if (lane == 0)
+        qg_st_relaxed_u64(&lb.status[tile], qg_lb_word(epoch, QG_LB_PREFIX, excl + aggregate));
+    return excl;
+}
+
 // Wide look-back: called by the NW*32 threads of warps 0..NW-1, which read
 // NW*32 predecessors per round (one each), synchronising on named barrier 1.
 // The inclusive-prefix frontier then advances NW*32 tiles per L2 round trip

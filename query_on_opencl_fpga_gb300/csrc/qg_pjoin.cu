@@ -100,12 +100,20 @@ k_pj_rrec(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
     }
 }
 
-// R's key range from the key column alone.
+// R's key range from the key column alone (16-byte loads where aligned).
 __global__ void __launch_bounds__(256)
 k_pj_rrange(const int32_t *__restrict__ rkey, long long nR, PjRange *range) {
     uint32_t lmin = 0xffffffffu, lmax = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += stride) {
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool vec = ((uintptr_t)rkey & 15) == 0;
+    const long long nv = vec ? nR / 4 : 0;
+    for (long long i = t0; i < nv; i += stride) {
+        const int4 v = __ldg(reinterpret_cast<const int4 *>(rkey) + i);
+        lmin = min(min(lmin, (uint32_t)v.x), min((uint32_t)v.y, min((uint32_t)v.z, (uint32_t)v.w)));
+        lmax = max(max(lmax, (uint32_t)v.x), max((uint32_t)v.y, max((uint32_t)v.z, (uint32_t)v.w)));
+    }
+    for (long long i = 4 * nv + t0; i < nR; i += stride) {
         const uint32_t k = (uint32_t)__ldg(rkey + i);
         lmin = min(lmin, k);
         lmax = max(lmax, k);
@@ -119,10 +127,11 @@ k_pj_rrange(const int32_t *__restrict__ rkey, long long nR, PjRange *range) {
 }
 
 // R after its key range is known.  Dense span (pj_dense_span): the presence
-// bit of every key offset is set with atomicOr -- a bit found set already
-// means a duplicate key (flags[0] = 1) -- and T[offset] = payload; flags[1] =
-// 1.  Otherwise: R records (key << 32 | payload) and the two 8-bit digit
-// histograms of their radix bucket ids into hist[0 .. 512).
+// bit of every key offset is set (fire-and-forget reductions) and T[offset] =
+// payload, flags[1] = 1; k_pj_distinct then counts the set bits, and fewer
+// than nR means a duplicate key.  Otherwise: R records (key << 32 | payload)
+// and the two 8-bit digit histograms of their radix bucket ids into
+// hist[0 .. 512).
 __global__ void __launch_bounds__(256)
 k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, long long nR,
           const PjRange *__restrict__ range, int lb2, uint32_t *__restrict__ bitmap, uint32_t *__restrict__ T,
@@ -133,14 +142,22 @@ k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
     const long long stride = (long long)gridDim.x * blockDim.x;
     if (dense) {
         if (blockIdx.x == 0 && threadIdx.x == 0) flags[1] = 1u;
-        bool dup = false;
-        for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nR; i += stride) {
-            const uint32_t off = (uint32_t)__ldg(rkey + i) - kmin;
-            const uint32_t bit = 1u << (off & 31u);
-            dup |= (atomicOr(&bitmap[off >> 5], bit) & bit) != 0u;
-            T[off] = (uint32_t)__ldg(rpay + i);
+        constexpr int U = 4;  // rows in flight per thread
+        for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < nR; i0 += U * stride) {
+            uint32_t off[U], pay[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const long long i = i0 + u * stride;
+                off[u] = i < nR ? (uint32_t)__ldg(rkey + i) - kmin : 0u;
+                pay[u] = i < nR ? (uint32_t)__ldg(rpay + i) : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (i0 + u * stride >= nR) break;
+                atomicOr(&bitmap[off[u] >> 5], 1u << (off[u] & 31u));  // result unused: a reduction
+                T[off[u]] = pay[u];
+            }
         }
-        if (__any_sync(QG_FULL_MASK, dup) && (threadIdx.x & 31) == 0) flags[0] = 1u;
         return;
     }
     for (int i = threadIdx.x; i < 512; i += blockDim.x) (&h[0][0])[i] = 0;
@@ -156,6 +173,22 @@ k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
     __syncthreads();
     for (int i = threadIdx.x; i < 512; i += blockDim.x)
         if ((&h[0][0])[i]) atomicAdd(&hist[i], (&h[0][0])[i]);
+}
+
+// Set bits of the presence bitmap over the dense span (only when k_pj_rtab
+// built it), added to *count: the distinct R keys.
+__global__ void __launch_bounds__(256)
+k_pj_distinct(const uint32_t *__restrict__ bitmap, const PjRange *__restrict__ range, int lb2, long long nR,
+              unsigned long long *__restrict__ count) {
+    const uint32_t kmin = range->kmin, kmax = range->kmax;
+    if (!pj_dense_span(kmin, kmax, lb2, nR)) return;
+    const unsigned long long words = ((unsigned long long)(kmax - kmin) + 1ull + 31ull) >> 5;
+    uint32_t c = 0;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < words;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        c += __popc(__ldcg(bitmap + i));
+    c = __reduce_add_sync(QG_FULL_MASK, c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, (unsigned long long)c);
 }
 
 // ---------------------------------------------------------------------------
@@ -812,17 +845,20 @@ k_pj_join(PbArgs a, qg_lookback lb) {
 
 // Dense build side (pj_dense_span, unique keys): one CTA per join group,
 // tickets in group order.  A group is a key range [kmin + gk[g], kmin +
-// gk[g + 1]) of at most PB_CSPAN keys with its S' rows [gs[g], gs[g + 1]).
-// The S' rows are counting-sorted by key in shared memory; a row matches when
-// its key's presence bit is set, and then produces exactly one output row
-// (key, T[key - kmin], S.payload).  The group's match count is published and
-// its output offset found by decoupled look-back, as in k_pj_join; each warp
-// writes its rows' matches at consecutive output rows.
+// gk[g + 1]) of at most PB_CSPAN keys with its S' rows [gs[g], gs[g + 1]).  A
+// row matches when its key's presence bit is set, and then produces exactly
+// one output row (key, T[key - kmin], S.payload).  So the group's output
+// count is known as soon as its rows are loaded: it is published at once
+// (successors' look-backs wait less), then the matching rows alone are
+// counting-sorted by key in shared memory -- the sorted index of a row is its
+// place in the group's output -- and, once the look-back has found the
+// group's offset, written with consecutive addresses.
 struct PdSmem {
-    unsigned long long s[PB_SMAX];
-    uint32_t cnt[PB_CSPAN];
+    unsigned long long s[PB_SMAX];  // the group's matching S' rows, sorted by key
+    uint32_t cnt[PB_CSPAN];         // counting-sort counters, then start offsets
+    uint32_t red[PB_WARPS];
     uint32_t wsum[PB_WARPS];
-    uint32_t tile, epoch, excl, pad;
+    uint32_t tile, epoch, excl, total;
 };
 
 struct PdArgs {
@@ -850,24 +886,42 @@ k_pj_join_dense(PdArgs a, qg_lookback lb) {
         if (tid == 0) qg_record_error(lb.ctl, QG_ERR_INVALID, QG_SITE_PJ_BUCKET);
         work = false;
     }
-    uint32_t my_cnt = 0;
-    uint32_t q = 0, r0 = 0;  // this warp's segment of sorted rows
+    const uint32_t base = a.kmin + k0;
+    unsigned long long v[PB_IPT];
+    uint32_t pres = 0, np = 0;
     if (work) {
-        const uint32_t base = a.kmin + k0;
-        unsigned long long it[PB_IPT];
-        uint32_t rk[PB_IPT];
+#pragma unroll
+        for (int j = 0; j < PB_IPT; j++) {
+            const uint32_t i = j * PB_THREADS + tid;
+            v[j] = i < sn ? __ldcs(a.S + sb + i) : 0ull;
+        }
         for (uint32_t i = tid; i < span; i += PB_THREADS) S.cnt[i] = 0;
 #pragma unroll
         for (int j = 0; j < PB_IPT; j++) {
             const uint32_t i = j * PB_THREADS + tid;
-            it[j] = i < sn ? __ldg(a.S + sb + i) : 0ull;
+            if (i < sn) {
+                const uint32_t off = (uint32_t)(v[j] >> 32) - a.kmin;
+                const uint32_t p = (__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u;
+                pres |= p << j;
+                np += p;
+            }
         }
-        __syncthreads();
+    }
+    np = __reduce_add_sync(QG_FULL_MASK, np);
+    if (lane == 0) S.red[warp] = np;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t t = 0;
 #pragma unroll
-        for (int j = 0; j < PB_IPT; j++) {
-            const uint32_t i = j * PB_THREADS + tid;
-            if (i < sn) rk[j] = atomicAdd(&S.cnt[(uint32_t)(it[j] >> 32) - base], 1u);
-        }
+        for (int w = 0; w < PB_WARPS; w++) t += S.red[w];
+        S.total = t;
+        qg_lb_publish_agg(lb, g, S.epoch, t);
+    }
+    if (work) {
+        uint32_t rk[PB_IPT];
+#pragma unroll
+        for (int j = 0; j < PB_IPT; j++)
+            if ((pres >> j) & 1u) rk[j] = atomicAdd(&S.cnt[(uint32_t)(v[j] >> 32) - base], 1u);
         __syncthreads();
         constexpr int PER = PB_CSPAN / PB_THREADS;
         const uint32_t c0 = tid * PER;
@@ -886,54 +940,28 @@ k_pj_join_dense(PdArgs a, qg_lookback lb) {
         }
         __syncthreads();
 #pragma unroll
-        for (int j = 0; j < PB_IPT; j++) {
-            const uint32_t i = j * PB_THREADS + tid;
-            if (i < sn) S.s[S.cnt[(uint32_t)(it[j] >> 32) - base] + rk[j]] = it[j];
-        }
-        __syncthreads();
-        r0 = min(sn, (uint32_t)warp * PB_WSEG);
-        q = min(sn, r0 + PB_WSEG) - r0;
-        for (uint32_t r = r0 + lane; r < r0 + q; r += 32) {
-            const uint32_t off = (uint32_t)(S.s[r] >> 32) - a.kmin;
-            my_cnt += (__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u;
-        }
+        for (int j = 0; j < PB_IPT; j++)
+            if ((pres >> j) & 1u) S.s[S.cnt[(uint32_t)(v[j] >> 32) - base] + rk[j]] = v[j];
     }
-    // warp totals -> warp offsets within the group (pb_excl: every thread, uniformly)
-    const uint32_t wcnt = __reduce_add_sync(QG_FULL_MASK, my_cnt);
-    uint32_t total;
-    const uint32_t my_off = pb_excl(lane == 0 ? wcnt : 0u, S.wsum, &total);
-    const uint32_t warp_off = __shfl_sync(QG_FULL_MASK, my_off, 0);
+    __syncthreads();
+    const uint32_t total = S.total;
     if (warp == 0) {
-        const uint32_t excl = qg_lb_warp_exclusive(lb, g, S.epoch, total);
+        const uint32_t excl = qg_lb_warp_lookback(lb, g, S.epoch, total);
         if (lane == 0) {
             S.excl = excl;
             if (g == gridDim.x - 1) *a.total = (unsigned long long)excl + total;
         }
     }
     __syncthreads();
-    if (work && wcnt) {  // warp-uniform
-        long long o = (long long)S.excl + warp_off;
-        const uint32_t lt = qg_lanemask_lt();
-        for (uint32_t s0 = r0; s0 < r0 + q; s0 += 32) {
-            const uint32_t r = s0 + lane;
-            unsigned long long v = 0;
-            uint32_t off = 0;
-            bool hit = false;
-            if (r < r0 + q) {
-                v = S.s[r];
-                off = (uint32_t)(v >> 32) - a.kmin;
-                hit = ((__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u) != 0u;
-            }
-            const uint32_t bal = __ballot_sync(QG_FULL_MASK, hit);
-            if (hit) {
-                const long long oo = o + __popc(bal & lt);
-                if (oo < a.cap) {
-                    a.out_k[oo] = (uint32_t)(v >> 32);
-                    a.out_a[oo] = __ldg(a.T + off);
-                    a.out_b[oo] = (uint32_t)v;
-                }
-            }
-            o += __popc(bal);
+    const long long o = S.excl;
+    for (uint32_t r = tid; r < total; r += PB_THREADS) {
+        const unsigned long long x = S.s[r];
+        const long long oo = o + r;
+        if (oo < a.cap) {
+            const uint32_t k = (uint32_t)(x >> 32);
+            a.out_k[oo] = k;
+            a.out_a[oo] = __ldg(a.T + (k - a.kmin));
+            a.out_b[oo] = (uint32_t)x;
         }
     }
     qg_lb_finish(lb, g, gridDim.x - 1, S.epoch);
@@ -1337,7 +1365,7 @@ struct PjLevel {
     PjMj *mj;
     unsigned long long *mjtot;  // matches of the sort-merge buckets
     PjPackOut *pk;              // the packing's counts
-    uint32_t *dflags;           // [4] dense build side: [0] duplicate key seen, [1] dense span
+    uint32_t *dflags;           // [4] dense build side: [1] dense span, [2..3] distinct keys (u64)
     PjPackCta *pkc;             // [nb / (PK_THREADS * 8) + 1] the pack CTAs' totals
     uint32_t *tg;               // [3][nb + PK_THREADS * PK_SEG] the packing's staging (group ends, flags)
     PjCross *tover;             // [nb + PK_THREADS * PK_SEG] the packing's staging (listed buckets)
@@ -1427,11 +1455,16 @@ qg_status pj_pool_get(qg_ctx *ctx, char **slot, size_t *slot_bytes, size_t bytes
     return QG_OK;
 }
 
+int g_pd_ctas_per_sm = 1;  // resident CTAs of k_pj_join_dense per SM
+
 qg_status pj_attrs(qg_ctx *ctx) {
     static bool done = false;
     if (!done) {
         QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PbSmem)), "attr join");
         QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PdSmem)), "attr join dense");
+        int occ = 0;
+        QG_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pj_join_dense, PB_THREADS, sizeof(PdSmem)), "occupancy");
+        g_pd_ctas_per_sm = occ > 0 ? occ : 1;
         done = true;
     }
     return QG_OK;
@@ -1719,6 +1752,7 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
         ctx->pj_stats[0] = 4;
         ctx->pj_stats[1] = nbu;
         for (int i = 2; i < 8; i++) ctx->pj_stats[i] = 0;
+        ctx->pj_stats[5] = (uint32_t)g_pd_ctas_per_sm;  // no model on this path: the bucket kernel's CTAs per SM
         return QG_OK;
     }
 
@@ -1935,6 +1969,10 @@ static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const i
     k_pj_rtab<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, L.range, lb2, bitmap,
                                                                  (uint32_t *)Rsp, L.dflags, R, L.dh);
     QG_TRY(qg_check_launch(ctx, "k_pj_rtab"));
+    qg_pre_launch(ctx);
+    k_pj_distinct<<<pj_grid(ctx, (nR + 31) / 16, 256, 4), 256, 0, ctx->stream>>>(
+        bitmap, L.range, lb2, nR, reinterpret_cast<unsigned long long *>(L.dflags + 2));
+    QG_TRY(qg_check_launch(ctx, "k_pj_distinct"));
     // S filter with the S' digit histograms of the radix function
     constexpr int SF_TILE = SF_THREADS * SF_ROUNDS * 4;
     const long long tiles = (nS + SF_TILE - 1) / SF_TILE;
@@ -1951,7 +1989,9 @@ static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const i
     QG_TRY(qg_collect_error(ctx));
     const PjRange hr = *hp;
     const long long ns1 = (long long)hr.count;
-    PjRSide rs{rkey, rpay, pin->dflags[1] == 0u, pin->dflags[1] != 0u && pin->dflags[0] == 0u && g_pj_dense,
+    unsigned long long distinct;
+    memcpy(&distinct, pin->dflags + 2, 8);
+    PjRSide rs{rkey, rpay, pin->dflags[1] == 0u, pin->dflags[1] != 0u && distinct == (unsigned long long)nR && g_pj_dense,
                bitmap, (const uint32_t *)Rsp};
     long long M = 0;
     // pj_core ends with a read of the output count and the error word
