@@ -1684,7 +1684,7 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
         uint16_t **bid = side_r ? bidr : bids;
         QG_TRY(qg_radix_passes_pf(ctx, false, qg_sort_bufs{a, nullptr, nullptr, nullptr, bid[0]},
                                   qg_sort_bufs{bb, nullptr, nullptr, nullptr, bid[1]}, n, pf, passes, np, bases,
-                                  &in_b));
+                                  &in_b, true));  // buckets in order; rows within a bucket in any order
         if (in_b) std::swap(a, bb);
         return QG_OK;
     };

@@ -93,7 +93,11 @@ __device__ __forceinline__ uint32_t rs_digit(uint32_t k, uint32_t key_off, int s
 // took 1.29 ms this way against 1.57 ms with two CTAs at 126 registers.
 // DIG: 0 radix digit of the key, 1 learned partition function of the key,
 // 2 bits of the bucket id in the source's sidecar (REC only).
-template <bool KV3, int DIG, bool MATCH = false>
+// RANK: how an item's rank within its digit is found -- 0 eight warp ballots,
+// 1 one match instruction (stable either way), 2 one shared-memory atomic on
+// the tile's digit counter (not stable: for a first LSD pass whose order
+// among equal digits nothing after it needs).
+template <bool KV3, int DIG, int RANK = 0>
 __global__ void __launch_bounds__(RS_THREADS, 4)
 k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
              const qg_cdf_model *model, const uint32_t *__restrict__ dbase,
@@ -186,8 +190,12 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
         rd[i] = d << 24;
         // lanes holding the same digit: one match instruction (passes with
         // few digit values in use) or eight ballots
+        if constexpr (RANK == 2) {
+            if (valid) rd[i] |= atomicAdd(&S.whist[0][d], 1u);
+            continue;
+        }
         uint32_t peers;
-        if (MATCH) {
+        if (RANK == 1) {
             peers = __match_any_sync(QG_FULL_MASK, valid ? d : 256u);  // the tail's invalid lanes share 256
         } else {
             peers = __ballot_sync(QG_FULL_MASK, valid);
@@ -211,11 +219,15 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
         // tile's count of the digit, then its place among the digits.
         const int t = tid;
         uint32_t run = 0;
+        if constexpr (RANK == 2) {
+            run = S.whist[0][t];  // ranks are tile-wide already
+        } else {
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; w++) {
-            uint32_t c = S.whist[w][t];
-            S.whist[w][t] = run;
-            run += c;
+            for (int w = 0; w < RS_WARPS; w++) {
+                uint32_t c = S.whist[w][t];
+                S.whist[w][t] = run;
+                run += c;
+            }
         }
         const uint32_t total = run;
         uint32_t inc = total;
@@ -277,7 +289,7 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
         long long idx = wbase + i * 32 + lane;
         if (idx < n) {
             const uint32_t d = rd[i] >> 24;
-            uint32_t pos = S.dstart[d] + S.whist[warp][d] + (rd[i] & 0xffffffu);
+            uint32_t pos = S.dstart[d] + (RANK == 2 ? 0u : S.whist[warp][d]) + (rd[i] & 0xffffffu);
             S.v[pos] = val[i];
             S.dg[pos] = (uint8_t)d;
             if (KV3) S.k[pos] = key[i];
@@ -345,10 +357,13 @@ template <bool KV3, int DIG>
 static qg_status rs_set_attr(qg_ctx *ctx) {
     static bool done = false;
     if (!done) {
-        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
-        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
+        if constexpr (!KV3)
+            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
         done = true;
     }
     return QG_OK;
@@ -370,7 +385,7 @@ static bool rs_few_digits(const uint32_t *hb, long long n) {
 
 qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
                              const qg_part_fn &pf, const int *passes, int np, const uint32_t *h_bases,
-                             bool *result_in_b) {
+                             bool *result_in_b, bool first_unstable) {
     *result_in_b = false;
     if (np == 0 || n <= 1) return QG_OK;
     if (n >= (1LL << 30)) return QG_ERR_UNSUPPORTED;
@@ -400,10 +415,12 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
         if (side && i == np - 1) d.bid = nullptr;  // the last pass's ids are not read again
         const int shift = (pf.learned || side) ? 8 * p : pf.shift + 8 * p;
         const bool m = rs_few_digits(h_bases + p * QG_RADIX, n);
-        auto kern = kv3 ? (m ? k_radix_pass<true, 0, true> : k_radix_pass<true, 0, false>)
-                    : side ? (m ? k_radix_pass<false, 2, true> : k_radix_pass<false, 2, false>)
-                    : pf.learned ? (m ? k_radix_pass<false, 1, true> : k_radix_pass<false, 1, false>)
-                                 : (m ? k_radix_pass<false, 0, true> : k_radix_pass<false, 0, false>);
+        // the first pass of a caller that needs only the grouping need not be stable
+        const int rk = (first_unstable && i == 0 && !kv3) ? 2 : (m ? 1 : 0);
+        auto kern = kv3 ? (m ? k_radix_pass<true, 0, 1> : k_radix_pass<true, 0, 0>)
+                    : side ? (rk == 2 ? k_radix_pass<false, 2, 2> : rk == 1 ? k_radix_pass<false, 2, 1> : k_radix_pass<false, 2, 0>)
+                    : pf.learned ? (rk == 2 ? k_radix_pass<false, 1, 2> : rk == 1 ? k_radix_pass<false, 1, 1> : k_radix_pass<false, 1, 0>)
+                                 : (rk == 2 ? k_radix_pass<false, 0, 2> : rk == 1 ? k_radix_pass<false, 0, 1> : k_radix_pass<false, 0, 0>);
         qg_pre_launch(ctx);
         kern<<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(s, d, n, shift, (kv3 || !(side || pf.learned)) ? pf.kmin : 0u,
                                                                  pf.learned && !side ? pf.model : nullptr,
@@ -498,7 +515,7 @@ qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b,
                           uint32_t key_off, const int *passes, int np, const uint32_t *h_bases,
                           bool *result_in_b) {
     qg_part_fn pf{0, key_off, 0, nullptr};
-    return qg_radix_passes_pf(ctx, kv3, a, b, n, pf, passes, np, h_bases, result_in_b);
+    return qg_radix_passes_pf(ctx, kv3, a, b, n, pf, passes, np, h_bases, result_in_b, false);
 }
 
 // Sort REC items in `data` (n u64) using `tmp` (n u64) as the ping-pong

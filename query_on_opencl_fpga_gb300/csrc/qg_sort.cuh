@@ -36,10 +36,13 @@ qg_status qg_radix_passes(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b,
                           bool *result_in_b);
 // Same, with the digits taken from a partition function: pass position p
 // sorts by bits [8p, 8p + 8) of the bucket (radix form: of (k - kmin) >> shift).
+// first_unstable: the caller needs the items grouped by bucket only, not in
+// input order within a bucket, so the first pass ranks with shared-memory
+// atomics instead of stable warp ballots (REC items only).
 struct qg_part_fn;
 qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs b, long long n,
                              const qg_part_fn &pf, const int *passes, int np, const uint32_t *h_bases,
-                             bool *result_in_b);
+                             bool *result_in_b, bool first_unstable = false);
 // Passes planned on the device, for sequences without host round trips
 // (CUDA graph capture): all `npos` positions from the device histogram d_hist
 // [npos][256] of (key - key_off) digits, over at most n_bound items whose real
