@@ -74,6 +74,14 @@ __host__ __device__ inline bool pj_dense_span(uint32_t kmin, uint32_t kmax, int 
     return w <= 2ull * (unsigned long long)nR && (1ull << pj_radix(kmin, kmax, lb2).shift) <= PJ_DENSE_BSPAN;
 }
 
+// Counts of the join groups packed on the device (k_pj_place): groups, buckets
+// listed as oversize, their rows, the largest of them.
+struct PjPackOut {
+    uint32_t groups, over;
+    unsigned long long over_rows;
+    uint32_t most, pad;
+};
+
 __global__ void k_pj_range_init(PjRange *r) {
     r->kmin = 0xffffffffu;
     r->kmax = 0;
@@ -129,9 +137,11 @@ k_pj_rrange(const int32_t *__restrict__ rkey, long long nR, PjRange *range) {
 // R after its key range is known.  Dense span (pj_dense_span): the presence
 // bit of every key offset is set (fire-and-forget reductions) and T[offset] =
 // payload, flags[1] = 1; k_pj_distinct then counts the set bits, and fewer
-// than nR means a duplicate key.  Otherwise: R records (key << 32 | payload)
-// and the two 8-bit digit histograms of their radix bucket ids into
-// hist[0 .. 512).
+// than nR means a duplicate key.  (An 8-byte entry holding both, one store
+// per row, measured slower: 0.37 against 0.21 ms at 16M rows, its 128 MB of
+// scattered partial-sector writes spilling out of L2, where the 64 MB table
+// and 2 MB bitmap stay.)  Otherwise: R records (key << 32 | payload) and the
+// two 8-bit digit histograms of their radix bucket ids into hist[0 .. 512).
 __global__ void __launch_bounds__(256)
 k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, long long nR,
           const PjRange *__restrict__ range, int lb2, uint32_t *__restrict__ bitmap, uint32_t *__restrict__ T,
@@ -633,6 +643,7 @@ __device__ __forceinline__ uint32_t pb_hash(uint32_t k) {
 }
 
 // Exclusive prefix of v over the CTA in thread order; *total = sum.
+template <int NW = PB_WARPS>
 __device__ __forceinline__ uint32_t pb_excl(uint32_t v, uint32_t *wsum, uint32_t *total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t inc = v;
@@ -645,7 +656,7 @@ __device__ __forceinline__ uint32_t pb_excl(uint32_t v, uint32_t *wsum, uint32_t
     __syncthreads();
     uint32_t off = 0, tot = 0;
 #pragma unroll
-    for (int w = 0; w < PB_WARPS; w++) {
+    for (int w = 0; w < NW; w++) {
         const uint32_t x = wsum[w];
         if (w < warp) off += x;
         tot += x;
@@ -844,7 +855,10 @@ k_pj_join(PbArgs a, qg_lookback lb) {
 }
 
 // Dense build side (pj_dense_span, unique keys): one CTA per join group,
-// tickets in group order.  A group is a key range [kmin + gk[g], kmin +
+// tickets in group order.  (Persistent CTAs taking groups from a counter,
+// launched without a host read of the group count, measured slower: 0.58
+// against 0.48 ms on config 2; so did a persistent form that bulk-copied the
+// next group's rows into a second shared-memory stage: 0.84 ms.)  A group is a key range [kmin + gk[g], kmin +
 // gk[g + 1]) of at most PB_CSPAN keys with its S' rows [gs[g], gs[g + 1]).  A
 // row matches when its key's presence bit is set, and then produces exactly
 // one output row (key, T[key - kmin], S.payload).  So the group's output
@@ -853,11 +867,12 @@ k_pj_join(PbArgs a, qg_lookback lb) {
 // counting-sorted by key in shared memory -- the sorted index of a row is its
 // place in the group's output -- and, once the look-back has found the
 // group's offset, written with consecutive addresses.
+template <int SMAX, int NW>
 struct PdSmem {
-    unsigned long long s[PB_SMAX];  // the group's matching S' rows, sorted by key
-    uint32_t cnt[PB_CSPAN];         // counting-sort counters, then start offsets
-    uint32_t red[PB_WARPS];
-    uint32_t wsum[PB_WARPS];
+    unsigned long long s[SMAX];  // the group's matching S' rows, sorted by key
+    uint32_t cnt[PB_CSPAN];      // counting-sort counters, then start offsets
+    uint32_t red[NW];
+    uint32_t wsum[NW];
     uint32_t tile, epoch, excl, total;
 };
 
@@ -872,89 +887,105 @@ struct PdArgs {
     long long cap;
 };
 
-__global__ void __launch_bounds__(PB_THREADS, 2)
-k_pj_join_dense(PdArgs a, qg_lookback lb) {
-    extern __shared__ __align__(16) unsigned char pd_raw[];
-    PdSmem &S = *reinterpret_cast<PdSmem *>(pd_raw);
+// One group of the dense bucket kernels.  THREADS threads, at most SMAX S'
+// rows per group (SMAX / THREADS per thread, in registers).  FULL: R's keys
+// fill their whole span (a permutation of [kmin, kmax]), so every S' row
+// matches (S' holds only keys of that span): the group's output starts at its
+// first S' row, with no presence test and no look-back.  Otherwise the
+// group's count is published as soon as its rows are loaded and its offset
+// comes from the look-back (tickets in group order).
+template <int THREADS, int SMAX, bool FULL>
+__device__ __forceinline__ void pd_group(const PdArgs &a, const qg_lookback &lb, PdSmem<SMAX, THREADS / 32> &S,
+                                         uint32_t g, uint32_t last) {
+    constexpr int NW = THREADS / 32, IPT = SMAX / THREADS;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    qg_lb_begin(lb, &S.tile, &S.epoch);
-    const uint32_t g = S.tile;
     const uint32_t sb = a.gs[g], sn = a.gs[g + 1] - sb;
     const uint32_t k0 = a.gk[g], span = a.gk[g + 1] - k0;
     bool work = sn > 0 && span > 0;
-    if (work && (sn > (uint32_t)PB_SMAX || span > (uint32_t)PB_CSPAN)) {  // the packing keeps groups within both
+    if (work && (sn > (uint32_t)SMAX || span > (uint32_t)PB_CSPAN)) {  // the packing keeps groups within both
         if (tid == 0) qg_record_error(lb.ctl, QG_ERR_INVALID, QG_SITE_PJ_BUCKET);
         work = false;
     }
     const uint32_t base = a.kmin + k0;
-    unsigned long long v[PB_IPT];
+    unsigned long long v[IPT];
     uint32_t pres = 0, np = 0;
     if (work) {
 #pragma unroll
-        for (int j = 0; j < PB_IPT; j++) {
-            const uint32_t i = j * PB_THREADS + tid;
+        for (int j = 0; j < IPT; j++) {
+            const uint32_t i = j * THREADS + tid;
             v[j] = i < sn ? __ldcs(a.S + sb + i) : 0ull;
         }
-        for (uint32_t i = tid; i < span; i += PB_THREADS) S.cnt[i] = 0;
+        for (uint32_t i = tid; i < span; i += THREADS) S.cnt[i] = 0;
 #pragma unroll
-        for (int j = 0; j < PB_IPT; j++) {
-            const uint32_t i = j * PB_THREADS + tid;
+        for (int j = 0; j < IPT; j++) {
+            const uint32_t i = j * THREADS + tid;
             if (i < sn) {
-                const uint32_t off = (uint32_t)(v[j] >> 32) - a.kmin;
-                const uint32_t p = (__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u;
+                uint32_t p = 1u;
+                if (!FULL) {
+                    const uint32_t off = (uint32_t)(v[j] >> 32) - a.kmin;
+                    p = (__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u;
+                }
                 pres |= p << j;
                 np += p;
             }
         }
     }
-    np = __reduce_add_sync(QG_FULL_MASK, np);
-    if (lane == 0) S.red[warp] = np;
-    __syncthreads();
-    if (tid == 0) {
-        uint32_t t = 0;
+    if (FULL) {
+        if (tid == 0) S.total = work ? sn : 0u;
+        __syncthreads();
+    } else {
+        np = __reduce_add_sync(QG_FULL_MASK, np);
+        if (lane == 0) S.red[warp] = np;
+        __syncthreads();
+        if (tid == 0) {
+            uint32_t t = 0;
 #pragma unroll
-        for (int w = 0; w < PB_WARPS; w++) t += S.red[w];
-        S.total = t;
-        qg_lb_publish_agg(lb, g, S.epoch, t);
+            for (int w = 0; w < NW; w++) t += S.red[w];
+            S.total = t;
+            qg_lb_publish_agg(lb, g, S.epoch, t);
+        }
     }
     if (work) {
-        uint32_t rk[PB_IPT];
+        uint32_t rk[IPT];
 #pragma unroll
-        for (int j = 0; j < PB_IPT; j++)
+        for (int j = 0; j < IPT; j++)
             if ((pres >> j) & 1u) rk[j] = atomicAdd(&S.cnt[(uint32_t)(v[j] >> 32) - base], 1u);
         __syncthreads();
-        constexpr int PER = PB_CSPAN / PB_THREADS;
+        // exclusive scan of the counters: thread t owns PER consecutive ones
+        constexpr int PER = PB_CSPAN / THREADS;
         const uint32_t c0 = tid * PER;
-        uint32_t loc[PER], sum = 0;
-#pragma unroll
-        for (int e = 0; e < PER; e++) {
-            loc[e] = (c0 + e < span) ? S.cnt[c0 + e] : 0u;
-            sum += loc[e];
-        }
+        uint32_t sum = 0;
+#pragma unroll 8
+        for (int e = 0; e < PER; e++) sum += (c0 + e < span) ? S.cnt[c0 + e] : 0u;
         uint32_t tot;
-        uint32_t run = pb_excl(sum, S.wsum, &tot);
-#pragma unroll
+        uint32_t run = pb_excl<NW>(sum, S.wsum, &tot);
+#pragma unroll 8
         for (int e = 0; e < PER; e++) {
-            if (c0 + e < span) S.cnt[c0 + e] = run;
-            run += loc[e];
+            if (c0 + e < span) {
+                const uint32_t c = S.cnt[c0 + e];
+                S.cnt[c0 + e] = run;
+                run += c;
+            }
         }
         __syncthreads();
 #pragma unroll
-        for (int j = 0; j < PB_IPT; j++)
+        for (int j = 0; j < IPT; j++)
             if ((pres >> j) & 1u) S.s[S.cnt[(uint32_t)(v[j] >> 32) - base] + rk[j]] = v[j];
     }
     __syncthreads();
     const uint32_t total = S.total;
-    if (warp == 0) {
+    if (FULL) {
+        if (tid == 0 && g == last) *a.total = (unsigned long long)a.gs[g + 1] - a.gs[0];
+    } else if (warp == 0) {
         const uint32_t excl = qg_lb_warp_lookback(lb, g, S.epoch, total);
         if (lane == 0) {
             S.excl = excl;
-            if (g == gridDim.x - 1) *a.total = (unsigned long long)excl + total;
+            if (g == last) *a.total = (unsigned long long)excl + total;
         }
     }
     __syncthreads();
-    const long long o = S.excl;
-    for (uint32_t r = tid; r < total; r += PB_THREADS) {
+    const long long o = FULL ? (long long)(sb - a.gs[0]) : (long long)S.excl;
+    for (uint32_t r = tid; r < total; r += THREADS) {
         const unsigned long long x = S.s[r];
         const long long oo = o + r;
         if (oo < a.cap) {
@@ -964,7 +995,27 @@ k_pj_join_dense(PdArgs a, qg_lookback lb) {
             a.out_b[oo] = (uint32_t)x;
         }
     }
-    qg_lb_finish(lb, g, gridDim.x - 1, S.epoch);
+}
+
+// One CTA per group: tickets in group order with the look-back, or (FULL) in
+// any order.  (Persistent CTAs taking the groups in turn -- by tickets, or
+// statically for FULL, launched without a host read of the group count --
+// measured slower on config 2: 0.58 against 0.48 ms, and 0.52 against 0.41
+// ms; 0.57 ms with the largest shared-memory carveout, which leaves the
+// bitmap and payload reads less L1.  A persistent form that bulk-copied the
+// next group's rows into a second shared-memory stage took 0.84 ms.)
+template <int THREADS, int SMAX, bool FULL>
+__global__ void __launch_bounds__(THREADS, 1024 / THREADS)
+k_pj_join_dense(PdArgs a, qg_lookback lb) {
+    extern __shared__ __align__(16) unsigned char pd_raw[];
+    PdSmem<SMAX, THREADS / 32> &S = *reinterpret_cast<PdSmem<SMAX, THREADS / 32> *>(pd_raw);
+    if (FULL) {
+        pd_group<THREADS, SMAX, true>(a, lb, S, blockIdx.x, gridDim.x - 1);
+    } else {
+        qg_lb_begin(lb, &S.tile, &S.epoch);
+        pd_group<THREADS, SMAX, false>(a, lb, S, S.tile, gridDim.x - 1);
+        qg_lb_finish(lb, S.tile, gridDim.x - 1, S.epoch);
+    }
 }
 
 // Group bounds of the dense build side in key offsets: the buckets' first key
@@ -1002,11 +1053,6 @@ struct PjMj {  // a bucket with several keys, joined by the sort-merge path
 // loads, the next 8 in flight while these are walked (seg is a multiple of 8;
 // rbk and sbk hold at least nb + 16 entries).  Several CTAs share the
 // scattered reads, which bound this kernel on one SM.
-struct PjPackOut {
-    uint32_t groups, over;
-    unsigned long long over_rows;
-    uint32_t most, pad;
-};
 struct PjPackCta {  // one pack CTA's totals
     uint32_t groups, over, most, pad;
     unsigned long long over_rows;
@@ -1461,9 +1507,13 @@ qg_status pj_attrs(qg_ctx *ctx) {
     static bool done = false;
     if (!done) {
         QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PbSmem)), "attr join");
-        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join_dense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(PdSmem)), "attr join dense");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join_dense<PB_THREADS, PB_SMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sizeof(PdSmem<PB_SMAX, PB_WARPS>)), "attr join dense");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_pj_join_dense<PB_THREADS, PB_SMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sizeof(PdSmem<PB_SMAX, PB_WARPS>)), "attr join dense");
         int occ = 0;
-        QG_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pj_join_dense, PB_THREADS, sizeof(PdSmem)), "occupancy");
+        QG_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_pj_join_dense<PB_THREADS, PB_SMAX, false>,
+                                                                       PB_THREADS, sizeof(PdSmem<PB_SMAX, PB_WARPS>)), "occupancy");
         g_pd_ctas_per_sm = occ > 0 ? occ : 1;
         done = true;
     }
@@ -1688,8 +1738,7 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
         if (in_b) std::swap(a, bb);
         return QG_OK;
     };
-    // fine bucket bounds, then the join groups packed on the device (one read of the counts)
-    auto pack = [&](uint32_t rmax, PjPackOut *pk) -> qg_status {
+    auto pack_launch = [&](uint32_t rmax) -> qg_status {
         const uint32_t nctas = (nbu + PK_THREADS * PK_SEG - 1) / (PK_THREADS * PK_SEG);
         const uint32_t seg = ((nbu + PK_THREADS * nctas - 1) / (PK_THREADS * nctas) + 7) & ~7u;
         const size_t tgn = (size_t)nb + PK_THREADS * PK_SEG;
@@ -1701,12 +1750,18 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
         k_pj_place<<<nctas, 256, 0, ctx->stream>>>(L.rbk, L.sbk, nbu, PK_THREADS * seg, L.tg, L.tg + tgn,
                                                    L.tg + 2 * tgn, L.tover, L.pkc, L.gr, L.gs, L.big, L.bigcnt,
                                                    L.cross, L.pk);
-        QG_TRY(qg_check_launch(ctx, "k_pj_place"));
+        return qg_check_launch(ctx, "k_pj_place");
+    };
+    auto pack_check = [&](const PjPackOut &pk) -> qg_status {
+        return (pk.groups == 0 || pk.groups > nbu || pk.over > pk.groups) ? QG_ERR_INVALID : QG_OK;  // G <= buckets
+    };
+    // fine bucket bounds, then the join groups packed on the device (one read of the counts)
+    auto pack = [&](uint32_t rmax, PjPackOut *pk) -> qg_status {
+        QG_TRY(pack_launch(rmax));
         QG_TRY_CUDA(ctx, cudaMemcpyAsync(&pin->pk, L.pk, sizeof(PjPackOut), cudaMemcpyDeviceToHost, ctx->stream), "pack d2h");
         QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
         *pk = pin->pk;
-        if (pk->groups == 0 || pk->groups > nbu || pk->over > pk->groups) return QG_ERR_INVALID;  // G <= buckets
-        return QG_OK;
+        return pack_check(*pk);
     };
     auto r_bounds = [&]() -> qg_status {
         qg_pre_launch(ctx);
@@ -1720,41 +1775,43 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
     QG_TRY(qg_check_launch(ctx, "k_pj_bounds"));
     PjPackOut pk;
     if (dense) {
-        // a group's "R rows" are its key span, at most a counting sort's
+        // A group's "R rows" are its key span, at most a counting sort's.
         qg_pre_launch(ctx);
         k_pj_vbounds<<<(nbu + 256) / 256, 256, 0, ctx->stream>>>(L.rbk, nbu, rp.shift,
                                                                 (unsigned long long)(kmax - kmin) + 1ull);
         QG_TRY(qg_check_launch(ctx, "k_pj_vbounds"));
         QG_TRY(pack(PJ_DENSE_BSPAN, &pk));
-        if (pk.over > 0) {  // an S' bucket above the bucket kernel's capacity: R's records after all
-            dense = false;
-            QG_TRY(ensure_rrec());
-            QG_TRY(partition(true));
-            QG_TRY(r_bounds());
-            QG_TRY(pack(g_pj_rmax, &pk));
+        if (pk.over == 0) {
+            // every S' row matches when R's keys fill their span (S' keys lie in it)
+            const bool full = (unsigned long long)(kmax - kmin) + 1ull == (unsigned long long)nR;
+            qg_lookback lb;
+            QG_TRY(qg_lb_make(ctx, pk.groups, QG_SITE_JOIN_PROBE, &lb));
+            PdArgs da{s, L.gr, L.gs, rs.bitmap, rs.T, kmin, L.total, ok, oa, ob, cap};
+            qg_pre_launch(ctx);
+            auto kern = full ? k_pj_join_dense<PB_THREADS, PB_SMAX, true> : k_pj_join_dense<PB_THREADS, PB_SMAX, false>;
+            kern<<<pk.groups, PB_THREADS, sizeof(PdSmem<PB_SMAX, PB_WARPS>), ctx->stream>>>(da, lb);
+            QG_TRY(qg_check_launch(ctx, "k_pj_join_dense"));
+            QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
+            QG_TRY(qg_collect_error(ctx));
+            *M_out = ctx->pinned[0];
+            ctx->pj_stats[0] = 4;
+            ctx->pj_stats[1] = nbu;
+            for (int i = 2; i < 8; i++) ctx->pj_stats[i] = 0;
+            ctx->pj_stats[5] = (uint32_t)g_pd_ctas_per_sm;  // no model on this path: the bucket kernel's CTAs per SM
+            return QG_OK;
         }
+        // an S' bucket above the bucket kernel's capacity: R's records after all
+        dense = false;
+        QG_TRY(ensure_rrec());
+        QG_TRY(partition(true));
+        QG_TRY(r_bounds());
+        QG_TRY(pack(g_pj_rmax, &pk));
     } else {
         QG_TRY(r_bounds());
         QG_TRY(pack(g_pj_rmax, &pk));
     }
     const uint32_t G = pk.groups;
     const uint32_t no = pk.over;
-    if (dense) {
-        qg_lookback lb;
-        QG_TRY(qg_lb_make(ctx, G, QG_SITE_JOIN_PROBE, &lb));
-        PdArgs da{s, L.gr, L.gs, rs.bitmap, rs.T, kmin, L.total, ok, oa, ob, cap};
-        qg_pre_launch(ctx);
-        k_pj_join_dense<<<G, PB_THREADS, sizeof(PdSmem), ctx->stream>>>(da, lb);
-        QG_TRY(qg_check_launch(ctx, "k_pj_join_dense"));
-        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.total, 8, cudaMemcpyDeviceToHost, ctx->stream), "total d2h");
-        QG_TRY(qg_collect_error(ctx));
-        *M_out = ctx->pinned[0];
-        ctx->pj_stats[0] = 4;
-        ctx->pj_stats[1] = nbu;
-        for (int i = 2; i < 8; i++) ctx->pj_stats[i] = 0;
-        ctx->pj_stats[5] = (uint32_t)g_pd_ctas_per_sm;  // no model on this path: the bucket kernel's CTAs per SM
-        return QG_OK;
-    }
 
     // Outside groups: a bucket with one key is a cross product (k_pj_cross);
     // the others all go through the sort-merge path together (k_pj_mj_*).

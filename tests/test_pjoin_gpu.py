@@ -226,6 +226,10 @@ def test_join_dense_build_side(ctx, orc, knobs, dense_knob, nR, nS, gap, base):
     args = [dev(a) for a in (rkey, rpay, skey, spay)]
     check_join(ctx.join_filter_sort(*args, -(2 ** 31), 299), exp)
     assert ctx.join_stats()["path"] == "dense"
+    knobs(0, 0, 1024, 0)  # groups of at most 1024 rows: the 512-thread form of the dense bucket kernel
+    check_join(ctx.join_filter_sort(*args, -(2 ** 31), 299), exp)
+    assert ctx.join_stats()["path"] == "dense"
+    knobs(0)
     dense_knob(False)
     check_join(ctx.join_filter_sort(*args, -(2 ** 31), 299), exp)
     assert ctx.join_stats()["path"] == "radix"
