@@ -82,10 +82,18 @@ struct PjPackOut {
     uint32_t most, pad;
 };
 
-__global__ void k_pj_range_init(PjRange *r) {
+// flags of the dense build side (u32 words): [1] dense span, [2..3] distinct
+// keys (u64), [4] / [5] smallest / largest R payload (int32), [6] a sentinel
+// payload exists, [7] the sentinel.
+enum { PJ_F_DENSE = 1, PJ_F_DISTINCT = 2, PJ_F_PMIN = 4, PJ_F_PMAX = 5, PJ_F_SENT_OK = 6, PJ_F_SENT = 7, PJ_F_WORDS = 8 };
+
+__global__ void k_pj_range_init(PjRange *r, uint32_t *flags) {
     r->kmin = 0xffffffffu;
     r->kmax = 0;
     r->count = 0;
+    for (int i = 0; i < PJ_F_WORDS; i++) flags[i] = 0;
+    flags[PJ_F_PMIN] = 0x7fffffffu;
+    flags[PJ_F_PMAX] = 0x80000000u;
 }
 
 __global__ void __launch_bounds__(256)
@@ -108,36 +116,82 @@ k_pj_rrec(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
     }
 }
 
-// R's key range from the key column alone (16-byte loads where aligned).
+// R's key range and payload range (16-byte loads where aligned).
 __global__ void __launch_bounds__(256)
-k_pj_rrange(const int32_t *__restrict__ rkey, long long nR, PjRange *range) {
+k_pj_rrange(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, long long nR, PjRange *range,
+            uint32_t *flags) {
     uint32_t lmin = 0xffffffffu, lmax = 0;
+    int32_t pmin = 0x7fffffff, pmax = (int32_t)0x80000000;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool vec = ((uintptr_t)rkey & 15) == 0;
+    const bool vec = (((uintptr_t)rkey | (uintptr_t)rpay) & 15) == 0;
     const long long nv = vec ? nR / 4 : 0;
     for (long long i = t0; i < nv; i += stride) {
         const int4 v = __ldg(reinterpret_cast<const int4 *>(rkey) + i);
+        const int4 p = __ldg(reinterpret_cast<const int4 *>(rpay) + i);
         lmin = min(min(lmin, (uint32_t)v.x), min((uint32_t)v.y, min((uint32_t)v.z, (uint32_t)v.w)));
         lmax = max(max(lmax, (uint32_t)v.x), max((uint32_t)v.y, max((uint32_t)v.z, (uint32_t)v.w)));
+        pmin = min(min(pmin, p.x), min(p.y, min(p.z, p.w)));
+        pmax = max(max(pmax, p.x), max(p.y, max(p.z, p.w)));
     }
     for (long long i = 4 * nv + t0; i < nR; i += stride) {
         const uint32_t k = (uint32_t)__ldg(rkey + i);
+        const int32_t p = __ldg(rpay + i);
         lmin = min(lmin, k);
         lmax = max(lmax, k);
+        pmin = min(pmin, p);
+        pmax = max(pmax, p);
     }
     lmin = __reduce_min_sync(QG_FULL_MASK, lmin);
     lmax = __reduce_max_sync(QG_FULL_MASK, lmax);
+    pmin = __reduce_min_sync(QG_FULL_MASK, pmin);
+    pmax = __reduce_max_sync(QG_FULL_MASK, pmax);
     if ((threadIdx.x & 31) == 0) {
         atomicMin(&range->kmin, lmin);
         atomicMax(&range->kmax, lmax);
+        atomicMin(reinterpret_cast<int *>(flags + PJ_F_PMIN), pmin);
+        atomicMax(reinterpret_cast<int *>(flags + PJ_F_PMAX), pmax);
     }
 }
 
-// R after its key range is known.  Dense span (pj_dense_span): the presence
-// bit of every key offset is set (fire-and-forget reductions) and T[offset] =
-// payload, flags[1] = 1; k_pj_distinct then counts the set bits, and fewer
-// than nR means a duplicate key.  (An 8-byte entry holding both, one store
+// A payload value that no R row holds and whose four bytes are equal (so a
+// byte memset could write it): the first b * 0x01010101 outside [pmin, pmax].
+__device__ __forceinline__ bool pj_sentinel(int32_t pmin, int32_t pmax, uint32_t *out) {
+    for (uint32_t b = 0; b < 256; b++) {
+        const int32_t v = (int32_t)(b * 0x01010101u);
+        if (v < pmin || v > pmax) {
+            *out = (uint32_t)v;
+            return true;
+        }
+    }
+    return false;
+}
+
+// Dense span with a sentinel payload: T[0 .. w) = the sentinel (no row yet),
+// flags[PJ_F_SENT_OK] = 1, flags[PJ_F_SENT] = the sentinel.
+__global__ void __launch_bounds__(256)
+k_pj_tfill(uint32_t *__restrict__ T, const PjRange *__restrict__ range, int lb2, long long nR, uint32_t *flags) {
+    const uint32_t kmin = range->kmin, kmax = range->kmax;
+    if (!pj_dense_span(kmin, kmax, lb2, nR)) return;
+    uint32_t sent;
+    if (!pj_sentinel((int32_t)flags[PJ_F_PMIN], (int32_t)flags[PJ_F_PMAX], &sent)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        flags[PJ_F_SENT_OK] = 1u;
+        flags[PJ_F_SENT] = sent;
+    }
+    const unsigned long long w = (unsigned long long)(kmax - kmin) + 1ull, w4 = w >> 2;
+    uint4 *t4 = reinterpret_cast<uint4 *>(T);  // T is 256-byte aligned
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < w4;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        t4[i] = make_uint4(sent, sent, sent, sent);
+    if (blockIdx.x == 0 && threadIdx.x < (w & 3ull)) T[4 * w4 + threadIdx.x] = sent;
+}
+
+// R after its key range is known.  Dense span (pj_dense_span): T[offset] =
+// payload, and -- unless k_pj_tfill found a sentinel payload (T then holds it
+// where no row is) -- the presence bit of every key offset is set (fire-and-
+// forget reductions); flags[PJ_F_DENSE] = 1.  k_pj_distinct then counts the
+// keys, and fewer than nR means a duplicate.  (An 8-byte entry holding both, one store
 // per row, measured slower: 0.37 against 0.21 ms at 16M rows, its 128 MB of
 // scattered partial-sector writes spilling out of L2, where the 64 MB table
 // and 2 MB bitmap stay.)  Otherwise: R records (key << 32 | payload) and the
@@ -151,7 +205,8 @@ k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
     const bool dense = pj_dense_span(kmin, kmax, lb2, nR);
     const long long stride = (long long)gridDim.x * blockDim.x;
     if (dense) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) flags[1] = 1u;
+        if (blockIdx.x == 0 && threadIdx.x == 0) flags[PJ_F_DENSE] = 1u;
+        const bool sent = flags[PJ_F_SENT_OK] != 0u;  // T holds the sentinel where no row is: no bitmap
         constexpr int U = 4;  // rows in flight per thread
         for (long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x; i0 < nR; i0 += U * stride) {
             uint32_t off[U], pay[U];
@@ -164,7 +219,7 @@ k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (i0 + u * stride >= nR) break;
-                atomicOr(&bitmap[off[u] >> 5], 1u << (off[u] & 31u));  // result unused: a reduction
+                if (!sent) atomicOr(&bitmap[off[u] >> 5], 1u << (off[u] & 31u));  // result unused: a reduction
                 T[off[u]] = pay[u];
             }
         }
@@ -185,18 +240,29 @@ k_pj_rtab(const int32_t *__restrict__ rkey, const int32_t *__restrict__ rpay, lo
         if ((&h[0][0])[i]) atomicAdd(&hist[i], (&h[0][0])[i]);
 }
 
-// Set bits of the presence bitmap over the dense span (only when k_pj_rtab
-// built it), added to *count: the distinct R keys.
+// Distinct R keys over the dense span (only when k_pj_rtab built it), added
+// to *count: the table entries that are not the sentinel, or the set bits of
+// the presence bitmap.
 __global__ void __launch_bounds__(256)
-k_pj_distinct(const uint32_t *__restrict__ bitmap, const PjRange *__restrict__ range, int lb2, long long nR,
-              unsigned long long *__restrict__ count) {
+k_pj_distinct(const uint32_t *__restrict__ bitmap, const uint32_t *__restrict__ T, const PjRange *__restrict__ range,
+              int lb2, long long nR, const uint32_t *__restrict__ flags, unsigned long long *__restrict__ count) {
     const uint32_t kmin = range->kmin, kmax = range->kmax;
     if (!pj_dense_span(kmin, kmax, lb2, nR)) return;
-    const unsigned long long words = ((unsigned long long)(kmax - kmin) + 1ull + 31ull) >> 5;
+    const unsigned long long w = (unsigned long long)(kmax - kmin) + 1ull;
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long t0 = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
     uint32_t c = 0;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < words;
-         i += (unsigned long long)gridDim.x * blockDim.x)
-        c += __popc(__ldcg(bitmap + i));
+    if (flags[PJ_F_SENT_OK]) {
+        const uint32_t sent = flags[PJ_F_SENT];
+        const uint4 *t4 = reinterpret_cast<const uint4 *>(T);
+        for (unsigned long long i = t0; i < (w >> 2); i += stride) {
+            const uint4 x = __ldcs(t4 + i);
+            c += (x.x != sent) + (x.y != sent) + (x.z != sent) + (x.w != sent);
+        }
+        for (unsigned long long i = 4 * (w >> 2) + t0; i < w; i += stride) c += __ldcs(T + i) != sent;
+    } else {
+        for (unsigned long long i = t0; i < ((w + 31ull) >> 5); i += stride) c += __popc(__ldcg(bitmap + i));
+    }
     c = __reduce_add_sync(QG_FULL_MASK, c);
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, (unsigned long long)c);
 }
@@ -879,9 +945,9 @@ struct PdSmem {
 struct PdArgs {
     const unsigned long long *S;  // bucket-ordered S' records
     const uint32_t *gk, *gs;      // [G + 1] first key offset and first S' row of each group
-    const uint32_t *bitmap;       // presence of each key offset
-    const uint32_t *T;            // R payload of each present key offset
-    uint32_t kmin;
+    const uint32_t *bitmap;       // presence of each key offset (unless sent_ok)
+    const uint32_t *T;            // R payload of each present key offset (sent_ok: `sent` where none)
+    uint32_t kmin, sent_ok, sent;
     unsigned long long *total;    // output rows (written by the last group)
     uint32_t *out_k, *out_a, *out_b;
     long long cap;
@@ -923,7 +989,8 @@ __device__ __forceinline__ void pd_group(const PdArgs &a, const qg_lookback &lb,
                 uint32_t p = 1u;
                 if (!FULL) {
                     const uint32_t off = (uint32_t)(v[j] >> 32) - a.kmin;
-                    p = (__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u;
+                    p = a.sent_ok ? (uint32_t)(__ldg(a.T + off) != a.sent)
+                                  : (__ldg(a.bitmap + (off >> 5)) >> (off & 31u)) & 1u;
                 }
                 pres |= p << j;
                 np += p;
@@ -1411,7 +1478,7 @@ struct PjLevel {
     PjMj *mj;
     unsigned long long *mjtot;  // matches of the sort-merge buckets
     PjPackOut *pk;              // the packing's counts
-    uint32_t *dflags;           // [4] dense build side: [1] dense span, [2..3] distinct keys (u64)
+    uint32_t *dflags;           // [PJ_F_WORDS] flags of the dense build side (set by k_pj_range_init)
     PjPackCta *pkc;             // [nb / (PK_THREADS * 8) + 1] the pack CTAs' totals
     uint32_t *tg;               // [3][nb + PK_THREADS * PK_SEG] the packing's staging (group ends, flags)
     PjCross *tover;             // [nb + PK_THREADS * PK_SEG] the packing's staging (listed buckets)
@@ -1436,7 +1503,7 @@ size_t pj_level_bytes(uint32_t nb, bool learned) {
     add((size_t)nb * sizeof(PjMj));
     add(8);
     add(sizeof(PjPackOut));
-    add(16);
+    add(PJ_F_WORDS * 4);
     add(((size_t)nb / (PK_THREADS * 8) + 1) * sizeof(PjPackCta));
     add((size_t)3 * (nb + PK_THREADS * PK_SEG) * 4);
     add((size_t)(nb + PK_THREADS * PK_SEG) * sizeof(PjCross));
@@ -1467,7 +1534,7 @@ void pj_level_carve(char *p, uint32_t nb, bool learned, PjLevel *L) {
     L->mj = (PjMj *)take((size_t)nb * sizeof(PjMj));
     L->mjtot = (unsigned long long *)take(8);
     L->pk = (PjPackOut *)take(sizeof(PjPackOut));
-    L->dflags = (uint32_t *)take(16);
+    L->dflags = (uint32_t *)take(PJ_F_WORDS * 4);
     L->pkc = (PjPackCta *)take(((size_t)nb / (PK_THREADS * 8) + 1) * sizeof(PjPackCta));
     L->tg = (uint32_t *)take((size_t)3 * (nb + PK_THREADS * PK_SEG) * 4);
     L->tover = (PjCross *)take((size_t)(nb + PK_THREADS * PK_SEG) * sizeof(PjCross));
@@ -1605,7 +1672,7 @@ qg_status pj_compare(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot,
 // so the next call may overwrite it.
 struct PjPin {
     uint32_t h[1024];                 // [side R, S'][digit 0, 1][256]
-    uint32_t dflags[4];
+    uint32_t dflags[PJ_F_WORDS];
     PjPackOut pk;
     PjCross over[PJ_MAX_BUCKETS];
     uint32_t mm[2 * PJ_MAX_BUCKETS];  // [mins][maxes] of the listed buckets
@@ -1643,7 +1710,9 @@ uint32_t pj_bucket_count(long long nR, long long nS) {
 struct PjRSide {
     const int32_t *rkey, *rpay;
     bool rec_ready;       // R records (and h[0 .. 512)) exist
-    bool dense_ok;        // dense span, no duplicate key: bitmap and T describe R
+    bool dense_ok;        // dense span, no duplicate key: bitmap (or the sentinel) and T describe R
+    bool sent_ok;         // T holds `sent` where no R row is (no bitmap)
+    uint32_t sent;
     const uint32_t *bitmap, *T;
 };
 
@@ -1786,7 +1855,7 @@ qg_status pj_core(qg_ctx *ctx, const PjLevel &L, PjPin *pin, uint32_t nb, int lb
             const bool full = (unsigned long long)(kmax - kmin) + 1ull == (unsigned long long)nR;
             qg_lookback lb;
             QG_TRY(qg_lb_make(ctx, pk.groups, QG_SITE_JOIN_PROBE, &lb));
-            PdArgs da{s, L.gr, L.gs, rs.bitmap, rs.T, kmin, L.total, ok, oa, ob, cap};
+            PdArgs da{s, L.gr, L.gs, rs.bitmap, rs.T, kmin, rs.sent_ok ? 1u : 0u, rs.sent, L.total, ok, oa, ob, cap};
             qg_pre_launch(ctx);
             auto kern = full ? k_pj_join_dense<PB_THREADS, PB_SMAX, true> : k_pj_join_dense<PB_THREADS, PB_SMAX, false>;
             kern<<<pk.groups, PB_THREADS, sizeof(PdSmem<PB_SMAX, PB_WARPS>), ctx->stream>>>(da, lb);
@@ -2007,28 +2076,31 @@ static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const i
     unsigned long long *R = (unsigned long long *)aux, *Rsp = (unsigned long long *)(aux + rb);
     unsigned long long *S = (unsigned long long *)(aux + 2 * rb), *Ssp = (unsigned long long *)(aux + 2 * rb + sb);
     uint32_t *bitmap = (uint32_t *)(aux + 2 * rb + 2 * sb);
+    uint32_t *T = (uint32_t *)Rsp;  // the dense build side's payloads (2 nR entries at most)
     const uint32_t nb = pj_bucket_count(nR, nS);
     int lb2 = 0;
     while ((1u << lb2) < nb) lb2++;
     PjLevel L;
     pj_level_carve(aux + 2 * rb + 2 * sb + bmb, nb, variant != 1, &L);
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dh, 0, 4 * 256 * 4, ctx->stream), "memset dhist");
-    QG_TRY_CUDA(ctx, cudaMemsetAsync(L.dflags, 0, 16, ctx->stream), "memset flags");
     QG_TRY_CUDA(ctx, cudaMemsetAsync(bitmap, 0, bmb, ctx->stream), "memset bitmap");
     qg_pre_launch(ctx);
-    k_pj_range_init<<<1, 1, 0, ctx->stream>>>(L.range);
+    k_pj_range_init<<<1, 1, 0, ctx->stream>>>(L.range, L.dflags);
     QG_TRY(qg_check_launch(ctx, "k_pj_range_init"));
     qg_pre_launch(ctx);
-    k_pj_rrange<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, nR, L.range);
+    k_pj_rrange<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, L.range, L.dflags);
     QG_TRY(qg_check_launch(ctx, "k_pj_rrange"));
-    // R: presence bitmap + payload table (dense span), else records + digit histograms
+    // R: payload table (+ presence bitmap without a sentinel) on a dense span, else records + digit histograms
     qg_pre_launch(ctx);
-    k_pj_rtab<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, L.range, lb2, bitmap,
-                                                                 (uint32_t *)Rsp, L.dflags, R, L.dh);
+    k_pj_tfill<<<pj_grid(ctx, nR / 2, 256, 8), 256, 0, ctx->stream>>>(T, L.range, lb2, nR, L.dflags);
+    QG_TRY(qg_check_launch(ctx, "k_pj_tfill"));
+    qg_pre_launch(ctx);
+    k_pj_rtab<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(rkey, rpay, nR, L.range, lb2, bitmap, T,
+                                                                 L.dflags, R, L.dh);
     QG_TRY(qg_check_launch(ctx, "k_pj_rtab"));
     qg_pre_launch(ctx);
-    k_pj_distinct<<<pj_grid(ctx, (nR + 31) / 16, 256, 4), 256, 0, ctx->stream>>>(
-        bitmap, L.range, lb2, nR, reinterpret_cast<unsigned long long *>(L.dflags + 2));
+    k_pj_distinct<<<pj_grid(ctx, nR, 256, 8), 256, 0, ctx->stream>>>(
+        bitmap, T, L.range, lb2, nR, L.dflags, reinterpret_cast<unsigned long long *>(L.dflags + PJ_F_DISTINCT));
     QG_TRY(qg_check_launch(ctx, "k_pj_distinct"));
     // S filter with the S' digit histograms of the radix function
     constexpr int SF_TILE = SF_THREADS * SF_ROUNDS * 4;
@@ -2042,14 +2114,16 @@ static qg_status join_filter_sort_impl(qg_ctx *ctx, const int32_t *rkey, const i
     PjRange *hp = reinterpret_cast<PjRange *>(ctx->pinned + 4);
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(hp, L.range, sizeof(PjRange), cudaMemcpyDeviceToHost, ctx->stream), "range d2h");
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->h, L.dh, 4 * 256 * 4, cudaMemcpyDeviceToHost, ctx->stream), "dhist d2h");
-    QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->dflags, L.dflags, 16, cudaMemcpyDeviceToHost, ctx->stream), "flags d2h");
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(pin->dflags, L.dflags, PJ_F_WORDS * 4, cudaMemcpyDeviceToHost, ctx->stream), "flags d2h");
     QG_TRY(qg_collect_error(ctx));
     const PjRange hr = *hp;
     const long long ns1 = (long long)hr.count;
     unsigned long long distinct;
-    memcpy(&distinct, pin->dflags + 2, 8);
-    PjRSide rs{rkey, rpay, pin->dflags[1] == 0u, pin->dflags[1] != 0u && distinct == (unsigned long long)nR && g_pj_dense,
-               bitmap, (const uint32_t *)Rsp};
+    memcpy(&distinct, pin->dflags + PJ_F_DISTINCT, 8);
+    PjRSide rs{rkey, rpay, pin->dflags[PJ_F_DENSE] == 0u,
+               pin->dflags[PJ_F_DENSE] != 0u && distinct == (unsigned long long)nR && g_pj_dense,
+               pin->dflags[PJ_F_SENT_OK] != 0u, pin->dflags[PJ_F_SENT],
+               bitmap, T};
     long long M = 0;
     // pj_core ends with a read of the output count and the error word
     QG_TRY(pj_core(ctx, L, pin, nb, lb2, rs, R, Rsp, nR, S, Ssp, ns1, hr.kmin, hr.kmax, variant,

@@ -202,6 +202,7 @@ def dense_knob(ctx):
     ctx.join_set_dense(True)
 
 
+@pytest.mark.parametrize("wide_pay", [False, True])
 @pytest.mark.parametrize("nR,nS,gap,base", [
     (1, 5, 1, 7),
     (1000, 50000, 1, 0),
@@ -209,15 +210,20 @@ def dense_knob(ctx):
     (1 << 16, 1 << 20, 2, -(1 << 20)),      # every other key, all negative (one unsigned span)
     (50000, 3 << 20, 1, (1 << 31) - 25000),  # keys across 0x7fffffff / 0x80000000 (unsigned order)
 ])
-def test_join_dense_build_side(ctx, orc, knobs, dense_knob, nR, nS, gap, base):
-    # Unique R keys over a dense span: R becomes a presence bitmap and a payload
-    # table indexed by key - min, and only S is partitioned.  Equal to the
-    # oracle, to the general path (dense build side off) and to the learned
-    # partitioning (which takes the general path).
+def test_join_dense_build_side(ctx, orc, knobs, dense_knob, nR, nS, gap, base, wide_pay):
+    # Unique R keys over a dense span: R becomes a payload table indexed by
+    # key - min -- absent keys marked by a sentinel payload that no R row holds,
+    # or, when R's payloads span every candidate (wide_pay), by a presence
+    # bitmap -- and only S is partitioned.  Equal to the oracle, to the general
+    # path (dense build side off) and to the learned partitioning (which takes
+    # the general path).
     rng = np.random.default_rng(nR + nS + gap)
     rk = (rng.permutation(nR).astype(np.int64) * gap + base)
     rkey = ((rk + (1 << 31)) % (1 << 32) - (1 << 31)).astype(np.int32)
     rpay = rng.integers(-1000, 1000, nR).astype(np.int32)
+    if wide_pay:
+        rpay[0] = -(2 ** 31)
+        rpay[-1] = 2 ** 31 - 1
     sk = rng.integers(base - 300, base + nR * gap + 300, nS)
     skey = ((sk + (1 << 31)) % (1 << 32) - (1 << 31)).astype(np.int32)
     spay = rng.integers(0, 1000, nS).astype(np.int32)
