@@ -334,8 +334,8 @@ k_gbd_main(const int32_t *__restrict__ key, const int32_t *__restrict__ val, con
     }
 }
 
-// 4. Emit in key order.  Tile t (taken from the control block's tile counter,
-// so tiles start in order) covers entries [lo + t*4096, lo + (t+1)*4096) of the
+// 4. Emit in key order.  Tile t (CTA t: CTAs start in index order) covers
+// entries [lo + t*4096, lo + (t+1)*4096) of the
 // touched range [lo, hi]; in round r thread i reads entry r*256 + i of its
 // tile, so the loads, the cleared entries and (after a per-round rank) the
 // groups written are contiguous across a warp.  Tiles past the touched range
@@ -348,14 +348,9 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
            int32_t *__restrict__ gkey, long long *__restrict__ gsum, long long *__restrict__ gcnt, long long cap,
            long long *__restrict__ d_num, qg_lookback lb) {
     constexpr int NW = GBD_EMIT_THREADS / 32;
-    __shared__ uint32_t s_tile, s_epoch, s_total, s_off[GBD_EMIT_PER * NW], s_tmp[2 * NW];
+    __shared__ uint32_t s_epoch, s_total, s_off[GBD_EMIT_PER * NW], s_tmp[2 * NW];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) {
-        s_tile = atomicAdd(&lb.ctl->tile_ctr, 1u);
-        s_epoch = *(volatile uint32_t *)&lb.ctl->epoch;
-    }
-    __syncthreads();
-    const uint32_t tile = s_tile, epoch = s_epoch;
+    const uint32_t tile = blockIdx.x;  // CTAs start in index order: a tile's predecessors are running or done
     if (tile < 16) {
         constexpr int PER_TILE = GBD_S / 16;
         for (int i = tid; i < PER_TILE; i += GBD_EMIT_THREADS) img[tile * PER_TILE + i] = 0ull;
@@ -368,10 +363,10 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
     const bool any = st[G_OK] && umin <= hi;
     const uint32_t lo = umin & ~15u;
     const uint32_t last = any ? (hi - lo) / GBD_EMIT_TILE : 0u;
-    if (tile > last) {
-        qg_lb_end(lb);
-        return;
-    }
+    if (tile > last) return;  // reads no epoch: the last touched tile may advance it at any time
+    if (tid == 0) s_epoch = *(volatile uint32_t *)&lb.ctl->epoch;
+    __syncthreads();
+    const uint32_t epoch = s_epoch;
     const uint32_t kbase = st[G_KBASE];
     const bool xtra = st[G_EXTRA] != 0;
     const unsigned long long mask = (1ull << shift) - 1ull;
@@ -433,7 +428,9 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
         }
         dense[i] = 0ull;
     }
-    qg_lb_end(lb);
+    // The last touched tile ends after every earlier tile published (its
+    // look-back waited for them), so each of them has read the epoch already.
+    qg_lb_finish(lb, tile, last, epoch);
 }
 
 }  // namespace
