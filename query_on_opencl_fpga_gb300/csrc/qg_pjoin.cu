@@ -688,7 +688,7 @@ struct PbSmem {
     uint32_t next[PB_RMAX];         // 1 + next R row of the chain, 0 = end
     uint32_t wsum[PB_WARPS];
     uint32_t red[2 * PB_WARPS];
-    uint32_t tile, epoch, excl, pad;
+    uint32_t tile, epoch, excl, total;
 };
 
 struct PbArgs {
@@ -743,88 +743,137 @@ k_pj_join(PbArgs a, qg_lookback lb) {
     const uint32_t sb = a.sbeg[b], sn = a.sbeg[b + 1] - sb;
     const bool outside = a.big[b] != 0;
     bool work = !outside && rn > 0 && sn > 0;
-    if (work && (rn > (uint32_t)PB_RMAX || sn > (uint32_t)PB_SMAX)) {  // host sends these outside
+    if (work && (rn > (uint32_t)PB_RMAX || sn > (uint32_t)PB_SMAX)) {  // the packing sends these outside
         if (tid == 0) qg_record_error(lb.ctl, QG_ERR_INVALID, QG_SITE_PJ_BUCKET);
         work = false;
     }
-    uint32_t my_cnt = 0;      // matches of this thread's rows
-    uint32_t q = 0, r0 = 0;   // this warp's segment of sorted rows
+    // S' rows -> registers, each probed against R's chained table right away:
+    // the group's output count is then known before any sorting and is
+    // published at once (successors' look-backs wait less).  Only rows with
+    // matches are sorted.
+    unsigned long long it[PB_IPT];
+    uint32_t cf[PB_IPT];  // per row: matches << 16 | 1 + first matching R row (0: none)
+    uint32_t my_m = 0;
+    uint32_t kmn = 0xffffffffu, kmx = 0;
     if (work) {
-        // R rows -> chained table
         for (uint32_t i = tid; i < PB_HEADS; i += PB_THREADS) S.head[i] = 0;
         for (uint32_t i = tid; i < rn; i += PB_THREADS) {
             const unsigned long long v = __ldg(a.R + rb + i);
             S.rk[i] = (uint32_t)(v >> 32);
             S.rp[i] = (uint32_t)v;
         }
-        // S' rows -> registers, key range of the bucket
-        unsigned long long it[PB_IPT];
-        uint32_t kmn = 0xffffffffu, kmx = 0;
 #pragma unroll
         for (int j = 0; j < PB_IPT; j++) {
             const uint32_t i = j * PB_THREADS + tid;
             it[j] = i < sn ? __ldg(a.S + sb + i) : 0ull;
-            if (i < sn) {
-                const uint32_t k = (uint32_t)(it[j] >> 32);
-                kmn = min(kmn, k);
-                kmx = max(kmx, k);
-            }
         }
-        kmn = __reduce_min_sync(QG_FULL_MASK, kmn);
-        kmx = __reduce_max_sync(QG_FULL_MASK, kmx);
-        if (lane == 0) { S.red[warp] = kmn; S.red[PB_WARPS + warp] = kmx; }
         __syncthreads();
         for (uint32_t i = tid; i < rn; i += PB_THREADS)
             S.next[i] = atomicExch(&S.head[pb_hash(S.rk[i])], i + 1);
-        kmn = 0xffffffffu;
-        kmx = 0;
+        __syncthreads();
 #pragma unroll
-        for (int w = 0; w < PB_WARPS; w++) {
-            kmn = min(kmn, S.red[w]);
-            kmx = max(kmx, S.red[PB_WARPS + w]);
+        for (int j = 0; j < PB_IPT; j++) {
+            cf[j] = 0;
+            if (j * PB_THREADS + tid < sn) {
+                const uint32_t k = (uint32_t)(it[j] >> 32);
+                uint32_t m = 0, first = 0;
+                for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1])
+                    if (S.rk[e - 1] == k) {
+                        first = m ? first : e;
+                        m++;
+                    }
+                cf[j] = (m << 16) | first;
+                my_m += m;
+                if (m) {
+                    kmn = min(kmn, k);
+                    kmx = max(kmx, k);
+                }
+            }
         }
-        const uint32_t span1 = kmx - kmn;  // span - 1
-        if (span1 < (uint32_t)PB_CSPAN) {
+    }
+    // the group's count (an outside group's comes from its own path) and the
+    // matching rows' key range
+    {
+        const uint32_t wm = __reduce_add_sync(QG_FULL_MASK, my_m);
+        const uint32_t wn = __reduce_min_sync(QG_FULL_MASK, kmn), wx = __reduce_max_sync(QG_FULL_MASK, kmx);
+        if (lane == 0) {
+            S.wsum[warp] = wm;
+            S.red[warp] = wn;
+            S.red[PB_WARPS + warp] = wx;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t t = 0;
+#pragma unroll
+        for (int w = 0; w < PB_WARPS; w++) t += S.wsum[w];
+        S.total = outside ? (uint32_t)a.bigcnt[b] : t;
+        qg_lb_publish_agg(lb, b, S.epoch, S.total);
+    }
+    kmn = 0xffffffffu;
+    kmx = 0;
+#pragma unroll
+    for (int w = 0; w < PB_WARPS; w++) {
+        kmn = min(kmn, S.red[w]);
+        kmx = max(kmx, S.red[PB_WARPS + w]);
+    }
+    __syncthreads();  // S.wsum is read above and rewritten below
+    uint32_t ns = 0;  // matching rows, sorted by key into S.s[0 .. ns)
+    if (work) {
+        uint32_t hit = 0;
+#pragma unroll
+        for (int j = 0; j < PB_IPT; j++) hit |= (cf[j] >> 16 ? 1u : 0u) << j;
+        uint32_t nh = __popc(hit), tot;
+        const uint32_t hoff = pb_excl(nh, S.wsum, &tot);  // this thread's first place among the matching rows
+        ns = tot;
+        const uint32_t span1 = kmx - kmn;  // key span of the matching rows, minus one (read when ns > 0)
+        if (ns > 0 && span1 < (uint32_t)PB_CSPAN) {
             // counting sort by (key - kmn); the order among equal keys is free
             for (uint32_t i = tid; i <= span1; i += PB_THREADS) S.cnt[i] = 0;
             __syncthreads();
             uint32_t rk[PB_IPT];
 #pragma unroll
-            for (int j = 0; j < PB_IPT; j++) {
-                const uint32_t i = j * PB_THREADS + tid;
-                if (i < sn) rk[j] = atomicAdd(&S.cnt[(uint32_t)(it[j] >> 32) - kmn], 1u);
-            }
+            for (int j = 0; j < PB_IPT; j++)
+                if ((hit >> j) & 1u) rk[j] = atomicAdd(&S.cnt[(uint32_t)(it[j] >> 32) - kmn], 1u);
             __syncthreads();
             constexpr int PER = PB_CSPAN / PB_THREADS;
             const uint32_t c0 = tid * PER;
-            uint32_t loc[PER], sum = 0;
+            uint32_t sum = 0;
+#pragma unroll
+            for (int e = 0; e < PER; e++) sum += (c0 + e <= span1) ? S.cnt[c0 + e] : 0u;
+            uint32_t t2;
+            uint32_t run = pb_excl(sum, S.wsum, &t2);
 #pragma unroll
             for (int e = 0; e < PER; e++) {
-                loc[e] = (c0 + e <= span1) ? S.cnt[c0 + e] : 0u;
-                sum += loc[e];
-            }
-            uint32_t tot;
-            uint32_t run = pb_excl(sum, S.wsum, &tot);
-#pragma unroll
-            for (int e = 0; e < PER; e++) {
-                if (c0 + e <= span1) S.cnt[c0 + e] = run;
-                run += loc[e];
+                if (c0 + e <= span1) {
+                    const uint32_t c = S.cnt[c0 + e];
+                    S.cnt[c0 + e] = run;
+                    run += c;
+                }
             }
             __syncthreads();
+            uint32_t pos[PB_IPT];
 #pragma unroll
-            for (int j = 0; j < PB_IPT; j++) {
-                const uint32_t i = j * PB_THREADS + tid;
-                if (i < sn) S.s[S.cnt[(uint32_t)(it[j] >> 32) - kmn] + rk[j]] = it[j];
-            }
-        } else {
-            // wide key span: bitonic sort of the rows, padded with all-ones
+            for (int j = 0; j < PB_IPT; j++)
+                if ((hit >> j) & 1u) {
+                    pos[j] = S.cnt[(uint32_t)(it[j] >> 32) - kmn] + rk[j];
+                    S.s[pos[j]] = it[j];
+                }
+            __syncthreads();
+            // the counters are dead: each sorted row keeps its count and first match there
+#pragma unroll
+            for (int j = 0; j < PB_IPT; j++)
+                if ((hit >> j) & 1u) S.cnt[pos[j]] = cf[j];
+        } else if (ns > 0) {
+            // wide key span: bitonic sort of the matching rows (padded with
+            // all-ones), then each sorted row is probed again for its matches
+            uint32_t o = hoff;
+#pragma unroll
+            for (int j = 0; j < PB_IPT; j++)
+                if ((hit >> j) & 1u) S.s[o++] = it[j];
             uint32_t P = 1;
-            while (P < sn) P <<= 1;
-#pragma unroll
-            for (int j = 0; j < PB_IPT; j++) {
-                const uint32_t i = j * PB_THREADS + tid;
-                if (i < P) S.s[i] = i < sn ? it[j] : ~0ull;
-            }
+            while (P < ns) P <<= 1;
+            for (uint32_t i = ns + tid; i < P; i += PB_THREADS) S.s[i] = ~0ull;
             __syncthreads();
             for (uint32_t k = 2; k <= P; k <<= 1) {
                 for (uint32_t j = k >> 1; j > 0; j >>= 1) {
@@ -838,38 +887,36 @@ k_pj_join(PbArgs a, qg_lookback lb) {
                     __syncthreads();
                 }
             }
-        }
-        __syncthreads();
-        // probe: warp w owns sorted rows [w * PB_WSEG, (w + 1) * PB_WSEG), taken
-        // 32 at a time (lane L has row step * 32 + L), so that the matches of
-        // a step are consecutive in the output and their stores coalesce
-        r0 = min(sn, (uint32_t)warp * PB_WSEG);
-        q = min(sn, r0 + PB_WSEG) - r0;
-        // The counting-sort counters are dead now: each row keeps its match
-        // count and first match there (count << 16 | 1 + R row) for the write.
-        for (uint32_t r = r0 + lane; r < r0 + q; r += 32) {
-            const uint32_t k = (uint32_t)(S.s[r] >> 32);
-            uint32_t m = 0, first = 0;
-            for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1])
-                if (S.rk[e - 1] == k) {
-                    first = m ? first : e;
-                    m++;
-                }
-            S.cnt[r] = (m << 16) | first;
-            my_cnt += m;
+            for (uint32_t r = tid; r < ns; r += PB_THREADS) {
+                const uint32_t k = (uint32_t)(S.s[r] >> 32);
+                uint32_t m = 0, first = 0;
+                for (uint32_t e = S.head[pb_hash(k)]; e; e = S.next[e - 1])
+                    if (S.rk[e - 1] == k) {
+                        first = m ? first : e;
+                        m++;
+                    }
+                S.cnt[r] = (m << 16) | first;
+            }
         }
     }
-    // warp totals -> warp offsets within the bucket
+    __syncthreads();
+    // warp w writes the matches of sorted rows [w * PB_WSEG, ...), 32 at a time
+    // (lane L has row step * 32 + L), so that a step's matches are consecutive
+    // in the output and their stores coalesce
+    const uint32_t r0 = min(ns, (uint32_t)warp * PB_WSEG);
+    const uint32_t q = min(ns, r0 + PB_WSEG) - r0;
+    uint32_t my_cnt = 0;
+    for (uint32_t r = r0 + lane; r < r0 + q; r += 32) my_cnt += S.cnt[r] >> 16;
     const uint32_t wcnt = __reduce_add_sync(QG_FULL_MASK, my_cnt);
-    uint32_t total;
-    const uint32_t my_off = pb_excl(lane == 0 ? wcnt : 0u, S.wsum, &total);  // lane 0 holds its warp's offset
+    uint32_t tot3;
+    const uint32_t my_off = pb_excl(lane == 0 ? wcnt : 0u, S.wsum, &tot3);  // lane 0 holds its warp's offset
     const uint32_t warp_off = __shfl_sync(QG_FULL_MASK, my_off, 0);
-    const uint32_t bucket_cnt = outside ? (uint32_t)a.bigcnt[b] : total;
+    const uint32_t total = S.total;
     if (warp == 0) {
-        const uint32_t excl = qg_lb_warp_exclusive(lb, b, S.epoch, bucket_cnt);
+        const uint32_t excl = qg_lb_warp_lookback(lb, b, S.epoch, total);
         if (lane == 0) {
             S.excl = excl;
-            if (b == gridDim.x - 1) *a.total = (unsigned long long)excl + bucket_cnt;
+            if (b == gridDim.x - 1) *a.total = (unsigned long long)excl + total;
             if (outside) a.off[b] = excl;
         }
     }

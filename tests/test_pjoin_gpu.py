@@ -274,3 +274,31 @@ def test_join_dense_oversize_bucket_falls_back(ctx, orc):
     st = ctx.join_stats()
     assert st["path"] == "radix" and st["outside_buckets"] > 0, st
     check_join(got, orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 299, cap=skey.size + 16, mt=True))
+
+
+@pytest.mark.parametrize("full", [True, False])
+def test_join_dense_capacity_error(ctx, orc, full):
+    # The dense bucket kernel writes only below `cap` and the call reports the
+    # size needed (QG_ERR_CAPACITY); the wrapper then retries with it.  With
+    # and without every S' row matching (a permutation of the span, or gaps).
+    from ctypes import byref, c_int64, c_void_p
+
+    rng = np.random.default_rng(41)
+    nR, nS = 1 << 14, 1 << 18
+    rkey = (rng.permutation(nR) * (1 if full else 2)).astype(np.int32)
+    rpay = rng.integers(0, 1000, nR).astype(np.int32)
+    skey = rng.integers(0, nR * (1 if full else 2), nS).astype(np.int32)
+    spay = rng.integers(0, 1000, nS).astype(np.int32)
+    exp = orc.join_filter_sort(rkey, rpay, skey, spay, -(2 ** 31), 299, cap=nS + 16, mt=True)
+    need = len(exp[0])
+    r, rp, s, sp = (dev(a) for a in (rkey, rpay, skey, spay))
+    small = need // 3
+    out = [torch.full((small + 64,), 7, dtype=torch.int32, device="cuda") for _ in range(3)]
+    m = c_int64()
+    p = lambda t: c_void_p(t.data_ptr())  # noqa: E731
+    st = ctx.lib.qg_join_filter_sort(ctx.handle, p(r), p(rp), nR, p(s), p(sp), nS, -(2 ** 31), 299,
+                                     p(out[0]), p(out[1]), p(out[2]), small, byref(m))
+    assert st == 3 and m.value == need
+    assert ctx.join_stats()["path"] == "dense"
+    assert all(int((o[small:] != 7).sum()) == 0 for o in out), "a row was written past cap"
+    check_join(ctx.join_filter_sort(r, rp, s, sp, -(2 ** 31), 299), exp)
