@@ -95,6 +95,7 @@ enum {
 };
 static_assert(G_WORDS <= 48, "gbd state words");
 static_assert(GBD_RUNS_PER_CTA * GBD_RUN * 2 <= GBD_SSLOTS, "sample table load <= 1/2");
+static_assert(GBD_SSLOTS % GBD_RUN == 0 && GBD_RUN % 32 == 0, "the sample's flush walks the table in whole warps");
 static_assert(GBD_LIST % GBD_CANDS_THREADS == 0, "cands: whole list per CTA");
 static_assert(2 * (1 << GBD_TLOG2) % (GBD_EMIT_TILES * GBD_EMIT_THREADS * 4) == 0, "emit clears the sketch");
 static_assert(GBD_EMIT_PER * (GBD_EMIT_THREADS / 32) % 32 == 0, "emit cells per lane");
@@ -166,13 +167,20 @@ k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_
     }
     __syncthreads();
     uint32_t *mine = lst + (size_t)blockIdx.x * GBD_LIST;
-    for (int sl = threadIdx.x; sl < GBD_SSLOTS; sl += GBD_RUN) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (int sl = threadIdx.x; sl < GBD_SSLOTS; sl += GBD_RUN) {  // GBD_SSLOTS % GBD_RUN == 0: whole warps
         const uint32_t c = tcnt[sl];
-        if (!c) continue;
         const uint32_t kk = tkey[sl];
-        atomicAdd(sketch + gbd_h1(kk), c);  // result unused: compiled as a reduction
-        atomicAdd(sketch + (1u << GBD_TLOG2) + gbd_h2(kk), c);
-        mine[atomicAdd(&s_n, 1u)] = kk;
+        if (c) {
+            atomicAdd(sketch + gbd_h1(kk), c);  // result unused: compiled as a reduction
+            atomicAdd(sketch + (1u << GBD_TLOG2) + gbd_h2(kk), c);
+        }
+        // one list reservation per warp (a single shared counter would serialise the keys)
+        const uint32_t m = __ballot_sync(QG_FULL_MASK, c != 0u);
+        uint32_t at = 0;
+        if (lane == 0 && m) at = atomicAdd(&s_n, (uint32_t)__popc(m));
+        at = __shfl_sync(QG_FULL_MASK, at, 0);
+        if (c) mine[at + __popc(m & qg_lanemask_lt())] = kk;
     }
     lmin = __reduce_min_sync(QG_FULL_MASK, lmin);
     lmax = __reduce_max_sync(QG_FULL_MASK, lmax);
