@@ -85,6 +85,7 @@ SIGNATURES: dict[str, tuple] = {
                                  POINTER(c_int64)]),
     "qg_join_set_knobs": (c_int, [c_int, c_int, c_uint32, c_uint32]),
     "qg_join_set_dense": (c_int, [c_int]),
+    "qg_sort_set_rank": (c_int, [c_int]),
     "qg_join_stats": (c_int, [c_void_p, c_void_p]),
     "qg_part_model_bytes": (c_int64, []),
     "qg_reduce_rec": (c_int, [c_void_p, c_void_p, c_int64, c_int, POINTER(c_uint32)]),

@@ -94,9 +94,11 @@ __device__ __forceinline__ uint32_t rs_digit(uint32_t k, uint32_t key_off, int s
 // DIG: 0 radix digit of the key, 1 learned partition function of the key,
 // 2 bits of the bucket id in the source's sidecar (REC only).
 // RANK: how an item's rank within its digit is found -- 0 eight warp ballots,
-// 1 one match instruction (stable either way), 2 one shared-memory atomic on
-// the tile's digit counter (not stable: for a first LSD pass whose order
-// among equal digits nothing after it needs).
+// 1 one match instruction, 3 one match instruction on the digit's high four
+// bits (at most 16 groups, where match is fast) and four ballots on the low
+// four (stable all three), 2 one shared-memory atomic on the tile's digit
+// counter (not stable: for a first LSD pass whose order among equal digits
+// nothing after it needs).
 template <bool KV3, int DIG, int RANK = 0>
 __global__ void __launch_bounds__(RS_THREADS, 4)
 k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_t key_off,
@@ -197,6 +199,16 @@ k_radix_pass(qg_sort_bufs src, qg_sort_bufs dst, long long n, int shift, uint32_
         uint32_t peers;
         if (RANK == 1) {
             peers = __match_any_sync(QG_FULL_MASK, valid ? d : 256u);  // the tail's invalid lanes share 256
+        } else if (RANK == 3) {
+            peers = __match_any_sync(QG_FULL_MASK, valid ? d >> 4 : 16u);  // the tail's invalid lanes share 16
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const uint32_t bal = __ballot_sync(QG_FULL_MASK, (d >> b) & 1u);
+                peers &= ((d >> b) & 1u) ? bal : ~bal;
+            }
+        } else if (RANK == 4) {
+            peers = __match_any_sync(QG_FULL_MASK, valid ? d >> 4 : 16u) &
+                    __match_any_sync(QG_FULL_MASK, valid ? d & 15u : 16u);
         } else {
             peers = __ballot_sync(QG_FULL_MASK, valid);
 #pragma unroll
@@ -361,6 +373,10 @@ static qg_status rs_set_attr(qg_ctx *ctx) {
                                               (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
         QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
+        QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
         if constexpr (!KV3)
             QG_TRY_CUDA(ctx, cudaFuncSetAttribute(k_radix_pass<KV3, DIG, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   (int)sizeof(RsSmem<KV3, DIG == 2>)), "attr");
@@ -374,6 +390,20 @@ static qg_status rs_set_attr(qg_ctx *ctx) {
 // sort of 20-bit keys, 1.30 -> 1.22 ms over its passes), while passes with
 // many digit values were slower with it (the join's partition passes 1.10 ->
 // 1.38 ms) and keep the eight ballots.
+// Stable ranking of the passes with many digit values: -1 by caller, else
+// forced -- 0 eight ballots, 3 a match on the high four bits and four ballots,
+// 4 a match on each half (ANDed).  Measured on GB300: the 64M-record sort's
+// passes took 1.222 / 1.137 / 1.098 ms with 0 / 3 / 4, the join's stable
+// partition pass 0.778 / 0.766 / 0.855 ms; so sorts take 4 and the join's
+// partition passes 3.
+static int g_rs_stable_rank = -1;
+
+extern "C" QG_API qg_status qg_sort_set_rank(int mode) {
+    if (mode != -1 && mode != 0 && mode != 3 && mode != 4) return QG_ERR_INVALID;
+    g_rs_stable_rank = mode;
+    return QG_OK;
+}
+
 static bool rs_few_digits(const uint32_t *hb, long long n) {
     int used = 0;
     for (int d = 0; d < QG_RADIX; d++) {
@@ -416,11 +446,13 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
         const int shift = (pf.learned || side) ? 8 * p : pf.shift + 8 * p;
         const bool m = rs_few_digits(h_bases + p * QG_RADIX, n);
         // the first pass of a caller that needs only the grouping need not be stable
-        const int rk = (first_unstable && i == 0 && !kv3) ? 2 : (m ? 1 : 0);
-        auto kern = kv3 ? (m ? k_radix_pass<true, 0, 1> : k_radix_pass<true, 0, 0>)
-                    : side ? (rk == 2 ? k_radix_pass<false, 2, 2> : rk == 1 ? k_radix_pass<false, 2, 1> : k_radix_pass<false, 2, 0>)
-                    : pf.learned ? (rk == 2 ? k_radix_pass<false, 1, 2> : rk == 1 ? k_radix_pass<false, 1, 1> : k_radix_pass<false, 1, 0>)
-                                 : (rk == 2 ? k_radix_pass<false, 0, 2> : rk == 1 ? k_radix_pass<false, 0, 1> : k_radix_pass<false, 0, 0>);
+        // the join's partitions (first_unstable) rank with 3, sorts with 4
+        const int sr = g_rs_stable_rank >= 0 ? g_rs_stable_rank : (first_unstable ? 3 : 4);
+        const int rk = (first_unstable && i == 0 && !kv3) ? 2 : (m ? 1 : sr);
+        auto kern = kv3 ? (m ? k_radix_pass<true, 0, 1> : sr == 3 ? k_radix_pass<true, 0, 3> : sr == 4 ? k_radix_pass<true, 0, 4> : k_radix_pass<true, 0, 0>)
+                    : side ? (rk == 2 ? k_radix_pass<false, 2, 2> : rk == 1 ? k_radix_pass<false, 2, 1> : rk == 3 ? k_radix_pass<false, 2, 3> : rk == 4 ? k_radix_pass<false, 2, 4> : k_radix_pass<false, 2, 0>)
+                    : pf.learned ? (rk == 2 ? k_radix_pass<false, 1, 2> : rk == 1 ? k_radix_pass<false, 1, 1> : rk == 3 ? k_radix_pass<false, 1, 3> : rk == 4 ? k_radix_pass<false, 1, 4> : k_radix_pass<false, 1, 0>)
+                                 : (rk == 2 ? k_radix_pass<false, 0, 2> : rk == 1 ? k_radix_pass<false, 0, 1> : rk == 3 ? k_radix_pass<false, 0, 3> : rk == 4 ? k_radix_pass<false, 0, 4> : k_radix_pass<false, 0, 0>);
         qg_pre_launch(ctx);
         kern<<<(unsigned)tiles, RS_THREADS, smem, ctx->stream>>>(s, d, n, shift, (kv3 || !(side || pf.learned)) ? pf.kmin : 0u,
                                                                  pf.learned && !side ? pf.model : nullptr,

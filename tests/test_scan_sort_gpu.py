@@ -90,3 +90,21 @@ def test_sort_is_stable_lsd(ctx):
     got = ctx.sort_rec(dev(rin)).cpu().numpy()
     order = np.argsort(rin[:, 1], kind="stable")
     assert np.array_equal(got, rin[order])
+
+
+@pytest.mark.parametrize("mode", [0, 3, 4])
+def test_sort_ranking_modes_stable(ctx, mode):
+    # Every stable ranking form of the radix passes (eight ballots; a match on
+    # the digit's high half and four ballots; a match on each half) gives the
+    # same stable sort, over keys using every digit value and a ragged tail.
+    assert ctx.lib.qg_sort_set_rank(mode) == 0
+    try:
+        n = 300001
+        rng = np.random.default_rng(mode + 5)
+        rin = np.stack([np.arange(n), rng.integers(0, 1 << 32, n, dtype=np.int64)], 1).astype(np.uint32).view(np.int32)
+        rin = np.ascontiguousarray(rin)
+        got = ctx.sort_rec(dev(rin)).cpu().numpy()
+        order = np.argsort(rin[:, 1].view(np.uint32), kind="stable")
+        assert np.array_equal(got, rin[order])
+    finally:
+        assert ctx.lib.qg_sort_set_rank(-1) == 0
