@@ -9,29 +9,41 @@
 // order among equal keys is unspecified (the reference's bitonic sort is not
 // stable either).
 //
-// Pipeline (one GPU, all data in HBM):
-//   1. R columns -> R records (key << 32 | payload) and R's key range.
+// Pipeline (one GPU, all data in HBM; two host reads before the last):
+//   1. R's key and payload ranges.  When R's keys are unique over at most
+//      2 nR values (the dense build side), R becomes a table indexed by
+//      key - kmin: payloads, with a sentinel payload (or a presence bitmap)
+//      marking absent keys, and R is never partitioned.  Otherwise R's
+//      records (key << 32 | payload) and their radix digit histograms.
 //   2. S: filter on S.payload and on R's key range, compacted in one pass
 //      into S' records (key << 32 | S.payload); the order of S' is free, so
-//      each tile takes its output range with one atomic.
+//      each tile takes its output range with one atomic.  The filter also
+//      counts the S' radix digit histograms.  Host read 1: ranges, counts,
+//      histograms, dense flags.
 //   3. A partition function maps keys to B buckets (key ranges): radix over
 //      (k - kmin), or a learned piecewise-linear CDF model fitted on a sample
-//      (qg_part.cuh).  Bucket histograms of R and S', then one or two stable
-//      onesweep radix passes over the bucket id (qg_sort.cu) put both sides
-//      in bucket order.
-//   4. One CTA per bucket (tickets in bucket order): the bucket's R rows go
-//      into a shared-memory chained table, its S' rows are counting-sorted by
-//      key in shared memory (bitonic sort when the bucket's key span is
-//      wide), every S' row is probed, the bucket's output count is published
-//      and its output offset found by decoupled look-back, and the matches are
-//      written in key order.  Buckets are key ranges, so the output is sorted
-//      with no global sort pass.
-//   5. Buckets too large for shared memory: a bucket with one key is a cross
-//      product (k_pj_cross); all the others are gathered, sorted by key and
-//      merge-joined together (k_pj_mj_*: a fixed number of launches however
-//      many such buckets there are).  Their match counts are known before
-//      step 4, which publishes every such bucket's output offset; the writes
-//      of step 5 read it.
+//      (qg_part.cuh).  One or two onesweep radix passes over the bucket id
+//      (qg_sort.cu; the first need not be stable) put S' -- and R on the
+//      general path -- in bucket order.
+//   4. Bucket bounds, and consecutive buckets packed into join groups on the
+//      device (k_pj_pack / k_pj_place).  Host read 2: the group count.
+//   5. One CTA per group (tickets in group order).  Dense build side
+//      (k_pj_join_dense): each S' row matches when its key's table entry is
+//      filled, the count is published at once, the matching rows are
+//      counting-sorted and written in key order (with R's keys filling their
+//      span every row matches, and no look-back is needed).  General path
+//      (k_pj_join): R's rows in a shared-memory chained table, S' rows probed
+//      in registers, the count published, the matching rows sorted and their
+//      matches written in key order.  Groups are key ranges, so the output
+//      is sorted with no global sort pass.
+//   6. Buckets too large for shared memory (general path): a bucket with one
+//      key is a cross product (k_pj_cross); all the others are gathered,
+//      sorted by key and merge-joined together (k_pj_mj_*: a fixed number of
+//      launches however many such buckets there are).  Their match counts are
+//      known before step 5, which publishes every such bucket's output
+//      offset; the writes of step 6 read it.  On the dense side an oversize
+//      bucket sends the call to the general path (R's records made then, the
+//      S' partitioning reused).
 #include <algorithm>
 #include <string.h>
 #include <vector>
