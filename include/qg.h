@@ -289,13 +289,19 @@ QG_API qg_status qg_split_rec(qg_ctx *ctx, const void *in_records, int64_t n, in
  * batch owns a private context whose work arenas the graph addresses.
  * Inputs and outputs stay the caller's and must stay valid while the batch
  * exists.  Joins in a batch use the global hash table + device-planned sort;
- * group-by outputs are unordered (QG_ORDER_NONE).  Errors of a replay (a
- * join over cap: QG_ERR_CAPACITY; a group-by spill overflow:
- * QG_ERR_TABLE_FULL) are reported by qg_batch_check. */
+ * group-by outputs are unordered (QG_ORDER_NONE).  A group-by query on the
+ * default variant is run once at creation on the dense-window path; when its
+ * keys fit a window, the graph takes that path for it (sync-free, output in
+ * key order), else the two-pass path.  Errors of a replay (a join over cap:
+ * QG_ERR_CAPACITY; a group-by spill overflow: QG_ERR_TABLE_FULL; new data in
+ * a dense-window query's buffers whose keys no longer fit a window:
+ * QG_ERR_UNSUPPORTED, create the batch again) are reported by
+ * qg_batch_check. */
 typedef enum { QG_OP_FILTER = 0, QG_OP_GROUPBY = 1, QG_OP_FUSED = 2, QG_OP_JOIN = 3 } qg_op;
 typedef struct {
     int op;                /* qg_op */
-    int variant;           /* -1 default; filter 0, 1 or 2 (default 2); group-by 0 two-pass (default), 1 global table, 2 two-pass 64-bit adds */
+    int variant;           /* -1 default; filter 0, 1 or 2 (default 2); group-by 0 dense window when the keys fit one, else
+                              two-pass (default), 1 global table, 2 two-pass 64-bit adds, 3 two-pass */
     int64_t n;             /* rows (join: S rows) */
     int64_t n2;            /* join: R rows */
     const int32_t *in[4];  /* filter: key, payload; group-by: key, value, value2 (fused); join: rkey, rpay, skey, spay */

@@ -64,6 +64,7 @@ struct qg_batch {
     cudaGraphExec_t exec = nullptr;
     int32_t info[4] = {0, 0, 0, 0};  // hot slots / group tile log2, table factor, best replay us, graph nodes
     bool persistent = false;
+    std::vector<char> gdense;        // lanes: the group-by query takes the dense-window path
     std::vector<int> pq;             // queries of the persistent kernel
     qg_bpersist *bp = nullptr;       // its state (of the kept graph)
 };
@@ -92,6 +93,12 @@ qg_status enqueue(qg_batch *b, const BatchCfg &c, qg_bpersist *bp) {
             break;
         case QG_OP_GROUPBY:
         case QG_OP_FUSED:
+            if (i < b->gdense.size() && b->gdense[i]) {
+                st = qg_groupby_dense_async(ctx, q.in[0], q.in[1], q.op == QG_OP_FUSED ? q.in[2] : nullptr, q.lo,
+                                            q.hi, q.n, (int32_t *)q.out[0], (int64_t *)q.out[1],
+                                            (int64_t *)q.out[2], q.cap, q.d_count);
+                break;
+            }
             st = qg_groupby_set_knobs(v, c.hot_log2, 0, 0);
             if (st == QG_OK)
                 st = qg_groupby_cols_async(ctx, q.in[0], q.in[1], q.op == QG_OP_FUSED ? q.in[2] : nullptr, q.lo,
@@ -213,6 +220,22 @@ QG_API qg_status qg_batch_create(const qg_query *queries, int nq, int autotune, 
             b->lane[i] = best;
             load[best] += rows(i);
         }
+    }
+    // Lanes: a group-by query on the default variant (dense window first) is
+    // run once on the dense-window path; when every row fell in the window the
+    // captured form takes that path too, sync-free (rows outside the window on
+    // a later replay are reported, QG_ERR_UNSUPPORTED, not handed over to the
+    // two-pass path, which needs a host read).  The others keep the sync-free
+    // two-pass path.
+    b->gdense.assign(nq, 0);
+    for (int i = 0; i < nq && st == QG_OK && !b->persistent; i++) {
+        const qg_query &q = b->q[i];
+        if ((q.op != QG_OP_GROUPBY && q.op != QG_OP_FUSED) || (q.variant >= 0 && q.variant != 0)) continue;
+        bool ok = false;
+        st = qg_groupby_dense_probe(b->own[b->lane[i]], q.in[0], q.in[1], q.op == QG_OP_FUSED ? q.in[2] : nullptr,
+                                    q.lo, q.hi, q.n, (int32_t *)q.out[0], (int64_t *)q.out[1], (int64_t *)q.out[2],
+                                    q.cap, q.d_count, &ok);
+        b->gdense[i] = ok ? 1 : 0;
     }
     std::vector<BatchCfg> cands;
     if (autotune) {

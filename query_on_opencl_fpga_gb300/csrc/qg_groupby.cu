@@ -1387,6 +1387,48 @@ extern "C" QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *ke
     return qg_check_launch(ctx, "k_gb_flags_to_error");
 }
 
+namespace {
+// Sync-free dense-window group-by: a row outside the window (which the
+// synchronous form would hand to the two-pass path) is reported instead.
+__global__ void k_gbd_outside_error(qg_control *ctl) {
+    if (ctl->gbd[QG_GBD_OUTSIDE]) qg_record_error(ctl, QG_ERR_UNSUPPORTED, QG_SITE_GROUPBY);
+}
+}  // namespace
+
+// The dense-window path without a host round trip (batches): output in key
+// order, the group count in *d_num; keys outside the sampled window are
+// reported as QG_ERR_UNSUPPORTED by qg_ctx_check (nothing valid is written).
+qg_status qg_groupby_dense_async(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
+                                 int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt,
+                                 int64_t cap, int64_t *d_num) {
+    if (!ctx || n < 0 || cap < 0 || !d_num || (n > 0 && (!key || !val))) return QG_ERR_INVALID;
+    if ((((uintptr_t)key) | ((uintptr_t)val) | ((uintptr_t)val2)) & 15) return QG_ERR_INVALID;
+    if (n == 0 || n >= (1LL << 32))
+        return qg_groupby_cols_async(ctx, key, val, val2, lo2, hi2, n, gkey, gsum, gcnt, cap, QG_ORDER_NONE, d_num);
+    QG_TRY(qg_gbd_launch(ctx, key, val, val2, lo2, hi2, n, gkey, gsum, gcnt, cap, (long long *)d_num));
+    qg_pre_launch(ctx);
+    k_gbd_outside_error<<<1, 1, 0, ctx->stream>>>(ctx->ctl);
+    return qg_check_launch(ctx, "k_gbd_outside_error");
+}
+
+// One synchronous run of the dense-window path: *ok when every row fell in
+// the window (the outputs then hold the result).
+qg_status qg_groupby_dense_probe(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
+                                 int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt,
+                                 int64_t cap, int64_t *d_num, bool *ok) {
+    *ok = false;
+    if (!ctx || n <= 0 || n >= (1LL << 32) || !key || !val || !d_num) return QG_OK;
+    if ((((uintptr_t)key) | ((uintptr_t)val) | ((uintptr_t)val2)) & 15) return QG_OK;
+    QG_TRY(qg_gbd_launch(ctx, key, val, val2, lo2, hi2, n, gkey, gsum, gcnt, cap, (long long *)d_num));
+    QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pin_ctl, ctx->ctl, offsetof(qg_control, ghist), cudaMemcpyDeviceToHost,
+                                     ctx->stream),
+                "ctl d2h");
+    QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "sync");
+    if (ctx->pin_ctl->err != 0) return qg_collect_error(ctx);
+    *ok = ctx->pin_ctl->gbd[QG_GBD_OUTSIDE] == 0;
+    return QG_OK;
+}
+
 static qg_status groupby_cols_impl(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
                                    int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum,
                                    int64_t *gcnt, int64_t cap, int order, int64_t *num_groups);

@@ -84,6 +84,12 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
                         int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt,
                         int64_t cap, long long *d_num);
 enum { QG_GBD_OUTSIDE = 6 };
+qg_status qg_groupby_dense_async(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
+                                 int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt,
+                                 int64_t cap, int64_t *d_num);
+qg_status qg_groupby_dense_probe(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2,
+                                 int32_t lo2, int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt,
+                                 int64_t cap, int64_t *d_num, bool *ok);
 
 // Operators the learned variant choice covers (the batch's OP_* order).
 enum { QG_STEER_FILTER = 0, QG_STEER_GROUPBY = 1, QG_STEER_FUSED = 2, QG_STEER_JOIN = 3, QG_STEER_OPS = 4 };

@@ -71,7 +71,7 @@ def test_batch_variants_are_bit_identical(ctx):
 
 
 def test_batch_join_over_capacity_reports_error(ctx):
-    from query_on_opencl_fpga_gb300.api import QGError
+    from query_on_opencl_fpga_gb300._lib import QGError
 
     qs = qb.mixed_queries(1, seed=3, lo=8192, hi=8193, ops=(qb.OP_JOIN,))
     qs[0]["cap"] = 10  # far fewer than the matches
@@ -208,10 +208,38 @@ def test_batch_persistent_table_overflow_reports_error(ctx):
     # More groups than the query's table holds (2 x cap rounded up to a power
     # of two): the persistent kernel records QG_ERR_TABLE_FULL, seen by the
     # batch's eager run; ordinary calls are unaffected.
-    from query_on_opencl_fpga_gb300.api import QGError
+    from query_on_opencl_fpga_gb300._lib import QGError
 
     kk = np.arange(20000, dtype=np.int32)
     with pytest.raises(QGError) as e:
         qb.Batch([_query(qb.OP_GROUPBY, kk, kk, cap=1000)], autotune=False, persistent=True)
     assert e.value.status == 4
     ctx.check(ctx.lib.qg_ctx_check(ctx.handle), "qg_ctx_check")
+
+
+def test_batch_dense_window_group_bys(ctx):
+    # Group-by queries whose keys fit a window run the dense-window path inside
+    # the graph; a query whose keys spread over 2^30 values takes the two-pass
+    # path.  Both equal the plain calls.  A replay after a dense query's keys
+    # were spread as wide reports the rows it could not place instead of a
+    # wrong result.
+    from query_on_opencl_fpga_gb300._lib import QGError
+
+    qs = qb.mixed_queries(8, seed=21, lo=1 << 16, hi=1 << 18, ops=(qb.OP_GROUPBY, qb.OP_FUSED))
+    qs[0]["inp"][0].mul_(1024)  # keys over [0, 2^30): no window holds them
+    plain = qb.run_plain(ctx, qs)
+    b = qb.Batch(qs, autotune=False)
+    try:
+        for q in qs:
+            q["count"].fill_(-1)
+        b.run()
+        b.check()
+        for q, got, exp in zip(qs, qb.batch_results(qs), plain):
+            _same(q["op"], got, exp)
+        qs[1]["inp"][0].mul_(1024)
+        b.run()
+        with pytest.raises(QGError) as ei:
+            b.check()
+        assert ei.value.status == 7  # QG_ERR_UNSUPPORTED
+    finally:
+        b.close()
