@@ -352,6 +352,19 @@ qg_status qg_collect_error(qg_ctx *ctx) {
 }
 
 qg_status qg_read_count(qg_ctx *ctx, const long long *d, long long *h) {
+    const uintptr_t base = (uintptr_t)ctx->ctl, at = (uintptr_t)d;
+    const size_t off = (size_t)(at - base);
+    if (at >= base && off + sizeof(long long) <= offsetof(qg_control, gbd)) {
+        // A count kept in the control block comes back with the error word
+        // in one copy.
+        QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pin_ctl, ctx->ctl, off + sizeof(long long), cudaMemcpyDeviceToHost,
+                                         ctx->stream),
+                    "cudaMemcpyAsync count");
+        QG_TRY_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+        memcpy(h, (const char *)ctx->pin_ctl + off, sizeof(long long));
+        const int32_t e[2] = {ctx->pin_ctl->err, ctx->pin_ctl->err_site};
+        return map_error(ctx, e);
+    }
     int32_t *e = reinterpret_cast<int32_t *>(ctx->pinned + 7);
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, d, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream),
                 "cudaMemcpyAsync count");

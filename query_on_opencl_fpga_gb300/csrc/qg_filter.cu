@@ -364,8 +364,9 @@ __device__ __forceinline__ uint32_t tp_flags(const int4 &k, long long idx, long 
 // 4 * round + j), so that pass B need not read the keys again.
 __global__ void __launch_bounds__(TP_THREADS)
 k_filter_count(const int32_t *__restrict__ key, long long n, int32_t lo, int32_t hi, uint32_t *__restrict__ counts,
-               uint32_t *__restrict__ gsum, uint16_t *__restrict__ mask) {
+               uint32_t *__restrict__ gsum, uint16_t *__restrict__ mask, uint32_t *__restrict__ arrivals) {
     __shared__ uint32_t ws[TP_WARPS];
+    __shared__ uint32_t s_last;
     const int tid = threadIdx.x;
     const long long base = (long long)blockIdx.x * TP_TILE;
     int4 kv[TP_ROUNDS];
@@ -380,11 +381,29 @@ k_filter_count(const int32_t *__restrict__ key, long long n, int32_t lo, int32_t
     c = __reduce_add_sync(QG_FULL_MASK, c);
     if ((tid & 31) == 0) ws[tid >> 5] = c;
     __syncthreads();
+    const uint32_t g = blockIdx.x / TP_GROUP;
+    const uint32_t gsize = min((uint32_t)TP_GROUP, gridDim.x - g * TP_GROUP);
     if (tid == 0) {
         uint32_t t = 0;
         for (int w = 0; w < TP_WARPS; w++) t += ws[w];
         counts[blockIdx.x] = t;
-        if (t) atomicAdd(&gsum[blockIdx.x / TP_GROUP], t);
+        __threadfence();
+        // atomicInc wraps to zero on the group's last arrival, which then
+        // sums the group's counts (all stored and fenced before their arrivals)
+        s_last = atomicInc(&arrivals[g], gsize - 1) == gsize - 1;
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    uint32_t gc = tid < (int)gsize ? __ldcg(counts + (size_t)g * TP_GROUP + tid) : 0u;
+    static_assert(TP_GROUP == TP_THREADS, "one count per thread");
+    gc = __reduce_add_sync(QG_FULL_MASK, gc);
+    if ((tid & 31) == 0) ws[tid >> 5] = gc;
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < TP_WARPS; w++) t += ws[w];
+        gsum[g] = t;
     }
 }
 
@@ -507,9 +526,11 @@ qg_status qg_filter_cols_launch(qg_ctx *ctx, const int32_t *key, const int32_t *
         QG_TRY(qg_scratch(ctx, cg_bytes + (size_t)tp_tiles * TP_THREADS * 2, &scr));
         uint32_t *counts = (uint32_t *)scr, *gsum = counts + tp_tiles;
         uint16_t *mask = (uint16_t *)(scr + cg_bytes);
-        QG_TRY_CUDA(ctx, cudaMemsetAsync(gsum, 0, (size_t)groups * 4, ctx->stream), "memset group sums");
+        static_assert(sizeof(((qg_control *)0)->fgroup) / 4 * (long long)TP_GROUP * TP_TILE >= 0x7fffffffLL,
+                      "one arrival counter per group of the largest accepted input");
         qg_pre_launch(ctx);
-        k_filter_count<<<(unsigned)tp_tiles, TP_THREADS, 0, ctx->stream>>>(key, n, lo, hi, counts, gsum, mask);
+        k_filter_count<<<(unsigned)tp_tiles, TP_THREADS, 0, ctx->stream>>>(key, n, lo, hi, counts, gsum, mask,
+                                                                         ctx->ctl->fgroup);
         QG_TRY(qg_check_launch(ctx, "k_filter_count"));
         qg_pre_launch(ctx);
         k_filter_write<<<(unsigned)tp_tiles, TP_THREADS, 0, ctx->stream>>>(mask, pay, n, counts, gsum, (int2 *)out,

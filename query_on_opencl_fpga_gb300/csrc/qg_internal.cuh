@@ -19,6 +19,10 @@ struct qg_control {
     unsigned long long counter[6];  // scratch counters (output cursors)
     uint32_t gbd[48];               // per-call state of the dense-window group-by (qg_gbdense.cu)
     uint32_t ghist[4 * 256];        // digit counts of emitted group keys (group-by in key order)
+    // Arrivals of the two-pass column filter's tiles per group of 256 tiles
+    // (inputs below 2^31 rows make at most 2048 groups).  The last tile of a
+    // group wraps its counter back to zero, so no launch has to clear them.
+    uint32_t fgroup[2048];
 };
 
 #define QG_MAX_TIMED 4096
