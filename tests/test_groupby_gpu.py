@@ -280,6 +280,24 @@ def test_groupby_dense_wide_and_signed_values(ctx, orc):
     _dense_case(ctx, orc, key[: n // 3], rng.integers(0, 1000, n // 3).astype(np.int32), path="dense")
 
 
+@pytest.mark.parametrize("n,nkeys,vmax", [(1 << 22, 8, 600_000), (1 << 20, 4, 1 << 23), (1 << 22, 1, None)])
+def test_groupby_dense_heavy_slot_bounds(ctx, orc, n, nkeys, vmax):
+    # A few keys take every row, so each CTA's heavy-key slots take thousands
+    # of adds per key, with values up to and past the bound on values the
+    # packed count/sum words take (the largest such value on every row, for
+    # one key), and at 2^20 rows values of 2^21 and more.
+    rng = np.random.default_rng(n + nkeys)
+    key = (rng.integers(0, nkeys, n) * 7919 + 12345).astype(np.int32)
+    if vmax is None:  # the largest fast value for n rows on every row
+        shift = 64 - n.bit_length()
+        val = np.full(n, ((1 << shift) - 1) // n, np.int64)
+        val = np.minimum(val, 2 ** 31 - 1).astype(np.int32)
+    else:
+        val = rng.integers(0, vmax, n).astype(np.int32)
+    _dense_case(ctx, orc, key, val, path="dense")
+    _dense_case(ctx, orc, key, val, val, -(2 ** 31), vmax // 2 if vmax else 2 ** 31 - 1, path="dense")
+
+
 @pytest.mark.parametrize("lo", [0, 2 ** 31 - 1000, 2 ** 32 - 3000])
 def test_groupby_dense_window_positions(ctx, orc, lo):
     # keys from 0 up, across the signed boundary, and at the top of the
