@@ -302,6 +302,8 @@ def run_ours(args, rank, world, local):
     peaks, peak_kind = load_peaks()
     peak = float(peaks["hbm_gbs"])
     ctx = Context(stream)
+    if args.gb_launches:
+        ctx.groupby_set_single_launch(args.gb_launches == 1)
 
     d = datagen.config1_groupby(N_ROWS, GROUPS, seed=rank, device="cuda")
     key, val, val2, lo2, hi2 = d["key"], d["val"], d["val2"], d["lo2"], d["hi2"]
@@ -702,6 +704,8 @@ def run_only(args):
         ctx.check(ctx.lib.qg_filter_set_variant(args.variant), "qg_filter_set_variant")
     if args.variant >= 0 and args.only in ("groupby", "fused"):
         ctx.check(ctx.lib.qg_groupby_set_knobs(args.variant, 13, 0, 0), "qg_groupby_set_knobs")
+    if args.gb_launches:
+        ctx.groupby_set_single_launch(args.gb_launches == 1)
     ms, kern, launches = timed(ctx, fn, args.steps, args.warmup, 1, stream)
     extra = {"groupby_stats": ctx.groupby_stats()} if args.only in ("groupby", "fused") else {}
     if args.only in ("join", "skew"):
@@ -719,6 +723,8 @@ def main():
     ap.add_argument("--rows", type=int, default=0, help="row count for --only (default: the config size)")
     ap.add_argument("--variant", type=int, default=-1, help="column filter kernel variant for --only filter")
     ap.add_argument("--rows2", type=int, default=0, help="build-side rows for --only join")
+    ap.add_argument("--gb-launches", type=int, default=0, choices=[0, 1, 4],
+                    help="group-by: the dense-window steps as one cooperative launch (1) or four (4); 0: the library default")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)

@@ -221,6 +221,11 @@ QG_API qg_status qg_groupby_cols_async(qg_ctx *ctx, const int32_t *key, const in
  * value forces the fallback, for testing). */
 QG_API qg_status qg_groupby_set_knobs(int mode, int hot_slots_log2, int partitions_log2,
                                       uint32_t bucket_cap);
+/* The dense-window path's four steps (sample, candidates, main pass, emit)
+ * as one cooperative launch with grid barriers between them (enable = 1), or
+ * as four launches (0, the default; also what runs while the stream is being
+ * captured into a graph).  Process-wide; results are identical. */
+QG_API qg_status qg_groupby_set_single_launch(int enable);
 /* Diagnostics of the context's last qg_groupby_cols call: out[0] = path
  * (0 two-pass, 1 global table, 2 dense window), out[1] = overflow flags
  * (bit 0 spill bucket, bit 1 pass-2 table), out[2] = fullest spill bucket,

@@ -68,6 +68,7 @@ SIGNATURES: dict[str, tuple] = {
     "qg_groupby_cols_async": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int32,
                                       c_int64, c_void_p, c_void_p, c_void_p, c_int64, c_int, c_void_p]),
     "qg_groupby_set_knobs": (c_int, [c_int, c_int, c_int, c_uint32]),
+    "qg_groupby_set_single_launch": (c_int, [c_int]),
     "qg_groupby_stats": (c_int, [c_void_p, c_void_p]),
     "qg_join_filter_sort": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                     c_int32, c_int32, c_void_p, c_void_p, c_void_p, c_int64,

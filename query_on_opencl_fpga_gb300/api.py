@@ -310,6 +310,10 @@ class Context:
         self.check(self.lib.qg_join_set_knobs(variant, buckets_log2, bucket_s_max, bucket_r_max),
                    "qg_join_set_knobs")
 
+    def groupby_set_single_launch(self, enable: bool):
+        """Dense-window group-by as one cooperative launch or four launches (default); results are identical."""
+        self.check(self.lib.qg_groupby_set_single_launch(1 if enable else 0), "qg_groupby_set_single_launch")
+
     def join_set_dense(self, enable: bool = True):
         """Dense build side (unique R keys over a dense span) on or off; results are identical."""
         self.check(self.lib.qg_join_set_dense(1 if enable else 0), "qg_join_set_dense")

@@ -91,7 +91,8 @@ enum {
     G_UMAX = 5,    // largest window offset of a counted row
     G_OUTSIDE = QG_GBD_OUTSIDE,  // rows outside the window (or 1 when no window)
     G_EXTRA = 7,   // 1: some value went to the extra (int64) table
-    G_WORDS = 8
+    G_BAR = 8,     // k_gbd_single: grid barrier arrivals
+    G_WORDS = 9
 };
 static_assert(G_WORDS <= 48, "gbd state words");
 static_assert(GBD_RUNS_PER_CTA * GBD_RUN * 2 <= GBD_SSLOTS, "sample table load <= 1/2");
@@ -131,12 +132,13 @@ __global__ void __launch_bounds__(GBD_RUN)
 k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_row,
              uint32_t *__restrict__ sketch, uint32_t *__restrict__ lst, uint32_t *__restrict__ lcnt,
              uint32_t *__restrict__ st) {
-    __shared__ uint32_t tkey[GBD_SSLOTS], tcnt[GBD_SSLOTS], s_n;
+    __shared__ uint32_t tkey[GBD_SSLOTS], tcnt[GBD_SSLOTS], s_n, s_mm[2];
     for (int i = threadIdx.x; i < GBD_SSLOTS; i += GBD_RUN) {
         tkey[i] = GBD_EMPTY;
         tcnt[i] = 0;
     }
     if (threadIdx.x == 0) s_n = 0;
+    if (threadIdx.x < 2) s_mm[threadIdx.x] = threadIdx.x == 0 ? 0xffffffffu : 0u;
     uint32_t k[GBD_RUNS_PER_CTA];
     bool have[GBD_RUNS_PER_CTA];
 #pragma unroll
@@ -184,12 +186,18 @@ k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_
     }
     lmin = __reduce_min_sync(QG_FULL_MASK, lmin);
     lmax = __reduce_max_sync(QG_FULL_MASK, lmax);
-    if ((threadIdx.x & 31) == 0 && lmin <= lmax) {
-        atomicMax(&st[G_NSMIN], ~lmin);
-        atomicMax(&st[G_SMAX], lmax);
+    if ((threadIdx.x & 31) == 0 && lmin <= lmax) {  // one global pair per CTA, not per warp
+        atomicMin(&s_mm[0], lmin);
+        atomicMax(&s_mm[1], lmax);
     }
     __syncthreads();
-    if (threadIdx.x == 0) lcnt[blockIdx.x] = s_n;
+    if (threadIdx.x == 0) {
+        lcnt[blockIdx.x] = s_n;
+        if (s_mm[0] <= s_mm[1]) {
+            atomicMax(&st[G_NSMIN], ~s_mm[0]);
+            atomicMax(&st[G_SMAX], s_mm[1]);
+        }
+    }
 }
 
 // 2. Candidates bid for their slots; the window.  CTA b reads sample CTA b's
@@ -227,26 +235,21 @@ k_gbd_cands(const uint32_t *__restrict__ sketch, const uint32_t *__restrict__ ls
     }
 }
 
-// 3. Main pass.
+// 3. Main pass: the body, shared by k_gbd_main and k_gbd_single.  `raw` is
+// the 192 KB of dynamic shared memory; img is read through L2 (the single
+// launch wrote it moments before).
 template <bool PRED>
-__global__ void __launch_bounds__(GBD_THREADS, 1)
-k_gbd_main(const int32_t *__restrict__ key, const int32_t *__restrict__ val, const int32_t *__restrict__ val2,
-           int32_t lo2, int32_t hi2, long long n, const unsigned long long *__restrict__ img,
-           uint32_t *__restrict__ st, unsigned long long *__restrict__ dense, long long *__restrict__ extra,
-           uint32_t shift, uint32_t fast_max) {
-    extern __shared__ __align__(16) unsigned char gbd_main_raw[];
-    uint32_t *hk = reinterpret_cast<uint32_t *>(gbd_main_raw);  // [GBD_S] window offsets, EMPTY if none
-    uint32_t *hc = hk + GBD_S;                                    // [GBD_S] counts
-    uint32_t *hl = hc + GBD_S;                                    // [GBD_S] sums of fast values
-    __shared__ uint32_t s_red[4];
+__device__ __forceinline__ void gbd_main_body(const int32_t *__restrict__ key, const int32_t *__restrict__ val,
+                                              const int32_t *__restrict__ val2, int32_t lo2, int32_t hi2, long long n,
+                                              const unsigned long long *img, uint32_t kbase, uint32_t *st,
+                                              unsigned long long *dense, long long *extra, uint32_t shift,
+                                              uint32_t fast_max, unsigned char *raw, uint32_t *s_red) {
+    uint32_t *hk = reinterpret_cast<uint32_t *>(raw);  // [GBD_S] window offsets, EMPTY if none
+    uint32_t *hc = hk + GBD_S;                           // [GBD_S] counts
+    uint32_t *hl = hc + GBD_S;                           // [GBD_S] sums of fast values
     const int tid = threadIdx.x;
-    if (!st[G_OK]) {  // no window: the caller takes the two-pass path
-        if (blockIdx.x == 0 && tid == 0) atomicAdd(&st[G_OUTSIDE], 1u);
-        return;
-    }
-    const uint32_t kbase = st[G_KBASE];
     for (int i = tid; i < GBD_S; i += GBD_THREADS) {
-        const unsigned long long w = img[i];
+        const unsigned long long w = __ldcg(img + i);
         // a candidate is a sampled key, and the window covers the sample
         hk[i] = w ? (uint32_t)w - kbase : GBD_EMPTY;
         hc[i] = 0;
@@ -340,6 +343,22 @@ k_gbd_main(const int32_t *__restrict__ key, const int32_t *__restrict__ val, con
         if (s_red[2]) atomicAdd(&st[G_OUTSIDE], s_red[2]);
         if (s_red[3]) atomicOr(&st[G_EXTRA], 1u);
     }
+}
+
+template <bool PRED>
+__global__ void __launch_bounds__(GBD_THREADS, 1)
+k_gbd_main(const int32_t *__restrict__ key, const int32_t *__restrict__ val, const int32_t *__restrict__ val2,
+           int32_t lo2, int32_t hi2, long long n, const unsigned long long *__restrict__ img,
+           uint32_t *__restrict__ st, unsigned long long *__restrict__ dense, long long *__restrict__ extra,
+           uint32_t shift, uint32_t fast_max) {
+    extern __shared__ __align__(16) unsigned char gbd_main_raw[];
+    __shared__ uint32_t s_red[4];
+    if (!st[G_OK]) {  // no window: the caller takes the two-pass path
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&st[G_OUTSIDE], 1u);
+        return;
+    }
+    gbd_main_body<PRED>(key, val, val2, lo2, hi2, n, img, st[G_KBASE], st, dense, extra, shift, fast_max,
+                        gbd_main_raw, s_red);
 }
 
 // 4. Emit in key order.  Tile t (CTA t: CTAs start in index order) covers
@@ -441,7 +460,281 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
     qg_lb_finish(lb, tile, last, epoch);
 }
 
+
+// ---------------------------------------------------------------------------
+// The four steps in one cooperative launch (k_gbd_single): one 1024-thread
+// CTA per SM runs the sample, the candidates, the main pass and the emit,
+// with a grid barrier between them, so the short steps use every SM at full
+// occupancy instead of a few latency-bound CTAs each, and no launch gap
+// separates them.
+//   A  sample: CTA b takes runs b, b + C, ... (at most 8, C >= 128); its
+//      distinct keys stay in its shared table (4096 slots, load <= 1/2).
+//   B  candidates: each CTA bids for its own distinct keys (the sketch is
+//      complete after the barrier); every CTA derives the window itself.
+//   C  main pass (gbd_main_body).
+//   D  emit: the touched range splits into C contiguous chunks; each CTA
+//      counts its chunk's groups, and after a barrier places them at the sum
+//      of the earlier chunks' counts, in tiles of 8192 entries held in
+//      registers.  The sketch, slot image and entries are cleared as before.
+// Every barrier wait is bounded (QG_ERR_TIMEOUT); the barrier counter lives
+// in the per-call state words the host clears before the launch.
+// ---------------------------------------------------------------------------
+constexpr int GBD1_SSLOTS = 4096;   // per-CTA sample table: up to 8 runs = 2048 keys
+constexpr int GBD1_MAX_RUNS = 8;    // runs per CTA (2 per thread)
+constexpr int GBD1_PER = 8;         // emit entries per thread and tile
+constexpr int GBD1_TILE = GBD_THREADS * GBD1_PER;
+constexpr int GBD1_NW = GBD_THREADS / 32;
+static_assert(GBD1_SSLOTS * 8 <= GBD_S * 12, "sample table inside the main pass's shared memory");
+static_assert(GBD1_MAX_RUNS * GBD_RUN * 2 <= GBD1_SSLOTS, "sample table load <= 1/2");
+static_assert(GBD_THREADS == 4 * GBD_RUN, "four run lanes per CTA");
+static_assert(GBD1_PER * GBD1_NW == 8 * 32, "emit cells: 8 per lane of warp 0");
+
+__device__ __forceinline__ bool gbd_grid_sync(uint32_t *bar, uint32_t target, uint32_t spin_limit, qg_control *ctl,
+                                              volatile uint32_t *s_ok) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        uint32_t ok = 1u, polls = 0;
+        while (qg_ld_relaxed_u32(bar) < target) {
+            if (polls++ >= spin_limit) {
+                qg_record_error(ctl, QG_ERR_TIMEOUT, QG_SITE_GROUPBY);
+                ok = 0u;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0u;
+}
+
+template <bool PRED>
+__global__ void __launch_bounds__(GBD_THREADS, 1)
+k_gbd_single(const int32_t *__restrict__ key, const int32_t *__restrict__ val, const int32_t *__restrict__ val2,
+             int32_t lo2, int32_t hi2, long long n, int runs, bool every_row, uint32_t *sketch,
+             unsigned long long *img, uint32_t *st, unsigned long long *dense, long long *extra, uint32_t shift,
+             uint32_t fast_max, int32_t *__restrict__ gkey, long long *__restrict__ gsum,
+             long long *__restrict__ gcnt, long long cap, long long *d_num, uint32_t *counts, qg_control *ctl,
+             uint32_t spin_limit) {
+    extern __shared__ __align__(16) unsigned char gbd_main_raw[];
+    __shared__ uint32_t s_red[4], s_wsum[GBD1_NW], s_off[GBD1_PER * GBD1_NW];
+    __shared__ volatile uint32_t s_ok;
+    __shared__ unsigned long long s_base;
+    __shared__ uint32_t s_tot;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t C = gridDim.x, b = blockIdx.x;
+
+    // A. sample
+    uint32_t *tkey = reinterpret_cast<uint32_t *>(gbd_main_raw), *tcnt = tkey + GBD1_SSLOTS;
+    for (int i = tid; i < GBD1_SSLOTS; i += GBD_THREADS) {
+        tkey[i] = GBD_EMPTY;
+        tcnt[i] = 0;
+    }
+    if (tid < 2) s_red[tid] = tid == 0 ? 0xffffffffu : 0u;
+    uint32_t k[2];
+    bool have[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const long long r = (long long)b + (long long)((tid >> 8) + 4 * j) * C;
+        const long long start = every_row ? r * GBD_RUN : (n - GBD_RUN) * r / (runs - 1);
+        const long long i = start + (tid & (GBD_RUN - 1));
+        have[j] = r < runs && i < n;
+        k[j] = have[j] ? (uint32_t)key[i] : 0u;
+    }
+    __syncthreads();
+    uint32_t lmin = 0xffffffffu, lmax = 0;
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        if (!have[j]) continue;
+        lmin = min(lmin, k[j]);
+        lmax = max(lmax, k[j]);
+        if (k[j] == GBD_EMPTY) continue;
+        uint32_t h = qg_hash32(k[j]) & (GBD1_SSLOTS - 1);
+        for (int p = 0; p < GBD1_SSLOTS; p++, h = (h + 1) & (GBD1_SSLOTS - 1)) {
+            const uint32_t old = atomicCAS(&tkey[h], GBD_EMPTY, k[j]);
+            if (old == GBD_EMPTY || old == k[j]) {
+                atomicAdd(&tcnt[h], 1u);
+                break;
+            }
+        }
+    }
+    __syncthreads();
+    for (int sl = tid; sl < GBD1_SSLOTS; sl += GBD_THREADS) {
+        const uint32_t c = tcnt[sl];
+        if (c) {
+            const uint32_t kk = tkey[sl];
+            atomicAdd(sketch + gbd_h1(kk), c);
+            atomicAdd(sketch + (1u << GBD_TLOG2) + gbd_h2(kk), c);
+        }
+    }
+    // the sampled key range: one pair of global atomics per CTA (atomics on
+    // one address from every warp of the grid would queue at its L2 slice)
+    lmin = __reduce_min_sync(QG_FULL_MASK, lmin);
+    lmax = __reduce_max_sync(QG_FULL_MASK, lmax);
+    if (lane == 0 && lmin <= lmax) {
+        atomicMin(&s_red[0], lmin);
+        atomicMax(&s_red[1], lmax);
+    }
+    __syncthreads();
+    if (tid == 0 && s_red[0] <= s_red[1]) {
+        atomicMax(&st[G_NSMIN], ~s_red[0]);
+        atomicMax(&st[G_SMAX], s_red[1]);
+    }
+    if (!gbd_grid_sync(&st[G_BAR], C, spin_limit, ctl, &s_ok)) return;
+
+    // B. candidates and the window
+    const uint32_t smin = ~__ldcg(&st[G_NSMIN]), smax = __ldcg(&st[G_SMAX]);
+    bool ok = false;
+    uint32_t kbase = 0;
+    if (smin <= smax) {
+        const unsigned long long span = (unsigned long long)(smax - smin) + 1ull;
+        if (span <= GBD_W / 2) {
+            const unsigned long long slack = (GBD_W - span) / 2;
+            unsigned long long kb = smin > slack ? smin - slack : 0ull;
+            if (kb + GBD_W > (1ull << 32)) kb = (1ull << 32) - GBD_W;
+            kbase = (uint32_t)kb;
+            ok = true;
+        }
+    }
+    if (b == 0 && tid == 0) {
+        st[G_KBASE] = kbase;
+        st[G_OK] = ok ? 1u : 0u;
+        if (!ok) atomicAdd(&st[G_OUTSIDE], 1u);  // no window: the caller takes the two-pass path
+    }
+    const uint32_t min_count = every_row ? 1u : 2u;
+    for (int sl = tid; sl < GBD1_SSLOTS; sl += GBD_THREADS) {
+        const uint32_t kk = tkey[sl];
+        if (!tcnt[sl]) continue;
+        const uint32_t c = min(__ldcg(sketch + gbd_h1(kk)), __ldcg(sketch + (1u << GBD_TLOG2) + gbd_h2(kk)));
+        if (c >= min_count) atomicMax(img + gbd_slot(kk), ((unsigned long long)c << 32) | kk);
+    }
+    if (!gbd_grid_sync(&st[G_BAR], 2 * C, spin_limit, ctl, &s_ok)) return;
+
+    // C. main pass
+    if (ok) gbd_main_body<PRED>(key, val, val2, lo2, hi2, n, img, kbase, st, dense, extra, shift, fast_max,
+                                gbd_main_raw, s_red);
+    if (!gbd_grid_sync(&st[G_BAR], 3 * C, spin_limit, ctl, &s_ok)) return;
+
+    // D. emit.  Clear this CTA's share of the slot image and the sketch.
+    for (uint32_t i = b * GBD_THREADS + tid; i < (uint32_t)GBD_S; i += C * GBD_THREADS) img[i] = 0ull;
+    {
+        uint4 *sk4 = reinterpret_cast<uint4 *>(sketch);
+        constexpr uint32_t W4 = (2u << GBD_TLOG2) / 4;
+        for (uint32_t i = b * GBD_THREADS + tid; i < W4; i += C * GBD_THREADS) sk4[i] = make_uint4(0, 0, 0, 0);
+    }
+    const uint32_t umin = ~__ldcg(&st[G_NUMIN]), hi = __ldcg(&st[G_UMAX]);
+    const bool any = ok && umin <= hi;
+    const bool xtra = __ldcg(&st[G_EXTRA]) != 0u;
+    const unsigned long long len = any ? (unsigned long long)(hi - umin) + 1ull : 0ull;
+    const unsigned long long ch = ((len + C - 1) / C + 31) & ~31ull;
+    const unsigned long long cb = (unsigned long long)umin + b * ch;
+    const unsigned long long ce = min(cb + ch, (unsigned long long)umin + len);
+    uint32_t cnt = 0;
+    for (unsigned long long t0 = cb; t0 < ce; t0 += GBD1_TILE) {
+        unsigned long long e[GBD1_PER];
+#pragma unroll
+        for (int r = 0; r < GBD1_PER; r++) {
+            const unsigned long long i = t0 + r * GBD_THREADS + tid;
+            e[r] = i < ce ? __ldcg(dense + i) : 0ull;
+        }
+#pragma unroll
+        for (int r = 0; r < GBD1_PER; r++) cnt += e[r] != 0ull;
+    }
+    cnt = __reduce_add_sync(QG_FULL_MASK, cnt);
+    if (lane == 0) s_wsum[warp] = cnt;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t t = __reduce_add_sync(QG_FULL_MASK, s_wsum[lane]);
+        if (lane == 0) __stcg(counts + b, t);
+    }
+    if (!gbd_grid_sync(&st[G_BAR], 4 * C, spin_limit, ctl, &s_ok)) return;
+    if (warp == 0) {
+        unsigned long long before = 0, all = 0;
+        for (uint32_t j = lane; j < C; j += 32) {
+            const uint32_t c = __ldcg(counts + j);
+            all += c;
+            if (j < b) before += c;
+        }
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) {
+            before += __shfl_down_sync(QG_FULL_MASK, before, d);
+            all += __shfl_down_sync(QG_FULL_MASK, all, d);
+        }
+        if (lane == 0) {
+            s_base = before;
+            if (b == 0) *d_num = (long long)all;
+        }
+    }
+    __syncthreads();
+    const unsigned long long mask = (1ull << shift) - 1ull;
+    unsigned long long base = s_base;
+    for (unsigned long long t0 = cb; t0 < ce; t0 += GBD1_TILE) {
+        unsigned long long e[GBD1_PER];
+#pragma unroll
+        for (int r = 0; r < GBD1_PER; r++) {
+            const unsigned long long i = t0 + r * GBD_THREADS + tid;
+            e[r] = i < ce ? __ldcg(dense + i) : 0ull;
+            const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
+            if (lane == 0) s_off[r * GBD1_NW + warp] = __popc(m);
+        }
+        __syncthreads();
+        if (warp == 0) {  // exclusive offsets of the (round, warp) cells in row order
+            uint32_t c[8], sum = 0;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                c[q] = s_off[lane * 8 + q];
+                sum += c[q];
+            }
+            uint32_t incl = sum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t x = __shfl_up_sync(QG_FULL_MASK, incl, d);
+                if (lane >= d) incl += x;
+            }
+            uint32_t run = incl - sum;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                s_off[lane * 8 + q] = run;
+                run += c[q];
+            }
+            if (lane == 31) s_tot = incl;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < GBD1_PER; r++) {
+            const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
+            if (e[r] == 0ull) continue;
+            const unsigned long long i = t0 + r * GBD_THREADS + tid;
+            const long long pos = (long long)(base + s_off[r * GBD1_NW + warp] + __popc(m & qg_lanemask_lt()));
+            long long sm = (long long)(e[r] & mask);
+            if (xtra) {
+                sm += __ldcg(extra + i);
+                extra[i] = 0;
+            }
+            if (pos < cap) {
+                gkey[pos] = (int32_t)(kbase + (uint32_t)i);
+                gsum[pos] = sm;
+                gcnt[pos] = (long long)(e[r] >> shift);
+            }
+            dense[i] = 0ull;
+        }
+        base += s_tot;
+        __syncthreads();
+    }
+}
+
 }  // namespace
+
+static int g_gbd_single = 0;  // 1: the four steps in one cooperative launch where it fits
+
+extern "C" QG_API qg_status qg_groupby_set_single_launch(int enable) {
+    if (enable != 0 && enable != 1) return QG_ERR_INVALID;
+    g_gbd_single = enable;
+    return QG_OK;
+}
 
 qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, const int32_t *val2, int32_t lo2,
                         int32_t hi2, int64_t n, int32_t *gkey, int64_t *gsum, int64_t *gcnt, int64_t cap,
@@ -474,7 +767,7 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
     if (fm > fm2) fm = fm2;
     const uint32_t fast_max = (uint32_t)fm;
 
-    static size_t attr_main[2] = {0, 0};
+    static size_t attr_main[2] = {0, 0};  // (the single launch's attribute is set with its occupancy check)
     const size_t smem_main = (size_t)GBD_S * 12;
     const bool pred = val2 != nullptr;
     auto mainf = pred ? k_gbd_main<true> : k_gbd_main<false>;
@@ -488,6 +781,47 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
     const bool every_row = n <= (long long)GBD_SAMPLE_RUNS * GBD_RUN;
     const int runs = every_row ? (int)qg_ceil_div(n, GBD_RUN) : GBD_SAMPLE_RUNS;
     qg_status s = QG_OK;
+
+    // One cooperative launch when every SM can hold one CTA and the stream is
+    // not being captured (graphs take the four launches below).
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    QG_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs), "capture status");
+    static int single_fits[2] = {-1, -1};
+    if (g_gbd_single && n > 0 && cs == cudaStreamCaptureStatusNone && C >= 128 &&
+        (long long)C * GBD1_MAX_RUNS >= runs) {
+        auto singlef = pred ? k_gbd_single<true> : k_gbd_single<false>;
+        if (single_fits[pred] < 0) {
+            int nb = 0;
+            QG_TRY_CUDA(ctx, cudaFuncSetAttribute(singlef, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_main),
+                        "attr");
+            QG_TRY_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, singlef, GBD_THREADS, smem_main),
+                        "occupancy");
+            single_fits[pred] = nb >= 1;
+        }
+        if (single_fits[pred]) {
+            uint32_t *counts = (uint32_t *)scr;  // [C] groups per emit chunk (the sample lists are unused)
+            bool er = every_row;
+            int32_t l2 = lo2, h2 = hi2;
+            long long nn = n, cp = cap;
+            uint32_t sh = shift, fm32 = fast_max, spin = ctx->spin_limit;
+            const int32_t *k0 = key, *v0 = val, *w0 = val2;
+            int rn = runs;
+            qg_control *ctl = ctx->ctl;
+            long long *gs = (long long *)gsum, *gc = (long long *)gcnt;
+            void *args[] = {&k0, &v0, &w0, &l2, &h2, &nn, &rn, &er, &sketch, &img, &st, &dense, &extra, &sh,
+                            &fm32, &gkey, &gs, &gc, &cp, &d_num, &counts, &ctl, &spin};
+            qg_pre_launch(ctx);
+            const cudaError_t e = cudaLaunchCooperativeKernel((const void *)singlef, dim3(C), dim3(GBD_THREADS), args,
+                                                              smem_main, ctx->stream);
+            if (e != cudaSuccess) {
+                ctx->table_dirty = true;
+                return qg_cuda_fail(ctx, e, "k_gbd_single");
+            }
+            s = qg_check_launch(ctx, pred ? "k_gbd_single_fused" : "k_gbd_single");
+            if (s != QG_OK) ctx->table_dirty = true;
+            return s;
+        }
+    }
     qg_pre_launch(ctx);  // with runs == 0 (n == 0) every CTA lists nothing
     k_gbd_sample<<<GBD_SAMPLE_CTAS, GBD_RUN, 0, ctx->stream>>>(key, n, runs, every_row, sketch, lst, lcnt, st);
     s = qg_check_launch(ctx, "k_gbd_sample");

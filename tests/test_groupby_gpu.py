@@ -280,6 +280,27 @@ def test_groupby_dense_wide_and_signed_values(ctx, orc):
     _dense_case(ctx, orc, key[: n // 3], rng.integers(0, 1000, n // 3).astype(np.int32), path="dense")
 
 
+@pytest.mark.parametrize("single", [1, 0])
+@pytest.mark.parametrize("n", [5, 4097, (1 << 18) + 3, (1 << 22) + 1])
+def test_groupby_dense_single_and_four_launches(ctx, orc, n, single):
+    # The dense-window steps as one cooperative launch (grid barriers) and as
+    # four launches give the same exact groups, plain and fused, on sizes
+    # below and above the every-row sample; repeated calls on one context
+    # start from a clean table either way.
+    ctx.groupby_set_single_launch(bool(single))
+    try:
+        rng = np.random.default_rng(n + single)
+        key = (rng.zipf(1.2, n) % 200000).astype(np.int32) - 300000  # negative: high unsigned keys
+        val = np.where(rng.random(n) < 0.01, rng.integers(-(2 ** 31), 2 ** 31 - 1, n),
+                       rng.integers(0, 1000, n)).astype(np.int32)
+        val2 = rng.integers(0, 1000, n).astype(np.int32)
+        for _ in range(2):
+            _dense_case(ctx, orc, key, val, path="dense")
+            _dense_case(ctx, orc, key, val, val2, -(2 ** 31), 499, path="dense")
+    finally:
+        ctx.groupby_set_single_launch(False)
+
+
 @pytest.mark.parametrize("n,nkeys,vmax", [(1 << 22, 8, 600_000), (1 << 20, 4, 1 << 23), (1 << 22, 1, None)])
 def test_groupby_dense_heavy_slot_bounds(ctx, orc, n, nkeys, vmax):
     # A few keys take every row, so each CTA's heavy-key slots take thousands
