@@ -69,11 +69,12 @@ constexpr int GBD_TLOG2 = 19;                     // counters per row of the sam
 constexpr uint32_t GBD_TMASK = (1u << GBD_TLOG2) - 1;
 constexpr int GBD_SAMPLE_RUNS = 1024;
 constexpr int GBD_RUN = 256;                      // consecutive rows per sample run
-constexpr int GBD_SAMPLE_CTAS = 256;              // runs b, b + 256, ... : at most 4 per CTA
+constexpr int GBD_SAMPLE_CTAS = 128;              // runs b, b + 128, ... : at most 8 per CTA
+constexpr int GBD_SAMPLE_THREADS = 1024;          // four lanes of 256 threads, two runs each
 constexpr int GBD_RUNS_PER_CTA = GBD_SAMPLE_RUNS / GBD_SAMPLE_CTAS;
-constexpr int GBD_SSLOTS = 2048;                  // per-CTA sample table (<= 1024 keys)
+constexpr int GBD_SSLOTS = 4096;                  // per-CTA sample table (<= 2048 keys)
 constexpr int GBD_LIST = GBD_RUNS_PER_CTA * GBD_RUN;  // distinct keys a sample CTA lists (at most)
-constexpr int GBD_CANDS_THREADS = 256;
+constexpr int GBD_CANDS_THREADS = 512;
 constexpr int GBD_THREADS = 1024;
 constexpr int GBD_EMIT_THREADS = 256;
 constexpr int GBD_EMIT_PER = 16;                  // entries per emit thread
@@ -96,7 +97,8 @@ enum {
 };
 static_assert(G_WORDS <= 48, "gbd state words");
 static_assert(GBD_RUNS_PER_CTA * GBD_RUN * 2 <= GBD_SSLOTS, "sample table load <= 1/2");
-static_assert(GBD_SSLOTS % GBD_RUN == 0 && GBD_RUN % 32 == 0, "the sample's flush walks the table in whole warps");
+static_assert(GBD_SSLOTS % GBD_SAMPLE_THREADS == 0 && GBD_RUN % 32 == 0, "the sample's flush walks the table in whole warps");
+static_assert(GBD_RUNS_PER_CTA * GBD_RUN == 2 * GBD_SAMPLE_THREADS, "two runs per sample thread");
 static_assert(GBD_LIST % GBD_CANDS_THREADS == 0, "cands: whole list per CTA");
 static_assert(2 * (1 << GBD_TLOG2) % (GBD_EMIT_TILES * GBD_EMIT_THREADS * 4) == 0, "emit clears the sketch");
 static_assert(GBD_EMIT_PER * (GBD_EMIT_THREADS / 32) % 32 == 0, "emit cells per lane");
@@ -118,8 +120,9 @@ __device__ __forceinline__ uint32_t gbd_h1(uint32_t k) { return qg_hash32(k) & G
 __device__ __forceinline__ uint32_t gbd_h2(uint32_t k) { return qg_hash32(k * 0x85EBCA77u + 0x27D4EB2Fu) & GBD_TMASK; }
 
 // 1. Sample.  Run r covers rows [start_r, start_r + 256); CTA b takes runs
-// b, b + 256, b + 512, b + 768.  Each thread loads its (up to) four keys
-// first, and the CTA counts them in a shared-memory table of 32-bit keys and
+// b, b + 128, ..., b + 896, one per 256-thread lane and round.  Each thread
+// loads its (up to) two keys first, and the CTA counts them in a shared-memory
+// table of 32-bit keys and
 // counts (64-bit shared atomics are several times slower).  Each distinct
 // key then adds its count to both rows of an L2 count sketch with
 // fire-and-forget reductions (no compare-and-swap round trips) and is listed
@@ -128,31 +131,31 @@ __device__ __forceinline__ uint32_t gbd_h2(uint32_t k) { return qg_hash32(k * 0x
 // so a counter shared by two keys costs speed at most.  Key 0xffffffff is the
 // shared table's empty mark and is never a candidate (its rows take the dense
 // table like any other key's).
-__global__ void __launch_bounds__(GBD_RUN)
+__global__ void __launch_bounds__(GBD_SAMPLE_THREADS)
 k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_row,
              uint32_t *__restrict__ sketch, uint32_t *__restrict__ lst, uint32_t *__restrict__ lcnt,
              uint32_t *__restrict__ st) {
     __shared__ uint32_t tkey[GBD_SSLOTS], tcnt[GBD_SSLOTS], s_n, s_mm[2];
-    for (int i = threadIdx.x; i < GBD_SSLOTS; i += GBD_RUN) {
+    for (int i = threadIdx.x; i < GBD_SSLOTS; i += GBD_SAMPLE_THREADS) {
         tkey[i] = GBD_EMPTY;
         tcnt[i] = 0;
     }
     if (threadIdx.x == 0) s_n = 0;
     if (threadIdx.x < 2) s_mm[threadIdx.x] = threadIdx.x == 0 ? 0xffffffffu : 0u;
-    uint32_t k[GBD_RUNS_PER_CTA];
-    bool have[GBD_RUNS_PER_CTA];
+    uint32_t k[2];
+    bool have[2];
 #pragma unroll
-    for (int j = 0; j < GBD_RUNS_PER_CTA; j++) {
-        const int r = blockIdx.x + j * GBD_SAMPLE_CTAS;
+    for (int j = 0; j < 2; j++) {
+        const int r = blockIdx.x + ((threadIdx.x >> 8) + 4 * j) * GBD_SAMPLE_CTAS;
         const long long start = every_row ? (long long)r * GBD_RUN : (n - GBD_RUN) * (long long)r / (runs - 1);
-        const long long i = start + threadIdx.x;
+        const long long i = start + (threadIdx.x & (GBD_RUN - 1));
         have[j] = r < runs && i < n;
         k[j] = have[j] ? (uint32_t)key[i] : 0u;
     }
     __syncthreads();
     uint32_t lmin = 0xffffffffu, lmax = 0;
 #pragma unroll
-    for (int j = 0; j < GBD_RUNS_PER_CTA; j++) {
+    for (int j = 0; j < 2; j++) {
         if (!have[j]) continue;
         lmin = min(lmin, k[j]);
         lmax = max(lmax, k[j]);
@@ -170,7 +173,7 @@ k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_
     __syncthreads();
     uint32_t *mine = lst + (size_t)blockIdx.x * GBD_LIST;
     const uint32_t lane = threadIdx.x & 31;
-    for (int sl = threadIdx.x; sl < GBD_SSLOTS; sl += GBD_RUN) {  // GBD_SSLOTS % GBD_RUN == 0: whole warps
+    for (int sl = threadIdx.x; sl < GBD_SSLOTS; sl += GBD_SAMPLE_THREADS) {  // whole warps every round
         const uint32_t c = tcnt[sl];
         const uint32_t kk = tkey[sl];
         if (c) {
@@ -823,7 +826,8 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
         }
     }
     qg_pre_launch(ctx);  // with runs == 0 (n == 0) every CTA lists nothing
-    k_gbd_sample<<<GBD_SAMPLE_CTAS, GBD_RUN, 0, ctx->stream>>>(key, n, runs, every_row, sketch, lst, lcnt, st);
+    k_gbd_sample<<<GBD_SAMPLE_CTAS, GBD_SAMPLE_THREADS, 0, ctx->stream>>>(key, n, runs, every_row, sketch, lst, lcnt,
+                                                                          st);
     s = qg_check_launch(ctx, "k_gbd_sample");
     if (s == QG_OK) {
         qg_pre_launch(ctx);
