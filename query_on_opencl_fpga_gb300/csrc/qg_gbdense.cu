@@ -32,13 +32,12 @@
 //                     other key adds one packed word to dense[key - kbase] in
 //                     L2 (red.global.add.u64: count << shift | value).  At the
 //                     end the shared table is added to the dense table.
-//  4. k_gbd_emit   -- the touched index range of the dense table is read in
-//                     order, every non-empty entry becomes a group, and the
-//                     entries (and the slot image and sketch) are cleared.  Output
-//                     positions come from a decoupled look-back over 4096-entry
-//                     tiles (all warps of a tile read 256 predecessors per
-//                     round); within a tile the writes are contiguous across
-//                     each warp.
+//  4. k_gbd_emit   -- one CTA per SM takes a contiguous chunk of the touched
+//                     index range of the dense table, counts its non-empty
+//                     entries, finds its output place by a decoupled look-back
+//                     over the chunks, and writes every non-empty entry as a
+//                     group in key order, clearing the entries (and its share
+//                     of the slot image and sketch).
 //
 // The shared-memory pipeline (L1TEX) bounds the main pass: a row costs about
 // one wavefront (its lookup, its shared or global update), which is why the
@@ -76,10 +75,6 @@ constexpr int GBD_SSLOTS = 4096;                  // per-CTA sample table (<= 20
 constexpr int GBD_LIST = GBD_RUNS_PER_CTA * GBD_RUN;  // distinct keys a sample CTA lists (at most)
 constexpr int GBD_CANDS_THREADS = 512;
 constexpr int GBD_THREADS = 1024;
-constexpr int GBD_EMIT_THREADS = 256;
-constexpr int GBD_EMIT_PER = 16;                  // entries per emit thread
-constexpr int GBD_EMIT_TILE = GBD_EMIT_THREADS * GBD_EMIT_PER;
-constexpr uint32_t GBD_EMIT_TILES = GBD_W / GBD_EMIT_TILE;
 constexpr uint32_t GBD_EMPTY = 0xffffffffu;
 
 // ctl->gbd word indices
@@ -100,9 +95,6 @@ static_assert(GBD_RUNS_PER_CTA * GBD_RUN * 2 <= GBD_SSLOTS, "sample table load <
 static_assert(GBD_SSLOTS % GBD_SAMPLE_THREADS == 0 && GBD_RUN % 32 == 0, "the sample's flush walks the table in whole warps");
 static_assert(GBD_RUNS_PER_CTA * GBD_RUN == 2 * GBD_SAMPLE_THREADS, "two runs per sample thread");
 static_assert(GBD_LIST % GBD_CANDS_THREADS == 0, "cands: whole list per CTA");
-static_assert(2 * (1 << GBD_TLOG2) % (GBD_EMIT_TILES * GBD_EMIT_THREADS * 4) == 0, "emit clears the sketch");
-static_assert(GBD_EMIT_PER * (GBD_EMIT_THREADS / 32) % 32 == 0, "emit cells per lane");
-static_assert(GBD_S % (16 * GBD_EMIT_THREADS) == 0, "emit clears the slot image in 16 tiles");
 
 // Heavy-key slot of a (raw) key: Fibonacci hashing, top GBD_SLOG2 bits.
 __device__ __forceinline__ uint32_t gbd_slot(uint32_t k) { return (k * 0x9E3779B1u) >> (32 - GBD_SLOG2); }
@@ -364,103 +356,150 @@ k_gbd_main(const int32_t *__restrict__ key, const int32_t *__restrict__ val, con
                         gbd_main_raw, s_red);
 }
 
-// 4. Emit in key order.  Tile t (CTA t: CTAs start in index order) covers
-// entries [lo + t*4096, lo + (t+1)*4096) of the
-// touched range [lo, hi]; in round r thread i reads entry r*256 + i of its
-// tile, so the loads, the cleared entries and (after a per-round rank) the
-// groups written are contiguous across a warp.  Tiles past the touched range
-// leave at once; the last touched tile publishes the group count.  Tiles 0-15
-// also clear the slot image, and every tile a share of the sample's sketch.
-__global__ void __launch_bounds__(GBD_EMIT_THREADS)
-k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra,
-           unsigned long long *__restrict__ img, uint4 *__restrict__ sketch, const uint32_t *__restrict__ st,
-           uint32_t shift,
-           int32_t *__restrict__ gkey, long long *__restrict__ gsum, long long *__restrict__ gcnt, long long cap,
-           long long *__restrict__ d_num, qg_lookback lb) {
-    constexpr int NW = GBD_EMIT_THREADS / 32;
-    __shared__ uint32_t s_epoch, s_total, s_off[GBD_EMIT_PER * NW], s_tmp[2 * NW];
+// 4. Emit in key order.  One 1024-thread CTA per SM; the touched index
+// range [umin, umax] is split into one contiguous chunk per CTA (chunk ids in
+// CTA start order).  A CTA counts its chunk's non-empty entries, publishes the
+// count to a decoupled look-back over the chunks (one wide round reads 256
+// predecessors, so no chain of waits forms), and then writes its groups from
+// that place on, in tiles of 8192 entries (8 per thread; the (round, warp)
+// cells ranked in row order), clearing the entries as it goes.  Every CTA also
+// clears its share of the slot image and the sample's sketch.
+constexpr int GBD_EPER = 8;  // emit entries per thread and tile
+constexpr int GBD_ETILE = GBD_THREADS * GBD_EPER;
+constexpr int GBD_ENW = GBD_THREADS / 32;
+static_assert(GBD_EPER * GBD_ENW == 8 * 32, "emit cells: 8 per lane of warp 0");
+
+struct GbdChunk {
+    unsigned long long cb, ce;  // entries [cb, ce) of the dense table
+};
+
+// Chunk c of C over the touched range (empty when nothing was counted).
+__device__ __forceinline__ GbdChunk gbd_chunk(uint32_t c, uint32_t C, bool any, uint32_t umin, uint32_t hi) {
+    const unsigned long long len = any ? (unsigned long long)(hi - umin) + 1ull : 0ull;
+    const unsigned long long ch = ((len + C - 1) / C + 31) & ~31ull;
+    const unsigned long long cb = (unsigned long long)umin + c * ch;
+    return {cb, min(cb + ch, (unsigned long long)umin + len)};
+}
+
+// Clear this CTA's share (CTA c of C) of the slot image and the sketch.
+__device__ __forceinline__ void gbd_clear_sample(unsigned long long *img, uint32_t *sketch, uint32_t c, uint32_t C) {
+    for (uint32_t i = c * GBD_THREADS + threadIdx.x; i < (uint32_t)GBD_S; i += C * GBD_THREADS) img[i] = 0ull;
+    uint4 *sk4 = reinterpret_cast<uint4 *>(sketch);
+    constexpr uint32_t W4 = (2u << GBD_TLOG2) / 4;
+    for (uint32_t i = c * GBD_THREADS + threadIdx.x; i < W4; i += C * GBD_THREADS) sk4[i] = make_uint4(0, 0, 0, 0);
+}
+
+// Non-empty entries of a chunk, summed over the CTA (every thread gets it).
+__device__ __forceinline__ uint32_t gbd_chunk_count(const unsigned long long *dense, GbdChunk k, uint32_t *s_wsum) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const uint32_t tile = blockIdx.x;  // CTAs start in index order: a tile's predecessors are running or done
-    if (tile < 16) {
-        constexpr int PER_TILE = GBD_S / 16;
-        for (int i = tid; i < PER_TILE; i += GBD_EMIT_THREADS) img[tile * PER_TILE + i] = 0ull;
+    uint32_t cnt = 0;
+    for (unsigned long long t0 = k.cb; t0 < k.ce; t0 += GBD_ETILE) {
+        unsigned long long e[GBD_EPER];
+#pragma unroll
+        for (int r = 0; r < GBD_EPER; r++) {
+            const unsigned long long i = t0 + r * GBD_THREADS + tid;
+            e[r] = i < k.ce ? __ldcg(dense + i) : 0ull;
+        }
+#pragma unroll
+        for (int r = 0; r < GBD_EPER; r++) cnt += e[r] != 0ull;
     }
-    {  // every tile clears its share of the sample's count sketch
-        constexpr int PER_TILE = 2 * (1 << GBD_TLOG2) / 4 / GBD_EMIT_TILES;  // uint4 words
-        for (int i = tid; i < PER_TILE; i += GBD_EMIT_THREADS) sketch[(size_t)tile * PER_TILE + i] = make_uint4(0, 0, 0, 0);
+    cnt = __reduce_add_sync(QG_FULL_MASK, cnt);
+    if (lane == 0) s_wsum[warp] = cnt;
+    __syncthreads();
+    const uint32_t t = __reduce_add_sync(QG_FULL_MASK, s_wsum[lane]);
+    __syncthreads();
+    return t;
+}
+
+// Writes a chunk's groups from output place `base` on and clears its entries.
+__device__ __forceinline__ void gbd_chunk_write(unsigned long long *dense, long long *extra, GbdChunk k,
+                                                unsigned long long base, uint32_t kbase, bool xtra, uint32_t shift,
+                                                int32_t *__restrict__ gkey, long long *__restrict__ gsum,
+                                                long long *__restrict__ gcnt, long long cap, uint32_t *s_off,
+                                                uint32_t *s_tot) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned long long mask = (1ull << shift) - 1ull;
+    for (unsigned long long t0 = k.cb; t0 < k.ce; t0 += GBD_ETILE) {
+        unsigned long long e[GBD_EPER];
+#pragma unroll
+        for (int r = 0; r < GBD_EPER; r++) {
+            const unsigned long long i = t0 + r * GBD_THREADS + tid;
+            e[r] = i < k.ce ? __ldcg(dense + i) : 0ull;
+            const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
+            if (lane == 0) s_off[r * GBD_ENW + warp] = __popc(m);
+        }
+        __syncthreads();
+        if (warp == 0) {  // exclusive offsets of the (round, warp) cells in row order
+            uint32_t c[8], sum = 0;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                c[q] = s_off[lane * 8 + q];
+                sum += c[q];
+            }
+            uint32_t incl = sum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t x = __shfl_up_sync(QG_FULL_MASK, incl, d);
+                if (lane >= d) incl += x;
+            }
+            uint32_t run = incl - sum;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                s_off[lane * 8 + q] = run;
+                run += c[q];
+            }
+            if (lane == 31) *s_tot = incl;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < GBD_EPER; r++) {
+            const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
+            if (e[r] == 0ull) continue;
+            const unsigned long long i = t0 + r * GBD_THREADS + tid;
+            const long long pos = (long long)(base + s_off[r * GBD_ENW + warp] + __popc(m & qg_lanemask_lt()));
+            long long sm = (long long)(e[r] & mask);
+            if (xtra) {
+                sm += __ldcg(extra + i);
+                extra[i] = 0;
+            }
+            if (pos < cap) {
+                gkey[pos] = (int32_t)(kbase + (uint32_t)i);
+                gsum[pos] = sm;
+                gcnt[pos] = (long long)(e[r] >> shift);
+            }
+            dense[i] = 0ull;
+        }
+        base += *s_tot;
+        __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(GBD_THREADS)
+k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra,
+           unsigned long long *__restrict__ img, uint32_t *__restrict__ sketch, const uint32_t *__restrict__ st,
+           uint32_t shift, int32_t *__restrict__ gkey, long long *__restrict__ gsum, long long *__restrict__ gcnt,
+           long long cap, long long *__restrict__ d_num, qg_lookback lb) {
+    __shared__ uint32_t s_tile, s_epoch, s_tot, s_wsum[GBD_ENW], s_off[GBD_EPER * GBD_ENW], s_tmp[2 * 8];
+    gbd_clear_sample(img, sketch, blockIdx.x, gridDim.x);
+    qg_lb_begin_dyn(lb, &s_tile, &s_epoch);  // chunk ids in CTA start order: predecessors are running
+    const uint32_t chunk = s_tile, epoch = s_epoch, C = gridDim.x;
     const uint32_t umin = ~st[G_NUMIN], hi = st[G_UMAX];
     const bool any = st[G_OK] && umin <= hi;
-    const uint32_t lo = umin & ~15u;
-    const uint32_t last = any ? (hi - lo) / GBD_EMIT_TILE : 0u;
-    if (tile > last) return;  // reads no epoch: the last touched tile may advance it at any time
-    if (tid == 0) s_epoch = *(volatile uint32_t *)&lb.ctl->epoch;
-    __syncthreads();
-    const uint32_t epoch = s_epoch;
-    const uint32_t kbase = st[G_KBASE];
-    const bool xtra = st[G_EXTRA] != 0;
-    const unsigned long long mask = (1ull << shift) - 1ull;
-    const unsigned long long first = (unsigned long long)lo + (unsigned long long)tile * GBD_EMIT_TILE + tid;
-    unsigned long long e[GBD_EMIT_PER];
-#pragma unroll
-    for (int r = 0; r < GBD_EMIT_PER; r++) {
-        const unsigned long long i = first + r * GBD_EMIT_THREADS;
-        e[r] = (any && i <= hi) ? dense[i] : 0ull;
-        const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
-        if (lane == 0) s_off[r * NW + warp] = __popc(m);
+    const GbdChunk k = gbd_chunk(chunk, C, any, umin, hi);
+    const uint32_t total = gbd_chunk_count(dense, k, s_wsum);
+    if (threadIdx.x < 8 * 32) {  // the wide look-back: 256 predecessors per round
+        const uint32_t excl = qg_lb_wide_exclusive<8>(lb, chunk, epoch, total, s_tmp);
+        if (threadIdx.x == 0) {
+            s_wsum[0] = excl;
+            if (chunk == C - 1) *d_num = (long long)excl + total;
+        }
     }
     __syncthreads();
-    // exclusive offsets of the (round, warp) cells in round-major order
-    if (warp == 0) {
-        constexpr int CPL = GBD_EMIT_PER * NW / 32;  // cells per lane
-        uint32_t c[CPL], sum = 0;
-#pragma unroll
-        for (int k = 0; k < CPL; k++) {
-            c[k] = s_off[lane * CPL + k];
-            sum += c[k];
-        }
-        uint32_t incl = sum;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const uint32_t x = __shfl_up_sync(QG_FULL_MASK, incl, d);
-            if (lane >= d) incl += x;
-        }
-        const uint32_t total = __shfl_sync(QG_FULL_MASK, incl, 31);
-        uint32_t run = incl - sum;
-#pragma unroll
-        for (int k = 0; k < CPL; k++) {
-            s_off[lane * CPL + k] = run;
-            run += c[k];
-        }
-        if (lane == 0) s_total = total;
-    }
-    __syncthreads();
-    // the tile's place: all warps look back, 256 predecessors per round
-    const uint32_t total = s_total;
-    const uint32_t excl = qg_lb_wide_exclusive<NW>(lb, tile, epoch, total, s_tmp);
-    if (tid == 0 && tile == last) *d_num = (long long)excl + total;
-    const long long tile_off = excl;
-#pragma unroll
-    for (int r = 0; r < GBD_EMIT_PER; r++) {
-        const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
-        if (e[r] == 0ull) continue;
-        const unsigned long long i = first + r * GBD_EMIT_THREADS;
-        const long long pos = tile_off + s_off[r * NW + warp] + __popc(m & qg_lanemask_lt());
-        long long sm = (long long)(e[r] & mask);
-        if (xtra) {
-            sm += extra[i];
-            extra[i] = 0;
-        }
-        if (pos < cap) {
-            gkey[pos] = (int32_t)(kbase + (uint32_t)i);
-            gsum[pos] = sm;
-            gcnt[pos] = (long long)(e[r] >> shift);
-        }
-        dense[i] = 0ull;
-    }
-    // The last touched tile ends after every earlier tile published (its
-    // look-back waited for them), so each of them has read the epoch already.
-    qg_lb_finish(lb, tile, last, epoch);
+    gbd_chunk_write(dense, extra, k, s_wsum[0], st[G_KBASE], st[G_EXTRA] != 0u, shift, gkey, gsum, gcnt, cap, s_off,
+                    &s_tot);
+    // The last chunk ends after every earlier chunk published (its look-back
+    // waited for them), and every CTA took its chunk before that.
+    qg_lb_finish_dyn(lb, chunk, C - 1, epoch);
 }
 
 
@@ -484,13 +523,9 @@ k_gbd_emit(unsigned long long *__restrict__ dense, long long *__restrict__ extra
 // ---------------------------------------------------------------------------
 constexpr int GBD1_SSLOTS = 4096;   // per-CTA sample table: up to 8 runs = 2048 keys
 constexpr int GBD1_MAX_RUNS = 8;    // runs per CTA (2 per thread)
-constexpr int GBD1_PER = 8;         // emit entries per thread and tile
-constexpr int GBD1_TILE = GBD_THREADS * GBD1_PER;
-constexpr int GBD1_NW = GBD_THREADS / 32;
 static_assert(GBD1_SSLOTS * 8 <= GBD_S * 12, "sample table inside the main pass's shared memory");
 static_assert(GBD1_MAX_RUNS * GBD_RUN * 2 <= GBD1_SSLOTS, "sample table load <= 1/2");
 static_assert(GBD_THREADS == 4 * GBD_RUN, "four run lanes per CTA");
-static_assert(GBD1_PER * GBD1_NW == 8 * 32, "emit cells: 8 per lane of warp 0");
 
 __device__ __forceinline__ bool gbd_grid_sync(uint32_t *bar, uint32_t target, uint32_t spin_limit, qg_control *ctl,
                                               volatile uint32_t *s_ok) {
@@ -523,7 +558,7 @@ k_gbd_single(const int32_t *__restrict__ key, const int32_t *__restrict__ val, c
              long long *__restrict__ gcnt, long long cap, long long *d_num, uint32_t *counts, qg_control *ctl,
              uint32_t spin_limit) {
     extern __shared__ __align__(16) unsigned char gbd_main_raw[];
-    __shared__ uint32_t s_red[4], s_wsum[GBD1_NW], s_off[GBD1_PER * GBD1_NW];
+    __shared__ uint32_t s_red[4], s_wsum[GBD_ENW], s_off[GBD_EPER * GBD_ENW];
     __shared__ volatile uint32_t s_ok;
     __shared__ unsigned long long s_base;
     __shared__ uint32_t s_tot;
@@ -621,38 +656,14 @@ k_gbd_single(const int32_t *__restrict__ key, const int32_t *__restrict__ val, c
                                 gbd_main_raw, s_red);
     if (!gbd_grid_sync(&st[G_BAR], 3 * C, spin_limit, ctl, &s_ok)) return;
 
-    // D. emit.  Clear this CTA's share of the slot image and the sketch.
-    for (uint32_t i = b * GBD_THREADS + tid; i < (uint32_t)GBD_S; i += C * GBD_THREADS) img[i] = 0ull;
-    {
-        uint4 *sk4 = reinterpret_cast<uint4 *>(sketch);
-        constexpr uint32_t W4 = (2u << GBD_TLOG2) / 4;
-        for (uint32_t i = b * GBD_THREADS + tid; i < W4; i += C * GBD_THREADS) sk4[i] = make_uint4(0, 0, 0, 0);
-    }
+    // D. emit: count this CTA's chunk, then (after a barrier) place its groups
+    // after the earlier chunks' counts.
+    gbd_clear_sample(img, sketch, b, C);
     const uint32_t umin = ~__ldcg(&st[G_NUMIN]), hi = __ldcg(&st[G_UMAX]);
-    const bool any = ok && umin <= hi;
     const bool xtra = __ldcg(&st[G_EXTRA]) != 0u;
-    const unsigned long long len = any ? (unsigned long long)(hi - umin) + 1ull : 0ull;
-    const unsigned long long ch = ((len + C - 1) / C + 31) & ~31ull;
-    const unsigned long long cb = (unsigned long long)umin + b * ch;
-    const unsigned long long ce = min(cb + ch, (unsigned long long)umin + len);
-    uint32_t cnt = 0;
-    for (unsigned long long t0 = cb; t0 < ce; t0 += GBD1_TILE) {
-        unsigned long long e[GBD1_PER];
-#pragma unroll
-        for (int r = 0; r < GBD1_PER; r++) {
-            const unsigned long long i = t0 + r * GBD_THREADS + tid;
-            e[r] = i < ce ? __ldcg(dense + i) : 0ull;
-        }
-#pragma unroll
-        for (int r = 0; r < GBD1_PER; r++) cnt += e[r] != 0ull;
-    }
-    cnt = __reduce_add_sync(QG_FULL_MASK, cnt);
-    if (lane == 0) s_wsum[warp] = cnt;
-    __syncthreads();
-    if (warp == 0) {
-        const uint32_t t = __reduce_add_sync(QG_FULL_MASK, s_wsum[lane]);
-        if (lane == 0) __stcg(counts + b, t);
-    }
+    const GbdChunk ck = gbd_chunk(b, C, ok && umin <= hi, umin, hi);
+    const uint32_t cnt = gbd_chunk_count(dense, ck, s_wsum);
+    if (tid == 0) __stcg(counts + b, cnt);
     if (!gbd_grid_sync(&st[G_BAR], 4 * C, spin_limit, ctl, &s_ok)) return;
     if (warp == 0) {
         unsigned long long before = 0, all = 0;
@@ -672,61 +683,7 @@ k_gbd_single(const int32_t *__restrict__ key, const int32_t *__restrict__ val, c
         }
     }
     __syncthreads();
-    const unsigned long long mask = (1ull << shift) - 1ull;
-    unsigned long long base = s_base;
-    for (unsigned long long t0 = cb; t0 < ce; t0 += GBD1_TILE) {
-        unsigned long long e[GBD1_PER];
-#pragma unroll
-        for (int r = 0; r < GBD1_PER; r++) {
-            const unsigned long long i = t0 + r * GBD_THREADS + tid;
-            e[r] = i < ce ? __ldcg(dense + i) : 0ull;
-            const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
-            if (lane == 0) s_off[r * GBD1_NW + warp] = __popc(m);
-        }
-        __syncthreads();
-        if (warp == 0) {  // exclusive offsets of the (round, warp) cells in row order
-            uint32_t c[8], sum = 0;
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                c[q] = s_off[lane * 8 + q];
-                sum += c[q];
-            }
-            uint32_t incl = sum;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                const uint32_t x = __shfl_up_sync(QG_FULL_MASK, incl, d);
-                if (lane >= d) incl += x;
-            }
-            uint32_t run = incl - sum;
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-                s_off[lane * 8 + q] = run;
-                run += c[q];
-            }
-            if (lane == 31) s_tot = incl;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int r = 0; r < GBD1_PER; r++) {
-            const uint32_t m = __ballot_sync(QG_FULL_MASK, e[r] != 0ull);
-            if (e[r] == 0ull) continue;
-            const unsigned long long i = t0 + r * GBD_THREADS + tid;
-            const long long pos = (long long)(base + s_off[r * GBD1_NW + warp] + __popc(m & qg_lanemask_lt()));
-            long long sm = (long long)(e[r] & mask);
-            if (xtra) {
-                sm += __ldcg(extra + i);
-                extra[i] = 0;
-            }
-            if (pos < cap) {
-                gkey[pos] = (int32_t)(kbase + (uint32_t)i);
-                gsum[pos] = sm;
-                gcnt[pos] = (long long)(e[r] >> shift);
-            }
-            dense[i] = 0ull;
-        }
-        base += s_tot;
-        __syncthreads();
-    }
+    gbd_chunk_write(dense, extra, ck, s_base, kbase, xtra, shift, gkey, gsum, gcnt, cap, s_off, &s_tot);
 }
 
 }  // namespace
@@ -757,7 +714,7 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
     QG_TRY(qg_scratch(ctx, lst_b + GBD_SAMPLE_CTAS * 4, &scr));
     uint32_t *lst = (uint32_t *)scr, *lcnt = (uint32_t *)(scr + lst_b);
     qg_lookback lb;
-    QG_TRY(qg_lb_make(ctx, GBD_EMIT_TILES, QG_SITE_GROUPBY, &lb));
+    QG_TRY(qg_lb_make(ctx, ctx->sm_count, QG_SITE_GROUPBY, &lb));
     uint32_t *st = ctx->ctl->gbd;
 
     const int C = ctx->sm_count;
@@ -843,9 +800,8 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
     }
     if (s == QG_OK) {
         qg_pre_launch(ctx);
-        k_gbd_emit<<<GBD_EMIT_TILES, GBD_EMIT_THREADS, 0, ctx->stream>>>(
-            dense, extra, img, (uint4 *)sketch, st, shift, gkey, (long long *)gsum, (long long *)gcnt, cap, d_num,
-            lb);
+        k_gbd_emit<<<C, GBD_THREADS, 0, ctx->stream>>>(dense, extra, img, sketch, st, shift, gkey, (long long *)gsum,
+                                                       (long long *)gcnt, cap, d_num, lb);
         s = qg_check_launch(ctx, "k_gbd_emit");
     }
     if (s != QG_OK) ctx->table_dirty = true;  // the dense table may hold partial sums
