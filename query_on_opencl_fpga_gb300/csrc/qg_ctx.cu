@@ -336,6 +336,7 @@ static qg_status map_error(qg_ctx *ctx, const int32_t *h) {
     // group-by table mid-way: reset them (in stream order).
     cudaMemsetAsync(&ctx->ctl->err, 0, 2 * sizeof(int32_t), ctx->stream);
     cudaMemsetAsync(&ctx->ctl->tile_ctr, 0, 2 * sizeof(uint32_t), ctx->stream);
+    cudaMemsetAsync(ctx->ctl->gbd, 0, sizeof(ctx->ctl->gbd), ctx->stream);  // dense group-by state words
     cudaStreamSynchronize(ctx->stream);  // done before any later stream of this context runs
     ctx->table_dirty = true;
     snprintf(ctx->msg, sizeof(ctx->msg), "device error %d (%s) at site %d", h[0],

@@ -134,6 +134,17 @@ k_gbd_sample(const int32_t *__restrict__ key, long long n, int runs, bool every_
     }
     if (threadIdx.x == 0) s_n = 0;
     if (threadIdx.x < 2) s_mm[threadIdx.x] = threadIdx.x == 0 ? 0xffffffffu : 0u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // The call's state words that later kernels set start at zero; the
+        // sampled key range was cleared by the previous call's candidates
+        // kernel (or the context's creation), so no memset precedes this.
+        st[G_OK] = 0;
+        st[G_KBASE] = 0;
+        st[G_NUMIN] = 0;
+        st[G_UMAX] = 0;
+        st[G_OUTSIDE] = 0;
+        st[G_EXTRA] = 0;
+    }
     uint32_t k[2];
     bool have[2];
 #pragma unroll
@@ -217,6 +228,8 @@ k_gbd_cands(const uint32_t *__restrict__ sketch, const uint32_t *__restrict__ ls
         if (c[j] >= min_count && c[j] > 0) atomicMax(img + gbd_slot(kk[j]), ((unsigned long long)c[j] << 32) | kk[j]);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const uint32_t smin = ~st[G_NSMIN], smax = st[G_SMAX];
+        st[G_NSMIN] = 0;  // cleared for the next call's sample (nothing else reads them)
+        st[G_SMAX] = 0;
         if (smin <= smax) {
             const unsigned long long span = (unsigned long long)(smax - smin) + 1ull;
             if (span <= GBD_W / 2) {
@@ -650,6 +663,10 @@ k_gbd_single(const int32_t *__restrict__ key, const int32_t *__restrict__ val, c
         if (c >= min_count) atomicMax(img + gbd_slot(kk), ((unsigned long long)c << 32) | kk);
     }
     if (!gbd_grid_sync(&st[G_BAR], 2 * C, spin_limit, ctl, &s_ok)) return;
+    if (b == 0 && tid == 0) {  // every CTA has read the sampled key range: cleared for a four-launch call
+        st[G_NSMIN] = 0;
+        st[G_SMAX] = 0;
+    }
 
     // C. main pass
     if (ok) gbd_main_body<PRED>(key, val, val2, lo2, hi2, n, img, kbase, st, dense, extra, shift, fast_max,
@@ -736,7 +753,6 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
                     "attr");
         attr_main[pred] = smem_main;
     }
-    QG_TRY_CUDA(ctx, cudaMemsetAsync(st, 0, G_WORDS * 4, ctx->stream), "memset gbd state");
 
     const bool every_row = n <= (long long)GBD_SAMPLE_RUNS * GBD_RUN;
     const int runs = every_row ? (int)qg_ceil_div(n, GBD_RUN) : GBD_SAMPLE_RUNS;
@@ -759,6 +775,7 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
             single_fits[pred] = nb >= 1;
         }
         if (single_fits[pred]) {
+            QG_TRY_CUDA(ctx, cudaMemsetAsync(st, 0, G_WORDS * 4, ctx->stream), "memset gbd state");
             uint32_t *counts = (uint32_t *)scr;  // [C] groups per emit chunk (the sample lists are unused)
             bool er = every_row;
             int32_t l2 = lo2, h2 = hi2;
