@@ -433,16 +433,31 @@ k_pj_dhist(const unsigned long long *__restrict__ rec, long long n, qg_part_fn p
     qg_cdf_head hd{};
     if (LEARNED) hd = qg_cdf_load_head<true>(sm);
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const uint32_t u = (uint32_t)(__ldg(rec + i) >> 32);
-        const uint32_t b = LEARNED ? qg_cdf_bucket_h<true>(sm, hd, u) : qg_part_bucket(pf, u);
+    auto count = [&](long long i, uint32_t b) {
         if (b >= nb) {  // a key outside the partition function's domain
             qg_record_error(ctl, QG_ERR_INVALID, QG_SITE_PJ_HIST);
-            continue;
+            return;
         }
         if (bid) bid[i] = (uint16_t)b;  // nb <= 2^16: the id for the partition passes
         atomicAdd(&h[0][b & 255u], 1u);
         atomicAdd(&h[1][b >> 8], 1u);
+    };
+    // Four rows per thread and round: their loads, then their buckets (four
+    // independent model evaluations), then their counts.
+    constexpr int U = 4;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + (U - 1) * stride < n; i += U * stride) {
+        uint32_t u[U], b[U];
+#pragma unroll
+        for (int j = 0; j < U; j++) u[j] = (uint32_t)(__ldg(rec + i + j * stride) >> 32);
+#pragma unroll
+        for (int j = 0; j < U; j++) b[j] = LEARNED ? qg_cdf_bucket_h<true>(sm, hd, u[j]) : qg_part_bucket(pf, u[j]);
+#pragma unroll
+        for (int j = 0; j < U; j++) count(i + j * stride, b[j]);
+    }
+    for (; i < n; i += stride) {
+        const uint32_t u = (uint32_t)(__ldg(rec + i) >> 32);
+        count(i, LEARNED ? qg_cdf_bucket_h<true>(sm, hd, u) : qg_part_bucket(pf, u));
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 512; i += blockDim.x)
