@@ -481,12 +481,37 @@ __global__ void k_pj_bounds(const unsigned long long *__restrict__ rec, long lon
 
 // Bucket counts of the key sample under a partition function (global atomics;
 // the sample has at most 2^20 keys).
-__global__ void k_pj_smp_hist(const unsigned long long *__restrict__ smp, long long m, qg_part_fn pf,
-                              uint32_t nb, uint32_t *__restrict__ counts) {
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m;
-         i += (long long)gridDim.x * blockDim.x) {
-        const uint32_t b = qg_part_bucket(pf, (uint32_t)(__ldg(smp + i) >> 32));
-        if (b < nb) atomicAdd(&counts[b], 1u);
+// The sample is sorted, so neighbouring lanes mostly share a bucket: one add
+// per bucket and warp (peers found by a match instruction) instead of one per
+// key onto the same L2 word.  A learned function is evaluated from a
+// shared-memory copy of the model.
+template <bool LEARNED>
+__global__ void __launch_bounds__(256)
+k_pj_smp_hist(const unsigned long long *__restrict__ smp, long long m, qg_part_fn pf, uint32_t nb,
+              uint32_t *__restrict__ counts) {
+    __shared__ __align__(16) unsigned char sm_model[LEARNED ? sizeof(qg_cdf_model) : 16];
+    if (LEARNED) {
+        const uint32_t *gsrc = reinterpret_cast<const uint32_t *>(pf.model);
+        uint32_t *sdst = reinterpret_cast<uint32_t *>(sm_model);
+        for (int i = threadIdx.x; i < (int)(sizeof(qg_cdf_model) / 4); i += blockDim.x) sdst[i] = __ldg(gsrc + i);
+        __syncthreads();
+    }
+    const qg_cdf_model *sm = reinterpret_cast<const qg_cdf_model *>(sm_model);
+    qg_cdf_head hd{};
+    if (LEARNED) hd = qg_cdf_load_head<true>(sm);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // whole warps through every round, so the match sees all 32 lanes
+    const long long m32 = (m + 31) & ~31ll;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m32; i += stride) {
+        uint32_t b = 0xffffffffu;
+        if (i < m) {
+            const uint32_t u = (uint32_t)(__ldg(smp + i) >> 32);
+            b = LEARNED ? qg_cdf_bucket_h<true>(sm, hd, u) : qg_part_bucket(pf, u);
+            if (b >= nb) b = 0xffffffffu;
+        }
+        const uint32_t peers = __match_any_sync(QG_FULL_MASK, b);
+        if (b != 0xffffffffu && (threadIdx.x & 31) == (uint32_t)(__ffs(peers) - 1))
+            atomicAdd(&counts[b], (uint32_t)__popc(peers));
     }
 }
 
@@ -1719,10 +1744,11 @@ qg_status pj_compare(qg_ctx *ctx, const PjLevel &L, long long m, long long ntot,
                    double *over_learned) {
     QG_TRY_CUDA(ctx, cudaMemsetAsync(L.scnt, 0, (size_t)2 * nb * 4, ctx->stream), "memset scnt");
     qg_pre_launch(ctx);
-    k_pj_smp_hist<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(L.smp, m, radix, nb_radix, L.scnt);
+    k_pj_smp_hist<false><<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(L.smp, m, radix, nb_radix, L.scnt);
     QG_TRY(qg_check_launch(ctx, "k_pj_smp_hist"));
     qg_pre_launch(ctx);
-    k_pj_smp_hist<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(L.smp, m, learned, nb, L.scnt + nb);
+    auto kl = learned.learned ? k_pj_smp_hist<true> : k_pj_smp_hist<false>;
+    kl<<<pj_grid(ctx, m, 256, 4), 256, 0, ctx->stream>>>(L.smp, m, learned, nb, L.scnt + nb);
     QG_TRY(qg_check_launch(ctx, "k_pj_smp_hist"));
     std::vector<uint32_t> c((size_t)2 * nb);
     QG_TRY_CUDA(ctx, cudaMemcpyAsync(c.data(), L.scnt, c.size() * 4, cudaMemcpyDeviceToHost, ctx->stream), "scnt d2h");
