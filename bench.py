@@ -700,14 +700,23 @@ def run_only(args):
         n = rows or (1 << 26)
         from query_on_opencl_fpga_gb300.datagen import records, uniform_i32
 
-        rec = records(uniform_i32(n, 0, 1 << 20, 0, "cuda"))
-        fn = lambda: ctx.sort_rec(rec)  # noqa: E731
+        # every call sorts a fresh copy of the unsorted records (re-sorting the
+        # sorted output would favour the ranking); ms_per_op includes that
+        # copy, kernels_ms_per_op does not
+        base = records(uniform_i32(n, 0, 1 << 20, 0, "cuda"))
+        rec = torch.empty_like(base)
+
+        def fn():
+            rec.copy_(base)
+            ctx.sort_rec(rec)
     else:
         raise SystemExit(f"unknown --only {args.only}")
     if args.variant >= 0 and args.only == "filter":
         ctx.check(ctx.lib.qg_filter_set_variant(args.variant), "qg_filter_set_variant")
     if args.variant >= 0 and args.only in ("groupby", "fused"):
         ctx.check(ctx.lib.qg_groupby_set_knobs(args.variant, 13, 0, 0), "qg_groupby_set_knobs")
+    if args.variant >= 0 and args.only == "sort":
+        ctx.check(ctx.lib.qg_sort_set_rank(args.variant), "qg_sort_set_rank")
     if args.gb_launches:
         ctx.groupby_set_single_launch(args.gb_launches == 1)
     ms, kern, launches = timed(ctx, fn, args.steps, args.warmup, 1, stream)
@@ -725,7 +734,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default=None, help="groupby|fused|filter|join|skew|sort|batched: one operator alone")
     ap.add_argument("--rows", type=int, default=0, help="row count for --only (default: the config size)")
-    ap.add_argument("--variant", type=int, default=-1, help="column filter kernel variant for --only filter")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="--only filter: kernel variant; groupby/fused: knob mode; sort: ranking form (0, 3, 4)")
     ap.add_argument("--rows2", type=int, default=0, help="build-side rows for --only join")
     ap.add_argument("--gb-launches", type=int, default=0, choices=[0, 1, 4],
                     help="group-by: the dense-window steps as one cooperative launch (1) or four (4); 0: the library default")

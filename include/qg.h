@@ -144,11 +144,10 @@ QG_API qg_status qg_scan_excl_i32(qg_ctx *ctx, const int32_t *in, int32_t *out, 
  * keys is unspecified, as in the reference. */
 QG_API qg_status qg_sort_rec_by_y(qg_ctx *ctx, void *records, int64_t n);
 /* Stable ranking of the radix passes whose digits take many values
- * (process-wide): -1 (default) by caller -- sorts mode 4, the join's
- * partition passes mode 3 (each measured faster there); 0 eight warp
- * ballots; 3 one match instruction on a digit's high four bits and four
- * ballots on its low four; 4 one match instruction on each half.  Results are
- * identical. */
+ * (process-wide): -1 (default) mode 3, measured fastest for sorts of unsorted
+ * input and the join's partition passes; 0 eight warp ballots; 3 one match
+ * instruction on a digit's high four bits and four ballots on its low four;
+ * 4 one match instruction on each half.  Results are identical. */
 QG_API qg_status qg_sort_set_rank(int mode);
 
 /* ---- group-by on Records (host/host/testGroupBy.cpp:81-154) ---------- */

@@ -416,12 +416,13 @@ static qg_status rs_set_attr(qg_ctx *ctx) {
 // sort of 20-bit keys, 1.30 -> 1.22 ms over its passes), while passes with
 // many digit values were slower with it (the join's partition passes 1.10 ->
 // 1.38 ms) and keep the eight ballots.
-// Stable ranking of the passes with many digit values: -1 by caller, else
-// forced -- 0 eight ballots, 3 a match on the high four bits and four ballots,
-// 4 a match on each half (ANDed).  Measured on GB300: the 64M-record sort's
-// passes took 1.222 / 1.137 / 1.098 ms with 0 / 3 / 4, the join's stable
-// partition pass 0.778 / 0.766 / 0.855 ms; so sorts take 4 and the join's
-// partition passes 3.
+// Stable ranking of the passes with many digit values: -1 the default (3),
+// else forced -- 0 eight ballots, 3 a match on the high four bits and four
+// ballots, 4 a match on each half (ANDed).  Measured on GB300 with 0 / 3 / 4:
+// the 64M-record sort of a fresh unsorted copy, passes 1.290 / 1.265 /
+// 1.437 ms; the join's stable partition pass 0.778 / 0.766 / 0.855 ms.  (Form
+// 4 had looked fastest when the sort was timed re-sorting its own sorted
+// output, where a warp's items share their high digits.)
 static int g_rs_stable_rank = -1;
 
 extern "C" QG_API qg_status qg_sort_set_rank(int mode) {
@@ -472,8 +473,7 @@ qg_status qg_radix_passes_pf(qg_ctx *ctx, bool kv3, qg_sort_bufs a, qg_sort_bufs
         const int shift = (pf.learned || side) ? 8 * p : pf.shift + 8 * p;
         const bool m = rs_few_digits(h_bases + p * QG_RADIX, n);
         // the first pass of a caller that needs only the grouping need not be stable
-        // the join's partitions (first_unstable) rank with 3, sorts with 4
-        const int sr = g_rs_stable_rank >= 0 ? g_rs_stable_rank : (first_unstable ? 3 : 4);
+        const int sr = g_rs_stable_rank >= 0 ? g_rs_stable_rank : 3;
         const int rk = (first_unstable && i == 0 && !kv3) ? 2 : (m ? 1 : sr);
         auto kern = kv3 ? (m ? k_radix_pass<true, 0, 1> : sr == 3 ? k_radix_pass<true, 0, 3> : sr == 4 ? k_radix_pass<true, 0, 4> : k_radix_pass<true, 0, 0>)
                     : side ? (rk == 2 ? k_radix_pass<false, 2, 2> : rk == 1 ? k_radix_pass<false, 2, 1> : rk == 3 ? k_radix_pass<false, 2, 3> : rk == 4 ? k_radix_pass<false, 2, 4> : k_radix_pass<false, 2, 0>)
