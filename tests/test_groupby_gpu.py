@@ -301,6 +301,41 @@ def test_groupby_dense_single_and_four_launches(ctx, orc, n, single):
         ctx.groupby_set_single_launch(False)
 
 
+@pytest.mark.parametrize("single", [0, 1])
+def test_groupby_dense_timeout_reports_and_recovers(ctx, orc, single):
+    # Poll limit 0: the emit's look-back over its chunks (four launches) gives
+    # up at once and the call reports a timeout; the single launch's grid
+    # barriers give up unless every CTA has already arrived.  Either way no
+    # hang and no fault, and the next call with the default limit is exact
+    # (the error path re-zeroes the table arena and the state words).
+    from query_on_opencl_fpga_gb300 import QGError
+
+    rng = np.random.default_rng(77)
+    n = 1 << 22
+    key = (rng.zipf(1.2, n) % 100000).astype(np.int32)
+    val = rng.integers(0, 1000, n).astype(np.int32)
+    exp = orc.groupby_cols(key, val, None, 0, 0)
+    ctx.groupby_set_single_launch(bool(single))
+    try:
+        ctx.set_spin_limit(0)
+        try:
+            if single:
+                try:
+                    check_groups(ctx.groupby_cols(dev(key), dev(val), None, 0, 0, cap=n), exp)
+                except QGError as e:
+                    assert e.status == 5
+            else:
+                with pytest.raises(QGError) as e:
+                    ctx.groupby_cols(dev(key), dev(val), None, 0, 0, cap=n)
+                assert e.value.status == 5
+        finally:
+            ctx.set_spin_limit(1 << 22)
+        for _ in range(2):
+            _dense_case(ctx, orc, key, val, path="dense")
+    finally:
+        ctx.groupby_set_single_launch(False)
+
+
 @pytest.mark.parametrize("n,nkeys,vmax", [(1 << 22, 8, 600_000), (1 << 20, 4, 1 << 23), (1 << 22, 1, None)])
 def test_groupby_dense_heavy_slot_bounds(ctx, orc, n, nkeys, vmax):
     # A few keys take every row, so each CTA's heavy-key slots take thousands
