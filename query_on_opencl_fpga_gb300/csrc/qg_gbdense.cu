@@ -761,7 +761,7 @@ qg_status qg_gbd_launch(qg_ctx *ctx, const int32_t *key, const int32_t *val, con
     // One cooperative launch when every SM can hold one CTA and the stream is
     // not being captured (graphs take the four launches below).
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    QG_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs), "capture status");
+    if (g_gbd_single) QG_TRY_CUDA(ctx, cudaStreamIsCapturing(ctx->stream, &cs), "capture status");
     static int single_fits[2] = {-1, -1};
     if (g_gbd_single && n > 0 && cs == cudaStreamCaptureStatusNone && C >= 128 &&
         (long long)C * GBD1_MAX_RUNS >= runs) {
